@@ -1,0 +1,343 @@
+"""Benchmark: GB energy + force evaluations per second on seeded synthetic
+globules (default: GBSW, 50,000 atoms, 32-point Gauss-Legendre x 110-point
+Lebedev quadrature, full N^2 pair term).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gb300|reference]
+
+A step is one energy + force evaluation of the whole molecule.
+* value: evaluations/s with positions resident in HBM (gbx_execute on device
+  buffers), timed with CUDA events on the library's execute stream, L2
+  flushed (256 MiB write) between timed steps, max over ranks.
+* e2e: the same metric through the host-buffer call (gbx_execute_host):
+  positions copied host->device and forces/energy device->host every step.
+* roofline: the dominant stage, from events the library records around each
+  stage on its own stream, against the FP32 pipe (the path has no dense
+  contraction and moves a few MB per step).
+* cpu_baseline: the FP64 oracle (a restatement of the reference CPU
+  algorithm) on the machine's host cores for the same workload.
+
+Multi-GPU: replicas (the path does not shard on one node here); each rank
+evaluates its own copy and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+from openmmcustomgbintegralforce_gb300.globule import make_globule  # noqa: E402
+from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for  # noqa: E402
+
+METRIC = "GB energy+force evals/s at 50k atoms; batched confs/s vs plain; err vs FP64"
+UNIT = "evals/s"
+
+# Algorithmic FP32 work per unit, counted op by op from the reference formulas
+# (FMA = 2 flops; sqrt / exp / reciprocal counted separately as SFU ops).
+# GBSW volume evaluation (CharmmReferenceGBSW.cpp:616-639): delta 3, r^2 5,
+# shell bounds 2 -> 10 flops + 1 sqrt; inside the switching shell dr 1,
+# dr^2 dr^3 2, cubic 4, product 1 -> +8 flops.
+FLOPS_GBSW_EVAL = 10.0
+FLOPS_GBSW_SHELL = 8.0
+# per quadrature point: point = x + v 3, cell index 6, two weighted sums 4
+FLOPS_POINT = 13.0
+# unique pair (CharmmReferenceGBSW.cpp:248-282): delta+r^2 8, D 3, exp arg 1,
+# f^2 2, 1/f^3 2, energy 3, dG/dr 4 + force 6, dG/dB 2x5 -> 39 flops + exp, rsqrt
+FLOPS_PAIR = 39.0
+
+
+def workloads():
+    return {
+        "gbsw50k": dict(n=50000, seed=2026, model=GBModel.charmm_gbsw(n_radial=32, lebedev=110),
+                        desc="GBSW 50,000-atom globule, 32x110 quadrature, full N^2 pair term"),
+        "gbsw50k_cutoff": dict(n=50000, seed=2026, model=GBModel.charmm_gbsw(n_radial=32, lebedev=110, cutoff=2.0),
+                               desc="GBSW 50,000-atom globule, 32x110 quadrature, 2.0 nm pair cutoff"),
+        "gbmv10k": dict(n=10000, seed=2027, model=None, gbmv=2,
+                        desc="GBMV-II 10,000-atom globule, 24x50 quadrature"),
+        "gbsw1k": dict(n=1000, seed=7, model=GBModel.charmm_gbsw(),
+                       desc="GBSW 1,000-atom globule, 24x38 quadrature (reference CPU case)"),
+    }
+
+
+def model_for(w, g):
+    if w.get("model") is not None:
+        return w["model"]
+    box = box_for(g.positions, margin=1.0)
+    if w["gbmv"] == 1:
+        return GBModel.gbmv1(box=box, lebedev=50)
+    return GBModel.gbmv2(box=box, lebedev=50)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_baseline(model, g, sample_s: float = 20.0):
+    """Time the FP64 oracle (restated reference algorithm) on host cores."""
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    out = O.Oracle(model, nthreads=cores).energy_forces(g.positions, g.charge, g.radius)
+    dt = time.perf_counter() - t0
+    return out, dt, cores
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the FP64 oracle port of the reference CPU algorithm
+    (the reference's own classes need the reference tree, absent on the GPU
+    host, and O(N^2) memory: 60 GB at 50k atoms)."""
+    if rank != 0:
+        return
+    w = workloads()[args.workload]
+    g = make_globule(w["n"], seed=w["seed"])
+    model = model_for(w, g)
+    times = []
+    for k in range(args.warmup + args.steps):
+        out, dt, cores = oracle_baseline(model, g)
+        if k >= args.warmup:
+            times.append(dt)
+    v = 1.0 / float(np.mean(times))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded globule", "config": {"workload": args.workload, "desc": w["desc"],
+                                                           "atoms": w["n"], "quadrature_points": model.n_quad},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"full evaluation of the workload ({w['n']} atoms) per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="gbsw50k", choices=sorted(workloads()))
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_CHECK, EXEC_COUNT_WORK, EXEC_ENERGY, EXEC_FORCES, Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workloads()[args.workload]
+    g = make_globule(w["n"], seed=w["seed"])
+    model = model_for(w, g)
+    n = g.n
+    ctx = Context(model, n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    stride = ((n + 31) // 32) * 32
+    posq = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    posq[:, :3] = torch.from_numpy(g.positions.astype(np.float32)).to(dev)
+    force = torch.zeros(3 * stride, dtype=torch.int64, device=dev)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def step(flags):
+        ctx.execute_device(posq.data_ptr(), force.data_ptr(), stride, energy.data_ptr(), flags, sptr)
+
+    for _ in range(max(args.warmup, 3)):
+        step(EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK)
+    torch.cuda.synchronize()
+
+    # timed region: device-resident inputs
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            starts[k].record(stream)
+            step(EXEC_FORCES | EXEC_ENERGY)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = allmax(world, float(np.mean(step_ms)))
+    value = world * 1000.0 / ms
+
+    # stage breakdown (events recorded by the library on its stream)
+    ctx.set_timing(True)
+    stages = []
+    for k in range(5):
+        flush.fill_(1.0)
+        step(EXEC_FORCES | EXEC_ENERGY)
+        torch.cuda.synchronize()
+        stages.append(ctx.stage_times())
+    ctx.set_timing(False)
+    stage_ms = {k: float(np.median([s[k] for s in stages])) for k in stages[0]}
+
+    # algorithmic work of this workload (counted on the device, reference order)
+    step(EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK | EXEC_COUNT_WORK)
+    torch.cuda.synchronize()
+    work = ctx.work()
+
+    peaks, peak_src = measured_peaks()
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
+    points = float(n) * model.n_quad
+    integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
+        FLOPS_POINT * points
+    pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
+    cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
+            "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12}
+    dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
+    achieved = cand.get(dominant)
+    roofline = {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                "peak_source": "nominal FP32 (152 SM x 128 lanes x 2 flop x max SM clock); "
+                               f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
+                "per_stage_tflops": cand, "stage_ms": stage_ms,
+                "work": {"volume_evals": work["volume_evals"], "shell_evals": work["shell_evals"],
+                         "points": points, "pairs": n * (n - 1) / 2.0}}
+
+    # e2e: host buffers through gbx_execute_host (copies inside the timed region)
+    for _ in range(2):
+        ctx.execute_host(g.positions)
+    e2e_times = []
+    for k in range(max(3, args.steps // 2)):
+        flush.fill_(2.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E_gpu, F_gpu = ctx.execute_host(g.positions)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = allmax(world, 1000.0 * float(np.mean(e2e_times)))
+    e2e = {"value": world * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+           "d2h_bytes_per_step": n * 3 * 8 + 8, "ms_per_step": e2e_ms}
+
+    cpu = None
+    err = None
+    if rank == 0 and not args.no_cpu_baseline:
+        out, dt, cores = oracle_baseline(model, g)
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"one full FP64 evaluation of the workload ({n} atoms, {model.n_quad} points) "
+                         f"with OpenMP on all host cores, {dt:.1f} s"}
+        err = {"energy_rel": abs(E_gpu / out["energy"] - 1.0),
+               "force_rel_rms": float(np.sqrt(((F_gpu - out["forces"]) ** 2).sum() / (out["forces"] ** 2).sum()))}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded globule (no dataset)",
+                "config": {"workload": args.workload, "desc": w["desc"], "atoms": n,
+                           "quadrature_points": model.n_quad, "l2": "flushed (256 MiB write) between steps",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "gpu_launches": 14, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "err_vs_fp64": err, "clocks": clk, "wall_s": wall}
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * gbx -- GB300-native CHARMM GBSW / GBMV implicit-solvent energy and forces.
+ *
+ * Plain C ABI over the CUDA implementation (sm_103a).  No C++ or torch types
+ * cross this boundary: handles are opaque, arrays are raw pointers with
+ * explicit sizes, every call returns a gbx_status and never throws.
+ *
+ * One gbx_context plays the role of one instance of the reference's kernel
+ * objects: it is what CalcCharmmGBSWForceKernel / CalcCharmmGBMVForceKernel
+ * (openmmapi/include/openmm/charmmKernels.h:49-129) hold between
+ * initialize(), execute() and copyParametersToContext().  An OpenMM plugin
+ * adapter is a thin C++ layer that forwards those three
+ * virtuals to the calls below.
+ *
+ * Units: nm, e, kJ/mol.  Device buffers follow OpenMM's CUDA conventions:
+ * positions as float4 (x, y, z, unused), forces as 64-bit fixed point
+ * (value * 2^32, two's complement) laid out [x(stride) | y(stride) | z(stride)].
+ */
+#ifndef GBX_H
+#define GBX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define GBX_API __declspec(dllexport)
+#else
+#define GBX_API __attribute__((visibility("default")))
+#endif
+
+typedef struct gbx_context gbx_context;
+typedef struct gbx_batch gbx_batch;
+
+typedef enum {
+  GBX_OK = 0,
+  GBX_ERR_INVALID_ARGUMENT = 1,
+  GBX_ERR_CUDA = 2,
+  GBX_ERR_OUT_OF_MEMORY = 3,
+  GBX_ERR_UNSUPPORTED = 4,
+  GBX_ERR_NONFINITE = 5,      /* a Born radius or the energy came out NaN/Inf */
+  GBX_ERR_TABLE_TOO_LARGE = 6, /* lookup grid would exceed its limits (reference: length > 1000 nm) */
+  GBX_ERR_NOT_READY = 7,      /* result queried before an execute */
+  GBX_ERR_TIMEOUT = 8         /* a device-side wait gave up (batched persistent kernel) */
+} gbx_status;
+
+/* Volume models: CharmmGBMVForce::GBIntegralType (CharmmGBMVForce.h:99-104). */
+enum { GBX_MODEL_GBSW = 0, GBX_MODEL_GBMV1 = 1, GBX_MODEL_GBMV2 = 2 };
+
+/* Lookup-table semantics. */
+enum {
+  GBX_TABLE_STANDALONE = 0, /* CharmmReferenceGBSW.cpp:440-552: grid points, uniform pad, uncapped */
+  GBX_TABLE_GRID = 1,       /* CustomGBIntegral.cpp:162-228,310-324: grid points, per-atom pad, capped */
+  GBX_TABLE_PERIODIC = 2    /* CustomGBIntegral.cpp:45-160,284-309: box grid, sampled membership, capped */
+};
+
+/* Presets reproducing the reference's native settings. */
+enum {
+  GBX_PRESET_CHARMM_GBSW = 0,   /* CharmmGBSWForce, Reference platform */
+  GBX_PRESET_GBSW_INTEGRAL = 1, /* CharmmGBMVForce + GBSWIntegral */
+  GBX_PRESET_GBMV1 = 2,         /* CharmmGBMVForce + GBMVIntegralTypeI */
+  GBX_PRESET_GBMV2 = 3          /* CharmmGBMVForce + GBMVIntegralTypeII */
+};
+
+/* Execute flags. */
+enum {
+  GBX_EXEC_FORCES = 1,  /* includeForces  */
+  GBX_EXEC_ENERGY = 2,  /* includeEnergy  */
+  GBX_EXEC_CHECK = 4,   /* synchronise the stream and report device status (table
+                           capacity, non-finite values); grows buffers and
+                           re-runs once if a capacity limit was hit */
+  GBX_EXEC_COUNT_WORK = 8 /* count (point, listed atom) evaluations (gbx_get_work) */
+};
+
+typedef struct {
+  int model;            /* GBX_MODEL_* */
+  int n_radial;         /* Gauss-Legendre points on [r0, r1] */
+  int lebedev_order;    /* 6, 14, 26, 38, 50, 74, 86 or 110 */
+  double r0, r1;        /* radial integration range (nm) */
+  int table_mode;       /* GBX_TABLE_* */
+  int table_cap;        /* per-cell cap (<= 0: uncapped) */
+  double grid_length;   /* lookup grid spacing h (nm) */
+  double table_buffer;  /* buffer length (nm) */
+  double box[3];        /* periodic box edge lengths (GBX_TABLE_PERIODIC) */
+  double switch_width;  /* GBSW half-width w (nm) */
+  double gamma0, beta, lambda, p1, p2, s0; /* GBMV constants */
+  double alpha0, alpha1; /* Born-radius coefficients (global parameters) */
+  double prefactor;     /* pair prefactor, -ONE_4PI_EPS0 (1 - 1/80) by default */
+  double cutoff;        /* <= 0: full N^2 pair term */
+  int cutoff_chain_quirk; /* drop chain terms beyond the cutoff (CharmmReferenceGBSW.cpp:291-292) */
+  int skip_empty;       /* GBSW: an empty list means V = 1 */
+  int reserved[8];
+} gbx_config;
+
+/* Library / error helpers. */
+GBX_API const char* gbx_status_string(gbx_status s);
+GBX_API int gbx_version(void);
+
+/* Fill *cfg with a preset (reference constants: CharmmReferenceGBSW.cpp:20-52,
+ * GBSWIntegral.cpp:24-61, GBMVIntegralTypeI.cpp:18-57, GBMVIntegralTypeII.cpp:19-62). */
+GBX_API gbx_status gbx_config_preset(int preset, gbx_config* cfg);
+
+/* Create a context for num_atoms particles on the current CUDA device.
+ * Replaces CalcCharmmGBSWForceKernel::initialize / CalcCharmmGBMVForceKernel::initialize
+ * (charmmKernels.h:71,111; CharmmCudaKernels.cpp:136-843). */
+GBX_API gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out);
+GBX_API gbx_status gbx_destroy(gbx_context* ctx);
+GBX_API gbx_status gbx_last_error(const gbx_context* ctx, char* buf, size_t len);
+
+/* Per-particle charge (e) and input radius (nm).  Replaces
+ * copyParametersToContext (charmmKernels.h:88,128; CharmmReferenceKernels.cpp:439-458). */
+GBX_API gbx_status gbx_set_particle_parameters(gbx_context* ctx, const double* charge, const double* radius);
+/* Global parameters alpha0, alpha1 (the GBMV force's computed-value globals). */
+GBX_API gbx_status gbx_set_global_parameters(gbx_context* ctx, double alpha0, double alpha1);
+/* Periodic box edges (nm) for GBX_TABLE_PERIODIC. */
+GBX_API gbx_status gbx_set_box(gbx_context* ctx, const double box[3]);
+
+/* Energy and forces on device buffers.  Replaces CalcCharmmGB*ForceKernel::execute
+ * (charmmKernels.h:81,121; CharmmCudaKernels.cpp:845-993).  posq: float4[num_atoms]
+ * on the device.  force_fixed: fixed-point buffer, ADDED to, components at
+ * [0, stride), [stride, 2 stride), [2 stride, 3 stride).  energy: one double on
+ * the device, ADDED to.  Either may be NULL when not requested by flags. */
+GBX_API gbx_status gbx_execute(gbx_context* ctx, const void* posq, unsigned long long* force_fixed,
+                               int force_stride, double* energy, int flags, void* stream);
+
+/* Same computation on host arrays (Reference-platform style): positions
+ * double[3n]; forces double[3n] ADDED to; *energy set.  Copies inside. */
+GBX_API gbx_status gbx_execute_host(gbx_context* ctx, const double* positions, double* forces, double* energy,
+                                    int flags);
+
+/* Results of the last execute, copied to host: Born radii (nm), integrals
+ * I4/I7 [2n], dE/dB [n]. */
+GBX_API gbx_status gbx_get_born_radii(gbx_context* ctx, double* born);
+GBX_API gbx_status gbx_get_integrals(gbx_context* ctx, double* integrals);
+GBX_API gbx_status gbx_get_dEdB(gbx_context* ctx, double* dEdB);
+
+/* Lookup table of the last execute (or built by gbx_build_lookup_table):
+ * dims, min corner, steps and the per-cell lists in ascending atom order.
+ * Pass NULL arrays to query sizes first. */
+GBX_API gbx_status gbx_build_lookup_table(gbx_context* ctx, const void* posq, void* stream);
+GBX_API gbx_status gbx_get_lookup_table(gbx_context* ctx, int dims[3], double min[3], double step[3],
+                                        int64_t* ncell, int32_t* counts, int64_t* total, int32_t* atoms);
+
+/* Adjoint: dE/dx (as forces), dE/dq [n], dE/dR_in [n], dE/dalpha [2].  The
+ * per-point volumes are recomputed, not stored.  No counterpart in the
+ * reference, which only returns forces; it carries the same chain rule
+ * (CharmmReferenceGBSW.cpp:597-674) to the parameters.  Host arrays. */
+GBX_API gbx_status gbx_adjoint_host(gbx_context* ctx, const double* positions, double* energy, double* forces,
+                                    double* dEdq, double* dEdR, double* dEdalpha);
+
+/* Work counters of the last execute run with GBX_EXEC_COUNT_WORK: (point,
+ * listed atom) evaluations, of which inside a GBSW switching shell, and
+ * ordered pairs.  Diagnostics for roofline accounting; no counterpart in the
+ * reference. */
+GBX_API gbx_status gbx_get_work(gbx_context* ctx, double* volume_evals, double* shell_evals, double* pairs);
+
+/* Per-stage device times (ms) of the last execute, from CUDA events recorded
+ * on the execute stream when timing is enabled.  Stages: 0 position staging,
+ * 1 lookup table, 2 integrals, 3 Born radii, 4 pair term, 5 chain prep,
+ * 6 chain rule, 7 energy reduction.  Diagnostics; no counterpart in the
+ * reference. */
+GBX_API gbx_status gbx_set_timing(gbx_context* ctx, int enable);
+GBX_API gbx_status gbx_get_stage_times(gbx_context* ctx, double* ms, int max_stages, int* num_stages);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBX_H */

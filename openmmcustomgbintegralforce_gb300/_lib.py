@@ -1,0 +1,254 @@
+"""ctypes binding of the gbx C ABI (``include/gbx.h``, ``lib/libgbx.so``).
+
+There is no fallback: if the CUDA library is missing or no GPU is present,
+calls raise.  The library is built in-tree by ``build.py``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .spec import GBModel
+
+GBX_OK = 0
+STATUS_NAMES = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported",
+    5: "non-finite result", 6: "lookup table too large", 7: "no result yet", 8: "device wait timed out",
+}
+EXEC_FORCES, EXEC_ENERGY, EXEC_CHECK, EXEC_COUNT_WORK = 1, 2, 4, 8
+
+# every symbol include/gbx.h declares
+EXPORTED = (
+    "gbx_status_string", "gbx_version", "gbx_config_preset", "gbx_create", "gbx_destroy", "gbx_last_error",
+    "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
+    "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
+    "gbx_adjoint_host", "gbx_get_work", "gbx_set_timing", "gbx_get_stage_times",
+)
+STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
+          "energy_reduce")
+
+
+class GBXError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"gbx: {STATUS_NAMES.get(status, status)}" + (f": {message}" if message else ""))
+
+
+class GbxConfig(ctypes.Structure):
+    _fields_ = [
+        ("model", ctypes.c_int),
+        ("n_radial", ctypes.c_int),
+        ("lebedev_order", ctypes.c_int),
+        ("r0", ctypes.c_double),
+        ("r1", ctypes.c_double),
+        ("table_mode", ctypes.c_int),
+        ("table_cap", ctypes.c_int),
+        ("grid_length", ctypes.c_double),
+        ("table_buffer", ctypes.c_double),
+        ("box", ctypes.c_double * 3),
+        ("switch_width", ctypes.c_double),
+        ("gamma0", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("lam", ctypes.c_double),
+        ("p1", ctypes.c_double),
+        ("p2", ctypes.c_double),
+        ("s0", ctypes.c_double),
+        ("alpha0", ctypes.c_double),
+        ("alpha1", ctypes.c_double),
+        ("prefactor", ctypes.c_double),
+        ("cutoff", ctypes.c_double),
+        ("cutoff_chain_quirk", ctypes.c_int),
+        ("skip_empty", ctypes.c_int),
+        ("reserved", ctypes.c_int * 8),
+    ]
+
+    @staticmethod
+    def from_model(m: GBModel) -> "GbxConfig":
+        c = GbxConfig()
+        c.model = m.model
+        c.n_radial = m.n_radial
+        c.lebedev_order = m.lebedev
+        c.r0, c.r1 = m.r0, m.r1
+        c.table_mode = m.table_mode
+        c.table_cap = m.cap
+        c.grid_length = m.h
+        c.table_buffer = m.buffer
+        for k in range(3):
+            c.box[k] = m.box[k] if m.box[k] > 0 else 10.0
+        c.switch_width = m.sw
+        c.gamma0, c.beta, c.lam = m.gamma0, m.beta, m.lam
+        c.p1, c.p2, c.s0 = m.p1, m.p2, m.s0
+        c.alpha0, c.alpha1 = m.alpha0, m.alpha1
+        c.prefactor = m.pref
+        c.cutoff = m.cutoff
+        c.cutoff_chain_quirk = 1 if m.cutoff_chain_quirk else 0
+        c.skip_empty = 1 if m.skip_empty else 0
+        return c
+
+
+_LIB = None
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load lib/libgbx.so (building it first if absent and nvcc is available)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise GBXError(4, f"CUDA library not built: {path}")
+        _build.build_cuda()
+    L = ctypes.CDLL(path)
+    vp, ci, cd, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    L.gbx_status_string.restype = ctypes.c_char_p
+    L.gbx_status_string.argtypes = [ci]
+    L.gbx_version.restype = ci
+    L.gbx_config_preset.argtypes = [ci, vp]
+    L.gbx_create.argtypes = [vp, ci, ctypes.POINTER(vp)]
+    L.gbx_destroy.argtypes = [vp]
+    L.gbx_last_error.argtypes = [vp, ctypes.c_char_p, sz]
+    L.gbx_set_particle_parameters.argtypes = [vp, vp, vp]
+    L.gbx_set_global_parameters.argtypes = [vp, cd, cd]
+    L.gbx_set_box.argtypes = [vp, vp]
+    L.gbx_execute.argtypes = [vp, vp, vp, ci, vp, ci, vp]
+    L.gbx_execute_host.argtypes = [vp, vp, vp, vp, ci]
+    L.gbx_get_born_radii.argtypes = [vp, vp]
+    L.gbx_get_integrals.argtypes = [vp, vp]
+    L.gbx_get_dEdB.argtypes = [vp, vp]
+    L.gbx_build_lookup_table.argtypes = [vp, vp, vp]
+    L.gbx_get_lookup_table.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    L.gbx_adjoint_host.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.gbx_get_work.argtypes = [vp, vp, vp, vp]
+    L.gbx_set_timing.argtypes = [vp, ci]
+    L.gbx_get_stage_times.argtypes = [vp, vp, ci, vp]
+    for name in EXPORTED:
+        if name not in ("gbx_status_string", "gbx_version"):
+            getattr(L, name).restype = ci
+    _LIB = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One gbx_context: the device state behind one force instance."""
+
+    def __init__(self, model: GBModel, num_atoms: int):
+        self.lib = load()
+        self.model = model
+        self.n = int(num_atoms)
+        self.cfg = GbxConfig.from_model(model)
+        h = ctypes.c_void_p()
+        self._check(self.lib.gbx_create(ctypes.byref(self.cfg), self.n, ctypes.byref(h)), ctx=False)
+        self.h = h
+
+    def _check(self, status: int, ctx: bool = True):
+        if status != GBX_OK:
+            msg = ""
+            if ctx and getattr(self, "h", None):
+                buf = ctypes.create_string_buffer(512)
+                self.lib.gbx_last_error(self.h, buf, 512)
+                msg = buf.value.decode()
+            raise GBXError(status, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_particle_parameters(self, charge, radius):
+        q = np.ascontiguousarray(charge, dtype=np.float64)
+        r = np.ascontiguousarray(radius, dtype=np.float64)
+        if q.shape != (self.n,) or r.shape != (self.n,):
+            raise GBXError(1, "charge/radius must have one entry per particle")
+        self._check(self.lib.gbx_set_particle_parameters(self.h, _p(q), _p(r)))
+
+    def set_global_parameters(self, alpha0: float, alpha1: float):
+        self._check(self.lib.gbx_set_global_parameters(self.h, float(alpha0), float(alpha1)))
+
+    def set_box(self, box):
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        self._check(self.lib.gbx_set_box(self.h, _p(b)))
+
+    def execute_host(self, positions, forces: bool = True, energy: bool = True, count_work: bool = False):
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        if x.shape != (self.n, 3):
+            raise GBXError(1, "positions must be [n, 3]")
+        F = np.zeros((self.n, 3))
+        E = np.zeros(1)
+        flags = (EXEC_FORCES if forces else 0) | (EXEC_ENERGY if energy else 0) | EXEC_CHECK
+        if count_work:
+            flags |= EXEC_COUNT_WORK
+        self._check(self.lib.gbx_execute_host(self.h, _p(x), _p(F), _p(E), flags))
+        return float(E[0]), F
+
+    def execute_device(self, posq_ptr: int, force_ptr: int, force_stride: int, energy_ptr: int, flags: int,
+                       stream: int = 0):
+        self._check(self.lib.gbx_execute(self.h, ctypes.c_void_p(posq_ptr), ctypes.c_void_p(force_ptr),
+                                         int(force_stride), ctypes.c_void_p(energy_ptr), int(flags),
+                                         ctypes.c_void_p(stream)))
+
+    def adjoint(self, positions):
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        E = np.zeros(1)
+        F = np.zeros((self.n, 3))
+        dq = np.zeros(self.n)
+        dR = np.zeros(self.n)
+        da = np.zeros(2)
+        self._check(self.lib.gbx_adjoint_host(self.h, _p(x), _p(E), _p(F), _p(dq), _p(dR), _p(da)))
+        return {"energy": float(E[0]), "forces": F, "dEdq": dq, "dEdR": dR, "dEdalpha": da}
+
+    def born_radii(self):
+        out = np.zeros(self.n)
+        self._check(self.lib.gbx_get_born_radii(self.h, _p(out)))
+        return out
+
+    def integrals(self):
+        out = np.zeros(2 * self.n)
+        self._check(self.lib.gbx_get_integrals(self.h, _p(out)))
+        return out.reshape(2, self.n)
+
+    def dEdB(self):
+        out = np.zeros(self.n)
+        self._check(self.lib.gbx_get_dEdB(self.h, _p(out)))
+        return out
+
+    def work(self):
+        v, s, p = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.gbx_get_work(self.h, ctypes.byref(v), ctypes.byref(s), ctypes.byref(p)))
+        return {"volume_evals": v.value, "shell_evals": s.value, "pairs": p.value}
+
+    def set_timing(self, enable: bool = True):
+        self._check(self.lib.gbx_set_timing(self.h, 1 if enable else 0))
+
+    def stage_times(self):
+        ms = np.zeros(len(STAGES))
+        k = ctypes.c_int()
+        self._check(self.lib.gbx_get_stage_times(self.h, _p(ms), len(STAGES), ctypes.byref(k)))
+        return dict(zip(STAGES, ms.tolist()))
+
+    def lookup_table(self):
+        dims = np.zeros(3, np.int32)
+        mn = np.zeros(3)
+        step = np.zeros(3)
+        ncell = ctypes.c_int64()
+        total = ctypes.c_int64()
+        self._check(self.lib.gbx_get_lookup_table(self.h, _p(dims), _p(mn), _p(step), ctypes.byref(ncell), None,
+                                                  ctypes.byref(total), None))
+        counts = np.zeros(ncell.value, np.int32)
+        atoms = np.zeros(max(total.value, 1), np.int32)
+        self._check(self.lib.gbx_get_lookup_table(self.h, _p(dims), _p(mn), _p(step), ctypes.byref(ncell),
+                                                  _p(counts), ctypes.byref(total), _p(atoms)))
+        return {"dims": dims, "min": mn, "step": step, "counts": counts, "atoms": atoms[: total.value]}

@@ -1,0 +1,684 @@
+// C-ABI entry points (include/gbx.h): context lifecycle, parameters, the
+// execute pipeline and result queries.  No exception crosses this boundary.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gbx_internal.cuh"
+#include "lebedev_rules.h"
+
+using gbx::Context;
+
+namespace {
+
+#define GBX_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      ctx->last_error = std::string(#call ": ") + cudaGetErrorString(e_);                \
+      return e_ == cudaErrorMemoryAllocation ? GBX_ERR_OUT_OF_MEMORY : GBX_ERR_CUDA;     \
+    }                                                                                    \
+  } while (0)
+
+#define GBX_TRY(expr)                 \
+  do {                                \
+    gbx_status s_ = (expr);           \
+    if (s_ != GBX_OK) return s_;      \
+  } while (0)
+
+// Gauss-Legendre by Newton iteration on the Legendre recurrence (Numerical
+// Recipes gauleg, the procedure CharmmQuadrature.h:47-75 follows, with the
+// same operation order so the rule is bit-identical to the reference's).
+void gauss_legendre(double x0, double x1, int n, std::vector<double>& x, std::vector<double>& w) {
+  const double eps = 3.0e-14;
+  const double pi = 3.14159265358979323846264338327950;
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const int m = (n + 1) / 2;
+  const double xm = 0.5 * (x1 + x0), xl = 0.5 * (x1 - x0);
+  for (int i = 1; i <= m; ++i) {
+    double z = cos(pi * (i - 0.25) / (n + 0.5)), z1 = 0.0, pp = 0.0;
+    bool first = true;
+    while (first || fabs(z - z1) > eps) {
+      first = false;
+      double p1 = 1.0, p2 = 0.0, p3;
+      for (int j = 1; j <= n; ++j) {
+        p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      z1 = z;
+      z = z1 - p1 / pp;
+    }
+    x[i - 1] = xm - xl * z;
+    x[n - i] = xm + xl * z;
+    w[i - 1] = 2.0 * xl / ((1.0 - z * z) * pp * pp);
+    w[n - i] = w[i - 1];
+  }
+}
+
+const double* lebedev_rule(int order) {
+  for (int k = 0; k < gbx_lebedev::kNumRules; ++k)
+    if (gbx_lebedev::kRules[k].order == order) return gbx_lebedev::kRules[k].xyzw;
+  return nullptr;
+}
+
+template <class T>
+gbx_status dalloc(Context* ctx, T** p, size_t count) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  if (count == 0) count = 1;
+  GBX_CUDA(cudaMalloc((void**)p, sizeof(T) * count));
+  return GBX_OK;
+}
+
+gbx_status validate_config(const gbx_config& c, std::string& why) {
+  if (c.model < GBX_MODEL_GBSW || c.model > GBX_MODEL_GBMV2) return why = "unknown model", GBX_ERR_INVALID_ARGUMENT;
+  if (c.table_mode < GBX_TABLE_STANDALONE || c.table_mode > GBX_TABLE_PERIODIC)
+    return why = "unknown table mode", GBX_ERR_INVALID_ARGUMENT;
+  if (c.n_radial < 1 || c.n_radial > 256) return why = "n_radial must be in [1, 256]", GBX_ERR_INVALID_ARGUMENT;
+  if (!lebedev_rule(c.lebedev_order)) return why = "unsupported Lebedev order", GBX_ERR_INVALID_ARGUMENT;
+  if (!(c.r0 > 0 && c.r1 > c.r0)) return why = "need 0 < r0 < r1", GBX_ERR_INVALID_ARGUMENT;
+  if (!(c.grid_length > 0)) return why = "grid_length must be > 0", GBX_ERR_INVALID_ARGUMENT;
+  if (!(c.table_buffer >= 0)) return why = "table_buffer must be >= 0", GBX_ERR_INVALID_ARGUMENT;
+  if (c.model == GBX_MODEL_GBSW && !(c.switch_width > 0)) return why = "switch_width must be > 0", GBX_ERR_INVALID_ARGUMENT;
+  if (c.table_mode == GBX_TABLE_PERIODIC)
+    for (int k = 0; k < 3; ++k)
+      if (!(c.box[k] > 0)) return why = "periodic table needs a positive box", GBX_ERR_INVALID_ARGUMENT;
+  if (c.table_cap > gbx::kMaxSortSegment) return why = "table_cap too large", GBX_ERR_INVALID_ARGUMENT;
+  return GBX_OK;
+}
+
+gbx_status upload_quadrature(Context* ctx) {
+  const gbx_config& c = ctx->cfg;
+  std::vector<double> xr, wr;
+  gauss_legendre(c.r0, c.r1, c.n_radial, xr, wr);
+  const double* leb = lebedev_rule(c.lebedev_order);
+  const int nS = c.lebedev_order, Q = c.n_radial * nS;
+  ctx->q_off.assign(3 * (size_t)Q, 0.0);
+  ctx->q_rad.assign(Q, 0.0);
+  ctx->q_w.assign(Q, 0.0);
+  std::vector<float4> qv(Q);
+  std::vector<float2> qw(Q);
+  double S4 = 0.0, S7 = 0.0;
+  for (int i = 0; i < c.n_radial; ++i)
+    for (int j = 0; j < nS; ++j) {
+      const int q = i * nS + j;
+      const double r = xr[i];
+      for (int k = 0; k < 3; ++k) ctx->q_off[3 * q + k] = r * leb[4 * j + k];
+      ctx->q_rad[q] = r;
+      ctx->q_w[q] = wr[i] * leb[4 * j + 3];
+      const double w4 = ctx->q_w[q] / (r * r), w7 = ctx->q_w[q] / (r * r * r * r * r);
+      S4 += w4;
+      S7 += w7;
+      qv[q] = make_float4((float)ctx->q_off[3 * q], (float)ctx->q_off[3 * q + 1], (float)ctx->q_off[3 * q + 2], (float)r);
+      qw[q] = make_float2((float)w4, (float)w7);
+    }
+  ctx->S4 = S4;
+  ctx->S7 = S7;
+  const double r0 = c.r0;
+  ctx->C4 = 1.0 / r0 - S4;
+  ctx->C7 = 1.0 / (4.0 * r0 * r0 * r0 * r0) - S7;
+  GBX_TRY(dalloc(ctx, &ctx->d_qv, Q));
+  GBX_TRY(dalloc(ctx, &ctx->d_qw, Q));
+  GBX_TRY(dalloc(ctx, &ctx->d_qoff, 3 * (size_t)Q));
+  GBX_CUDA(cudaMemcpy(ctx->d_qv, qv.data(), sizeof(float4) * Q, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(ctx->d_qw, qw.data(), sizeof(float2) * Q, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(ctx->d_qoff, ctx->q_off.data(), sizeof(double) * 3 * Q, cudaMemcpyHostToDevice));
+  return GBX_OK;
+}
+
+int choose_chunks(int n, int Q) {
+  // >= ~48 resident warps per SM on 152 SMs; each chunk keeps >= 16 points
+  const int groups = (n + gbx::kWarp - 1) / gbx::kWarp;
+  int c = (152 * 48 + groups - 1) / groups;
+  c = std::max(1, std::min(c, std::max(1, Q / 16)));
+  return c;
+}
+
+gbx_status alloc_atom_buffers(Context* ctx) {
+  const int n = ctx->n;
+  const int Q = ctx->cfg.n_radial * ctx->cfg.lebedev_order;
+  ctx->n_chunks = choose_chunks(n, Q);
+  GBX_TRY(dalloc(ctx, &ctx->d_radius, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_charge, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_par, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_wpar, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_pos, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_J, 2 * (size_t)ctx->n_chunks * n));
+  GBX_TRY(dalloc(ctx, &ctx->d_born, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_bornf, 2 * (size_t)n));
+  GBX_TRY(dalloc(ctx, &ctx->d_dBdJ, 6 * (size_t)n));
+  GBX_TRY(dalloc(ctx, &ctx->d_integrals, 2 * (size_t)n));
+  GBX_TRY(dalloc(ctx, &ctx->d_dEdB_fx, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_dEdJ, n));
+  ctx->energy_parts = gbx::pair_energy_parts(n, gbx::pair_segments(n));
+  GBX_TRY(dalloc(ctx, &ctx->d_energy_part, ctx->energy_parts));
+  GBX_TRY(dalloc(ctx, &ctx->d_force_fx, 3 * (size_t)n));
+  GBX_TRY(dalloc(ctx, &ctx->d_energy, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_dEdR_fx, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_dEdq_fx, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_alpha_grad, 2));
+  GBX_TRY(dalloc(ctx, &ctx->d_status, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_work, 4));
+  GBX_TRY(dalloc(ctx, &ctx->d_geom, 1));
+  GBX_CUDA(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+  GBX_CUDA(cudaMemset(ctx->d_work, 0, sizeof(unsigned long long) * 4));
+  GBX_CUDA(cudaMallocHost((void**)&ctx->h_pos, sizeof(float4) * n));
+  GBX_CUDA(cudaMallocHost((void**)&ctx->h_force_fx, sizeof(unsigned long long) * 3 * n));
+  return GBX_OK;
+}
+
+gbx_status grow_table(Context* ctx, long long cells, long long entries) {
+  if (cells > ctx->cell_cap) {
+    const long long cap = cells + cells / 4 + 1024;
+    GBX_TRY(dalloc(ctx, &ctx->d_cell_count, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_cell_start, cap + 1));
+    GBX_TRY(dalloc(ctx, &ctx->d_cell_cursor, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_block_sums, cap / (1024 * 8) + 2));
+    ctx->cell_cap = cap;
+  }
+  if (entries > ctx->entry_cap) {
+    const long long cap = entries + entries / 4 + 4096;
+    if (cap > 0x7fffffffLL) {
+      ctx->last_error = "lookup table would exceed 2^31 entries";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    GBX_TRY(dalloc(ctx, &ctx->d_entries, cap));
+    ctx->entry_cap = cap;
+  }
+  return GBX_OK;
+}
+
+// Build the table; on a capacity miss read the needed sizes back, grow and
+// rebuild.  Synchronises the stream when `check` is set.
+gbx_status build_table_checked(Context* ctx, bool check) {
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    GBX_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream));
+    GBX_TRY(gbx::launch_table_build(ctx, ctx->d_pos));
+    if (!check && ctx->cell_cap > 0 && ctx->entry_cap > 0) return GBX_OK;
+    unsigned st = 0;
+    gbx::TableGeom g;
+    GBX_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaMemcpyAsync(&g, ctx->d_geom, sizeof(g), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st & gbx::kStatusSegmentTooLong) {
+      ctx->last_error = "a lookup-table cell holds more atoms than the sort supports";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    const bool cells_short = (st & gbx::kStatusTableCells) != 0;
+    const bool entries_short = (st & gbx::kStatusTableEntries) != 0;
+    if (!cells_short && !entries_short) {
+      ctx->table_valid = true;
+      return GBX_OK;
+    }
+    if (cells_short && g.ncell <= 1) {
+      ctx->last_error = "lookup table dimension is too large, check atom positions";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    if (g.ncell > (long long)1 << 31) {
+      ctx->last_error = "lookup grid would exceed 2^31 cells";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    // the entry count is only known once the cell array was large enough
+    long long entries = cells_short ? (long long)ctx->n * 64 : g.total;
+    GBX_TRY(grow_table(ctx, g.ncell, std::max(entries, (long long)ctx->n)));
+  }
+  ctx->last_error = "lookup table did not fit after resizing";
+  return GBX_ERR_TABLE_TOO_LARGE;
+}
+
+gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* force, int stride, double* energy,
+                        bool check, bool adjoint, bool count_work) {
+  int stage = 0;
+  auto mark = [&]() -> gbx_status {
+    if (ctx->timing) GBX_CUDA(cudaEventRecord(ctx->ev[stage], ctx->stream));
+    ++stage;
+    return GBX_OK;
+  };
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_stage_positions(ctx, posq));
+  GBX_TRY(mark());
+  GBX_TRY(build_table_checked(ctx, check));
+  if (count_work) GBX_CUDA(cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * 4, ctx->stream));
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_integrals(ctx, ctx->d_pos, count_work));
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_born(ctx));
+  if (adjoint) {
+    GBX_CUDA(cudaMemsetAsync(ctx->d_dEdq_fx, 0, sizeof(unsigned long long) * ctx->n, ctx->stream));
+    GBX_CUDA(cudaMemsetAsync(ctx->d_dEdR_fx, 0, sizeof(unsigned long long) * ctx->n, ctx->stream));
+  }
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_pair(ctx, ctx->d_pos, force, stride, adjoint));
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_chain_prep(ctx, adjoint));
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_chain(ctx, ctx->d_pos, force, stride, adjoint));
+  GBX_TRY(mark());
+  GBX_TRY(gbx::launch_energy_reduce(ctx, energy, adjoint));
+  GBX_TRY(mark());
+  ctx->have_result = true;
+  if (check) {
+    unsigned st = 0;
+    GBX_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st & gbx::kStatusNonFinite) {
+      ctx->last_error = "non-finite Born radius";
+      return GBX_ERR_NONFINITE;
+    }
+  }
+  return GBX_OK;
+}
+
+void set_model_params(Context* ctx, std::vector<float>& wpar, std::vector<float2>& par) {
+  const gbx_config& c = ctx->cfg;
+  const int n = ctx->n;
+  wpar.resize(n);
+  par.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const double R = ctx->radius[i];
+    if (c.model == GBX_MODEL_GBSW) {
+      wpar[i] = (float)((R + 0.03) * 0.9520);  // CharmmReferenceGBSW.cpp:625
+      par[i] = make_float2((float)R, 0.0f);
+    } else if (c.model == GBX_MODEL_GBMV1) {
+      wpar[i] = (float)(c.gamma0 * log(c.lambda) / (R * R * R * R));  // GBMVIntegralTypeI.cpp:168
+      par[i] = make_float2((float)R, 0.0f);
+    } else {
+      const double C = c.p1 * R * 10 + c.p2;  // GBMVIntegralTypeII.cpp:179
+      wpar[i] = (float)C;
+      par[i] = make_float2((float)(C - 100.0 * R * R), (float)R);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbx_status_string(gbx_status s) {
+  switch (s) {
+    case GBX_OK: return "ok";
+    case GBX_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GBX_ERR_CUDA: return "CUDA error";
+    case GBX_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GBX_ERR_UNSUPPORTED: return "unsupported";
+    case GBX_ERR_NONFINITE: return "non-finite result";
+    case GBX_ERR_TABLE_TOO_LARGE: return "lookup table too large";
+    case GBX_ERR_NOT_READY: return "no result yet";
+    case GBX_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+int gbx_version(void) { return 10000; }
+
+gbx_status gbx_config_preset(int preset, gbx_config* cfg) {
+  if (!cfg) return GBX_ERR_INVALID_ARGUMENT;
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->n_radial = 24;
+  cfg->r0 = 0.05;   // CharmmReferenceGBSW.cpp:27-28, GBSWIntegral.cpp:31-34
+  cfg->r1 = 2.0;
+  cfg->grid_length = 0.15;
+  cfg->switch_width = 0.03;
+  cfg->gamma0 = 0.44;
+  cfg->alpha0 = -0.180;  // CharmmReferenceGBSW.cpp:559-560
+  cfg->alpha1 = 1.817;
+  cfg->prefactor = -138.935456 * (1.0 - 1.0 / 80.0);  // CharmmReferenceGBSW.cpp:177-178
+  cfg->cutoff = 0.0;
+  cfg->skip_empty = 1;
+  cfg->box[0] = cfg->box[1] = cfg->box[2] = 10.0;
+  switch (preset) {
+    case GBX_PRESET_CHARMM_GBSW:
+      cfg->model = GBX_MODEL_GBSW;
+      cfg->lebedev_order = 38;
+      cfg->table_mode = GBX_TABLE_STANDALONE;
+      cfg->table_buffer = 0.20;  // CharmmReferenceGBSW.cpp:47
+      cfg->table_cap = 0;
+      cfg->cutoff_chain_quirk = 1;
+      return GBX_OK;
+    case GBX_PRESET_GBSW_INTEGRAL:
+      cfg->model = GBX_MODEL_GBSW;
+      cfg->lebedev_order = 26;
+      cfg->table_mode = GBX_TABLE_GRID;
+      cfg->table_buffer = 0.04;  // GBSWIntegral.cpp:60
+      cfg->table_cap = 64;       // CustomGBIntegral.cpp:15
+      return GBX_OK;
+    case GBX_PRESET_GBMV1:
+      cfg->model = GBX_MODEL_GBMV1;
+      cfg->lebedev_order = 26;
+      cfg->table_mode = GBX_TABLE_PERIODIC;
+      cfg->table_buffer = 0.21;  // GBMVIntegralTypeI.cpp:56
+      cfg->table_cap = 64;
+      cfg->beta = -100;  // GBMVIntegralTypeI.cpp:22-24
+      cfg->lambda = 0.1;
+      cfg->skip_empty = 0;
+      return GBX_OK;
+    case GBX_PRESET_GBMV2:
+      cfg->model = GBX_MODEL_GBMV2;
+      cfg->lebedev_order = 26;
+      cfg->table_mode = GBX_TABLE_PERIODIC;
+      cfg->table_buffer = 0.21;
+      cfg->table_cap = 64;
+      cfg->beta = -20;  // GBMVIntegralTypeII.cpp:23-28
+      cfg->lambda = 0.5;
+      cfg->p1 = 0.45;
+      cfg->p2 = 1.25;
+      cfg->s0 = 0.7;
+      cfg->skip_empty = 0;
+      return GBX_OK;
+  }
+  return GBX_ERR_INVALID_ARGUMENT;
+}
+
+gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
+  if (!cfg || !out || num_atoms < 1) return GBX_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::string why;
+  gbx_status s = validate_config(*cfg, why);
+  if (s != GBX_OK) return s;
+  Context* ctx = new (std::nothrow) Context();
+  if (!ctx) return GBX_ERR_OUT_OF_MEMORY;
+  ctx->cfg = *cfg;
+  ctx->n = num_atoms;
+  ctx->alpha0 = (float)cfg->alpha0;
+  ctx->alpha1 = (float)cfg->alpha1;
+  if (cudaGetDevice(&ctx->device) != cudaSuccess) {
+    delete ctx;
+    return GBX_ERR_CUDA;
+  }
+  s = upload_quadrature(ctx);
+  if (s == GBX_OK) s = alloc_atom_buffers(ctx);
+  if (s == GBX_OK && cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) s = GBX_ERR_CUDA;
+  if (s != GBX_OK) {
+    gbx_destroy(reinterpret_cast<gbx_context*>(ctx));
+    return s;
+  }
+  // neutral defaults: zero charge, 0.15 nm radius
+  ctx->charge.assign(num_atoms, 0.0);
+  ctx->radius.assign(num_atoms, 0.15);
+  s = gbx_set_particle_parameters(reinterpret_cast<gbx_context*>(ctx), ctx->charge.data(), ctx->radius.data());
+  if (s != GBX_OK) {
+    gbx_destroy(reinterpret_cast<gbx_context*>(ctx));
+    return s;
+  }
+  *out = reinterpret_cast<gbx_context*>(ctx);
+  return GBX_OK;
+}
+
+gbx_status gbx_destroy(gbx_context* handle) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  void* ptrs[] = {ctx->d_qv, ctx->d_qw, ctx->d_qoff, ctx->d_radius, ctx->d_charge, ctx->d_par, ctx->d_wpar,
+                  ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_cell_cursor, ctx->d_entries,
+                  ctx->d_block_sums, ctx->d_reduce, ctx->d_pos, ctx->d_J, ctx->d_born, ctx->d_bornf, ctx->d_dBdJ,
+                  ctx->d_integrals, ctx->d_dEdB_fx, ctx->d_dEdJ, ctx->d_energy_part, ctx->d_force_fx,
+                  ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (int k = 0; k <= Context::kStages; ++k)
+    if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+  if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
+  if (ctx->h_force_fx) cudaFreeHost(ctx->h_force_fx);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GBX_OK;
+}
+
+gbx_status gbx_last_error(const gbx_context* handle, char* buf, size_t len) {
+  const Context* ctx = reinterpret_cast<const Context*>(handle);
+  if (!ctx || !buf || len == 0) return GBX_ERR_INVALID_ARGUMENT;
+  strncpy(buf, ctx->last_error.c_str(), len - 1);
+  buf[len - 1] = 0;
+  return GBX_OK;
+}
+
+gbx_status gbx_set_particle_parameters(gbx_context* handle, const double* charge, const double* radius) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !charge || !radius) return GBX_ERR_INVALID_ARGUMENT;
+  const int n = ctx->n;
+  for (int i = 0; i < n; ++i) {
+    if (!isfinite(charge[i]) || !isfinite(radius[i]) || !(radius[i] > 0)) {
+      ctx->last_error = "charges must be finite and radii finite and > 0 (particle " + std::to_string(i) + ")";
+      return GBX_ERR_INVALID_ARGUMENT;
+    }
+  }
+  ctx->charge.assign(charge, charge + n);
+  ctx->radius.assign(radius, radius + n);
+  std::vector<float> qf(n), wpar;
+  std::vector<float2> par;
+  for (int i = 0; i < n; ++i) qf[i] = (float)charge[i];
+  set_model_params(ctx, wpar, par);
+  GBX_CUDA(cudaMemcpy(ctx->d_radius, radius, sizeof(double) * n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(ctx->d_charge, qf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(ctx->d_wpar, wpar.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(ctx->d_par, par.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  return GBX_OK;
+}
+
+gbx_status gbx_set_global_parameters(gbx_context* handle, double alpha0, double alpha1) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !isfinite(alpha0) || !isfinite(alpha1)) return GBX_ERR_INVALID_ARGUMENT;
+  ctx->cfg.alpha0 = alpha0;
+  ctx->cfg.alpha1 = alpha1;
+  ctx->alpha0 = (float)alpha0;
+  ctx->alpha1 = (float)alpha1;
+  return GBX_OK;
+}
+
+gbx_status gbx_set_box(gbx_context* handle, const double box[3]) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !box) return GBX_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < 3; ++k)
+    if (!(box[k] > 0) || !isfinite(box[k])) return GBX_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < 3; ++k) ctx->cfg.box[k] = box[k];
+  return GBX_OK;
+}
+
+gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long* force_fixed, int force_stride,
+                       double* energy, int flags, void* stream) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
+  if ((flags & GBX_EXEC_FORCES) && (!force_fixed || force_stride < ctx->n)) return GBX_ERR_INVALID_ARGUMENT;
+  if ((flags & GBX_EXEC_ENERGY) && !energy) return GBX_ERR_INVALID_ARGUMENT;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->stream;
+  unsigned long long* f = force_fixed;
+  int stride = force_stride;
+  if (!(flags & GBX_EXEC_FORCES)) {
+    f = ctx->d_force_fx;
+    stride = ctx->n;
+    GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
+  }
+  double* e = (flags & GBX_EXEC_ENERGY) ? energy : ctx->d_energy;
+  const bool check = (flags & GBX_EXEC_CHECK) || ctx->cell_cap == 0 || !ctx->table_valid;
+  return run_pipeline(ctx, reinterpret_cast<const float4*>(posq), f, stride, e, check, false,
+                      (flags & GBX_EXEC_COUNT_WORK) != 0);
+}
+
+}  // extern "C"
+
+namespace {
+
+gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work) {
+  const int n = ctx->n;
+  for (int i = 0; i < n; ++i)
+    ctx->h_pos[i] = make_float4((float)positions[3 * i], (float)positions[3 * i + 1], (float)positions[3 * i + 2], 0.f);
+  GBX_CUDA(cudaMemcpyAsync(ctx->d_pos, ctx->h_pos, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
+  GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));
+  GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
+  // d_pos holds the raw copy; staging rewrites it in place with the model parameter
+  return run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, true, adjoint, count_work);
+}
+
+gbx_status host_results(Context* ctx, double* forces, double* energy) {
+  const int n = ctx->n;
+  if (forces) {
+    GBX_CUDA(cudaMemcpyAsync(ctx->h_force_fx, ctx->d_force_fx, sizeof(unsigned long long) * 3 * n,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  double e = 0;
+  GBX_CUDA(cudaMemcpyAsync(&e, ctx->d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (forces)
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) forces[3 * i + k] += gbx::fixed_to_double(ctx->h_force_fx[(size_t)k * n + i]);
+  if (energy) *energy = e;
+  if (!isfinite(e)) {
+    ctx->last_error = "non-finite energy";
+    return GBX_ERR_NONFINITE;
+  }
+  return GBX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbx_status gbx_execute_host(gbx_context* handle, const double* positions, double* forces, double* energy, int flags) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !positions) return GBX_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 3 * ctx->n; ++i)
+    if (!isfinite(positions[i])) {
+      ctx->last_error = "non-finite position";
+      return GBX_ERR_INVALID_ARGUMENT;
+    }
+  GBX_TRY(host_run(ctx, positions, false, (flags & GBX_EXEC_COUNT_WORK) != 0));
+  return host_results(ctx, (flags & GBX_EXEC_FORCES) ? forces : nullptr, energy);
+}
+
+gbx_status gbx_adjoint_host(gbx_context* handle, const double* positions, double* energy, double* forces,
+                            double* dEdq, double* dEdR, double* dEdalpha) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !positions) return GBX_ERR_INVALID_ARGUMENT;
+  GBX_TRY(host_run(ctx, positions, true, false));
+  const int n = ctx->n;
+  std::vector<unsigned long long> q(n), r(n);
+  double a[2];
+  GBX_CUDA(cudaMemcpyAsync(q.data(), ctx->d_dEdq_fx, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(r.data(), ctx->d_dEdR_fx, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(a, ctx->d_alpha_grad, sizeof(a), cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_TRY(host_results(ctx, forces, energy));
+  for (int i = 0; i < n; ++i) {
+    if (dEdq) dEdq[i] = gbx::fixed_to_double(q[i]);
+    if (dEdR) dEdR[i] = gbx::fixed_to_double(r[i]);
+  }
+  if (dEdalpha) {
+    dEdalpha[0] = a[0];
+    dEdalpha[1] = a[1];
+  }
+  return GBX_OK;
+}
+
+gbx_status gbx_get_born_radii(gbx_context* handle, double* born) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !born) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->have_result) return GBX_ERR_NOT_READY;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(born, ctx->d_born, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+  return GBX_OK;
+}
+
+gbx_status gbx_get_integrals(gbx_context* handle, double* integrals) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !integrals) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->have_result) return GBX_ERR_NOT_READY;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(integrals, ctx->d_integrals, sizeof(double) * 2 * ctx->n, cudaMemcpyDeviceToHost));
+  return GBX_OK;
+}
+
+gbx_status gbx_get_dEdB(gbx_context* handle, double* dEdB) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !dEdB) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->have_result) return GBX_ERR_NOT_READY;
+  std::vector<unsigned long long> v(ctx->n);
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(v.data(), ctx->d_dEdB_fx, sizeof(unsigned long long) * ctx->n, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < ctx->n; ++i) dEdB[i] = gbx::fixed_to_double(v[i]);
+  return GBX_OK;
+}
+
+gbx_status gbx_build_lookup_table(gbx_context* handle, const void* posq, void* stream) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->stream;
+  GBX_TRY(gbx::launch_stage_positions(ctx, reinterpret_cast<const float4*>(posq)));
+  return build_table_checked(ctx, true);
+}
+
+gbx_status gbx_get_lookup_table(gbx_context* handle, int dims[3], double mn[3], double step[3], int64_t* ncell,
+                                int32_t* counts, int64_t* total, int32_t* atoms) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->table_valid) return GBX_ERR_NOT_READY;
+  gbx::TableGeom g;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(&g, ctx->d_geom, sizeof(g), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 3; ++k) {
+    if (dims) dims[k] = g.dims[k];
+    if (mn) mn[k] = g.min[k];
+    if (step) step[k] = g.step[k];
+  }
+  if (ncell) *ncell = g.ncell;
+  std::vector<int> cnt(g.ncell), st(g.ncell + 1);
+  GBX_CUDA(cudaMemcpy(cnt.data(), ctx->d_cell_count, sizeof(int) * g.ncell, cudaMemcpyDeviceToHost));
+  GBX_CUDA(cudaMemcpy(st.data(), ctx->d_cell_start, sizeof(int) * (g.ncell + 1), cudaMemcpyDeviceToHost));
+  long long tot = 0;
+  for (long long c = 0; c < g.ncell; ++c) tot += cnt[c];
+  if (total) *total = tot;
+  if (counts) memcpy(counts, cnt.data(), sizeof(int) * g.ncell);
+  if (atoms) {
+    std::vector<int> all(g.total > 0 ? g.total : 1);
+    if (g.total > 0)
+      GBX_CUDA(cudaMemcpy(all.data(), ctx->d_entries, sizeof(int) * g.total, cudaMemcpyDeviceToHost));
+    long long o = 0;
+    for (long long c = 0; c < g.ncell; ++c)
+      for (int m = 0; m < cnt[c]; ++m) atoms[o++] = all[st[c] + m];
+  }
+  return GBX_OK;
+}
+
+gbx_status gbx_set_timing(gbx_context* handle, int enable) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  if (enable && !ctx->ev[0])
+    for (int k = 0; k <= Context::kStages; ++k) GBX_CUDA(cudaEventCreate(&ctx->ev[k]));
+  ctx->timing = enable != 0;
+  return GBX_OK;
+}
+
+gbx_status gbx_get_stage_times(gbx_context* handle, double* ms, int max_stages, int* num_stages) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !ms) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->timing || !ctx->have_result) return GBX_ERR_NOT_READY;
+  GBX_CUDA(cudaEventSynchronize(ctx->ev[Context::kStages]));
+  const int n = std::min(max_stages, (int)Context::kStages);
+  for (int k = 0; k < n; ++k) {
+    float t = 0.f;
+    GBX_CUDA(cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]));
+    ms[k] = t;
+  }
+  if (num_stages) *num_stages = Context::kStages;
+  return GBX_OK;
+}
+
+gbx_status gbx_get_work(gbx_context* handle, double* volume_evals, double* shell_evals, double* pairs) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  unsigned long long w[4];
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(w, ctx->d_work, sizeof(w), cudaMemcpyDeviceToHost));
+  if (volume_evals) *volume_evals = (double)w[0];
+  if (shell_evals) *shell_evals = (double)w[1];
+  if (pairs) *pairs = (double)ctx->n * (double)(ctx->n - 1);
+  return GBX_OK;
+}
+
+}  // extern "C"

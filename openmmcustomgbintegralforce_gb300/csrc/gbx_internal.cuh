@@ -1,0 +1,158 @@
+// Internal types shared by the gbx CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gbx.h"
+
+namespace gbx {
+
+constexpr int kWarp = 32;
+constexpr double kFixedScale = 4294967296.0;  // 2^32, OpenMM's force fixed-point scale
+constexpr int kMaxSortSegment = 2048;         // longest cell list the sort handles
+
+// Device status bits (context->d_status).
+enum : unsigned {
+  kStatusTableCells = 1u,     // grid has more cells than allocated
+  kStatusTableEntries = 2u,   // more list entries than allocated
+  kStatusSegmentTooLong = 4u, // a cell list exceeded kMaxSortSegment
+  kStatusNonFinite = 8u,      // NaN/Inf Born radius
+  kStatusTimeout = 16u,       // bounded device wait expired
+};
+
+// Lookup-table geometry, computed on the device each step.
+struct TableGeom {
+  double min[3];
+  double max[3];
+  double step[3];
+  double box[3];
+  double pad;       // standalone uniform pad
+  double L;         // periodic: max(step)
+  int dims[3];
+  int mode;
+  long long ncell;
+  long long total;  // list entries before capping
+};
+
+// Per-model constants used inside the kernels (FP32 hot path + FP64 exact paths).
+struct ModelConst {
+  int model;
+  int table_mode;
+  int cap;
+  int skip_empty;
+  int nq;
+  int cutoff_chain_quirk;
+  float sw, c1, c3;          // GBSW: u = 1/2 + c1 dr - c3 dr^3, c1 = 3/(4w), c3 = 1/(4w^3)
+  float gamma0_lnlambda;     // GBMV-I gamma_j = gamma0 ln(lambda) / R^4
+  float beta, lambda, s0;    // GBMV
+  float p1, p2;              // GBMV-II
+  float cutoff2;             // pair cutoff squared (<= 0: none)
+  float pref;                // pair prefactor
+  double h, buffer, cutoff;
+};
+
+// One evaluation context (one force instance).
+struct Context {
+  gbx_config cfg{};
+  int n = 0;
+  int device = 0;
+  std::string last_error;
+
+  // quadrature (host, FP64) and device copies
+  std::vector<double> q_off, q_rad, q_w;  // [Q*3], [Q], [Q]
+  double S4 = 0, S7 = 0;                  // sum_q w/r^2, sum_q w/r^5 (FP64)
+  double C4 = 0, C7 = 0;                  // 1/r0 - S4, 1/(4 r0^4) - S7
+  float4* d_qv = nullptr;                 // (vx, vy, vz, r) FP32
+  float2* d_qw = nullptr;                 // (w/r^2, w/r^5) FP32
+  double* d_qoff = nullptr;               // FP64 offsets for the exact cell query
+
+  // particle data
+  std::vector<double> charge, radius;
+  double* d_radius = nullptr;  // FP64 radii (table geometry)
+  float* d_charge = nullptr;
+  float2* d_par = nullptr;     // secondary model parameters per atom
+  float* d_wpar = nullptr;     // main model parameter (staged into pos.w)
+  float alpha0 = 0, alpha1 = 0;
+
+  // table
+  TableGeom* d_geom = nullptr;
+  long long cell_cap = 0, entry_cap = 0;
+  int* d_cell_count = nullptr;   // uncapped count -> final (capped) count
+  int* d_cell_start = nullptr;   // [cell_cap+1]
+  int* d_cell_cursor = nullptr;
+  int* d_entries = nullptr;      // [entry_cap]
+  int* d_block_sums = nullptr;
+  double* d_reduce = nullptr;    // geometry reduction scratch
+  bool table_valid = false;
+
+  // per-step state
+  float4* d_pos = nullptr;       // internal positions (x, y, z, 0)
+  int n_chunks = 0;              // quadrature chunks per atom
+  float* d_J = nullptr;          // [2][n_chunks][n] FP32 partial integrals
+  double* d_born = nullptr;      // [n]
+  float* d_bornf = nullptr;      // [n] (B, 1/B interleaved as float2)
+  double* d_dBdJ = nullptr;      // [6n]: dB/dJ [2n], dB/dalpha [2n], adjoint alpha terms [2n]
+  double* d_integrals = nullptr; // [2n]  I4, I7
+  unsigned long long* d_dEdB_fx = nullptr;  // [n] fixed point
+  float2* d_dEdJ = nullptr;      // [n]
+  double* d_energy_part = nullptr;  // [max warps]
+  int energy_parts = 0;
+  unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
+  double* d_energy = nullptr;     // internal energy (host path)
+  unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]
+  unsigned long long* d_dEdq_fx = nullptr;  // adjoint [n]
+  double* d_alpha_grad = nullptr; // adjoint [2]
+  unsigned* d_status = nullptr;
+  unsigned long long* d_work = nullptr;  // [4] evaluation counters
+  bool have_result = false;
+
+  // optional per-stage timing (CUDA events on the execute stream)
+  bool timing = false;
+  static constexpr int kStages = 8;
+  cudaEvent_t ev[kStages + 1] = {};
+
+  // host staging
+  float4* h_pos = nullptr;                 // pinned
+  unsigned long long* h_force_fx = nullptr; // pinned
+  cudaStream_t stream = nullptr;
+};
+
+// --------------------------------------------------------------------------
+// Device helpers
+// --------------------------------------------------------------------------
+
+__device__ __forceinline__ void red_add_fixed(unsigned long long* addr, float v) {
+  long long q = __double2ll_rn((double)v * kFixedScale);
+  atomicAdd(addr, (unsigned long long)q);
+}
+
+__device__ __forceinline__ void red_add_fixed_d(unsigned long long* addr, double v) {
+  long long q = __double2ll_rn(v * kFixedScale);
+  atomicAdd(addr, (unsigned long long)q);
+}
+
+__host__ __device__ __forceinline__ double fixed_to_double(unsigned long long v) {
+  return (double)(long long)v / kFixedScale;
+}
+
+// --------------------------------------------------------------------------
+// Launchers (implemented in the k_*.cu files); all enqueue on ctx->stream.
+// --------------------------------------------------------------------------
+
+gbx_status launch_stage_positions(Context* ctx, const float4* posq);
+gbx_status launch_table_build(Context* ctx, const float4* pos);
+gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
+gbx_status launch_born(Context* ctx);
+gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
+int pair_energy_parts(int n, int segments);
+int pair_segments(int n);
+ModelConst make_model_const(const Context* ctx);
+gbx_status launch_chain_prep(Context* ctx, bool adjoint);
+gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
+gbx_status launch_energy_reduce(Context* ctx, double* energy, bool adjoint);
+
+}  // namespace gbx

@@ -1,0 +1,512 @@
+// Lookup-table build: bins atoms into per-cell lists that are bit-identical
+// to the reference's tables.
+//
+//   geometry  one block reduces the bounding box / centre of geometry and
+//             derives the grid exactly as the reference does (FP64);
+//   count     one warp per atom enumerates its candidate cells (or samples)
+//             and counts members with atomics;
+//   scan      exclusive prefix sum of the counts -> CSR offsets;
+//   fill      second enumeration writes members at atomic cursors;
+//   sort      one warp per cell ranks its entries, restoring the reference's
+//             ascending-atom insertion order, then applies the per-cell cap.
+//
+// Every FP64 operation that decides membership is written with explicit
+// round-to-nearest intrinsics so that no multiply-add is contracted: the
+// decisions match the reference's separately rounded C++ arithmetic.
+#include <math.h>
+
+#include "gbx_internal.cuh"
+
+namespace gbx {
+namespace {
+
+constexpr int kGeomThreads = 1024;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 8;
+constexpr int kMaxSamples = 96;  // samples per axis in the periodic branch
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// sqrt(3.0)/2.0 as the reference computes it in double.
+__device__ __forceinline__ double half_sqrt3() { return ddiv(__dsqrt_rn(3.0), 2.0); }
+
+// --------------------------------------------------------------------------
+// Geometry: CharmmReferenceGBSW.cpp:444-466, CustomGBIntegral.cpp:53-113,163-193
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const float4* __restrict__ pos,
+                                                                  const double* __restrict__ radius, int n,
+                                                                  int mode, double h, double buffer, double sw,
+                                                                  double bx, double by, double bz,
+                                                                  TableGeom* __restrict__ g, long long cell_cap,
+                                                                  unsigned* __restrict__ status) {
+  __shared__ double s_min[3][kGeomThreads / kWarp];
+  __shared__ double s_max[3][kGeomThreads / kWarp];
+  __shared__ double s_sum[3][kGeomThreads];
+  __shared__ double s_r[kGeomThreads / kWarp];
+  const int t = threadIdx.x;
+  double mn[3], mx[3], sm[3] = {0, 0, 0};
+  double rmax = 0.0;
+  if (n > 0) {
+    float4 p0 = pos[0];
+    mn[0] = mx[0] = p0.x;
+    mn[1] = mx[1] = p0.y;
+    mn[2] = mx[2] = p0.z;
+  }
+  for (int a = t; a < n; a += blockDim.x) {
+    float4 p = pos[a];
+    double c[3] = {(double)p.x, (double)p.y, (double)p.z};
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fmin(mn[k], c[k]);
+      mx[k] = fmax(mx[k], c[k]);
+      sm[k] = dadd(sm[k], c[k]);
+    }
+    rmax = fmax(rmax, radius[a]);
+  }
+  // warp min/max (exact in any order)
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+      mx[k] = fmax(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+    }
+    rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+  }
+  const int w = t / kWarp, l = t % kWarp;
+  if (l == 0) {
+    for (int k = 0; k < 3; ++k) {
+      s_min[k][w] = mn[k];
+      s_max[k][w] = mx[k];
+    }
+    s_r[w] = rmax;
+  }
+  for (int k = 0; k < 3; ++k) s_sum[k][t] = sm[k];
+  __syncthreads();
+  // fixed-shape tree for the centre-of-geometry sum (deterministic)
+  for (int stride = kGeomThreads / 2; stride > 0; stride >>= 1) {
+    if (t < stride)
+      for (int k = 0; k < 3; ++k) s_sum[k][t] = dadd(s_sum[k][t], s_sum[k][t + stride]);
+    __syncthreads();
+  }
+  if (t != 0) return;
+  for (int ww = 1; ww < kGeomThreads / kWarp; ++ww) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fmin(mn[k], s_min[k][ww]);
+      mx[k] = fmax(mx[k], s_max[k][ww]);
+    }
+    rmax = fmax(rmax, s_r[ww]);
+  }
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = fmin(mn[k], s_min[k][0]);
+    mx[k] = fmax(mx[k], s_max[k][0]);
+  }
+  rmax = fmax(rmax, s_r[0]);
+  TableGeom G;
+  G.mode = mode;
+  G.total = 0;
+  G.L = h;
+  long long ncell = 1;
+  if (mode == GBX_TABLE_STANDALONE || mode == GBX_TABLE_GRID) {
+    double pad;
+    if (mode == GBX_TABLE_STANDALONE)
+      pad = dadd(dadd(dadd(dadd(buffer, rmax), sw), dmul(half_sqrt3(), h)), 1e-6);
+    else
+      pad = dadd(dadd(0.03, dmul(half_sqrt3(), h)), buffer);
+    G.pad = pad;
+    for (int k = 0; k < 3; ++k) {
+      double lo = dsub(mn[k], pad), hi = dadd(mx[k], pad);
+      double length = dsub(hi, lo);
+      if (mode == GBX_TABLE_GRID && length > 1000.0) {
+        atomicOr(status, kStatusTableCells);
+        G.dims[k] = 1;
+      } else {
+        G.dims[k] = (int)ceil(ddiv(length, h)) + 1;
+      }
+      G.min[k] = lo;
+      G.max[k] = dadd(lo, dmul((double)(G.dims[k] - 1), h));
+      G.step[k] = h;
+      G.box[k] = 0.0;
+      ncell *= G.dims[k];
+    }
+  } else {
+    double box[3] = {bx, by, bz};
+    double cog[3];
+    for (int k = 0; k < 3; ++k) cog[k] = ddiv(s_sum[k][0], (double)n);
+    double L = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double d = box[k];
+      G.box[k] = d;
+      G.min[k] = dsub(cog[k], ddiv(d, 2.0));
+      G.max[k] = dadd(cog[k], ddiv(d, 2.0));
+      G.dims[k] = (int)ceil(ddiv(d, h)) + 1;
+      G.step[k] = ddiv(d, (double)G.dims[k]);
+      ncell *= G.dims[k];
+    }
+    L = fmax(fmax(G.step[0], G.step[1]), G.step[2]);
+    G.L = L;
+    G.pad = 0.0;
+  }
+  G.ncell = ncell;
+  if (ncell > cell_cap) atomicOr(status, kStatusTableCells);
+  *g = G;
+}
+
+// --------------------------------------------------------------------------
+// Membership enumeration (count / fill)
+// --------------------------------------------------------------------------
+
+struct Emit {
+  int* count;
+  const int* start;
+  int* cursor;
+  int* entries;
+  long long entry_cap;
+  unsigned* status;
+  template <bool FILL>
+  __device__ __forceinline__ void put(long long idx, int atom, long long ncell) const {
+    if (idx < 0 || idx >= ncell) return;
+    if (!FILL) {
+      atomicAdd(&count[idx], 1);
+    } else {
+      int slot = atomicAdd(&cursor[idx], 1);
+      long long p = (long long)start[idx] + slot;
+      if (p < entry_cap) entries[p] = atom;
+      else atomicOr(status, kStatusTableEntries);
+    }
+  }
+};
+
+// CharmmReferenceGBSW.cpp:472-496 (STANDALONE) and CustomGBIntegral.cpp:198-227 (GRID).
+template <int MODE, bool FILL>
+__global__ void table_members_grid_kernel(const float4* __restrict__ pos, const double* __restrict__ radius, int n,
+                                          const TableGeom* __restrict__ gp, double h, double buffer, Emit em,
+                                          long long cell_cap) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  const TableGeom& g = *gp;
+  if (g.ncell > cell_cap) return;
+  const long long ncell = g.ncell;
+  for (int a = warp; a < n; a += (gridDim.x * blockDim.x) / kWarp) {
+    float4 p = pos[a];
+    const double c[3] = {(double)p.x, (double)p.y, (double)p.z};
+    double pad;
+    if (MODE == GBX_TABLE_STANDALONE) pad = g.pad;
+    else pad = dadd(dadd(radius[a], dmul(half_sqrt3(), h)), buffer);
+    const double pad2 = dmul(pad, pad);
+    int b[3], e[3];
+    for (int k = 0; k < 3; ++k) {
+      b[k] = (int)floor(ddiv(dsub(dsub(c[k], pad), g.min[k]), h));
+      e[k] = (int)ceil(ddiv(dsub(dadd(c[k], pad), g.min[k]), h));
+    }
+    const int nx = e[0] - b[0] + 1, ny = e[1] - b[1] + 1, nz = e[2] - b[2] + 1;
+    // non-finite or absurd inputs: skip the atom instead of looping on garbage bounds
+    if (!(nx >= 1 && ny >= 1 && nz >= 1 && nx <= 1024 && ny <= 1024 && nz <= 1024)) {
+      if (lane == 0) atomicOr(em.status, kStatusTableCells);
+      continue;
+    }
+    const int total = nx * ny * nz;
+    const long long sy = g.dims[2], sx = (long long)g.dims[1] * g.dims[2];
+    for (int t = lane; t < total; t += kWarp) {
+      const int i = b[0] + t / (ny * nz);
+      const int j = b[1] + (t / nz) % ny;
+      const int k = b[2] + t % nz;
+      const double d0 = dsub(dadd(g.min[0], dmul((double)i, h)), c[0]);
+      const double d1 = dsub(dadd(g.min[1], dmul((double)j, h)), c[1]);
+      const double d2 = dsub(dadd(g.min[2], dmul((double)k, h)), c[2]);
+      const double s = dadd(dadd(dmul(d0, d0), dmul(d1, d1)), dmul(d2, d2));
+      bool member;
+      if (MODE == GBX_TABLE_STANDALONE) member = __dsqrt_rn(s) < pad;
+      else member = s < pad2;
+      if (member) em.put<FILL>((long long)i * sx + (long long)j * sy + k, a, ncell);
+    }
+  }
+}
+
+// CustomGBIntegral.cpp:117-159 (PERIODIC): samples at the grid step, accumulated
+// by repeated addition exactly as the reference's for-loops do.
+template <bool FILL>
+__global__ void table_members_periodic_kernel(const float4* __restrict__ pos, const double* __restrict__ radius,
+                                              int n, const TableGeom* __restrict__ gp, double buffer, Emit em,
+                                              long long cell_cap, unsigned* __restrict__ status) {
+  __shared__ double s_samp[8][3][kMaxSamples];
+  const int wib = threadIdx.x / kWarp;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  const TableGeom& g = *gp;
+  if (g.ncell > cell_cap) return;
+  const long long ncell = g.ncell;
+  double (*samp)[kMaxSamples] = s_samp[wib];
+  for (int a = warp; a < n; a += (gridDim.x * blockDim.x) / kWarp) {
+    float4 p = pos[a];
+    const double c[3] = {(double)p.x, (double)p.y, (double)p.z};
+    const double L = g.L;
+    const double pad = dadd(dadd(radius[a], dmul(half_sqrt3(), L)), buffer);
+    const double pad2 = dmul(pad, pad);
+    int cnt[3] = {0, 0, 0};
+    // lanes 0..2 walk one axis each
+    if (lane < 3) {
+      const int k = lane;
+      double x = dsub(dsub(c[k], pad), L);
+      const double end = dadd(dadd(c[k], pad), L);
+      int m = 0;
+      while (x < end && m <= kMaxSamples) {
+        if (m < kMaxSamples) samp[k][m] = x;
+        ++m;
+        x = dadd(x, g.step[k]);
+      }
+      if (m > kMaxSamples) atomicOr(status, kStatusTableEntries);
+      cnt[0] = m;  // reused below via shuffle
+    }
+    __syncwarp();
+    for (int k = 0; k < 3; ++k) {
+      int v = __shfl_sync(0xffffffffu, cnt[0], k);
+      cnt[k] = v < kMaxSamples ? v : kMaxSamples;
+    }
+    const int total = cnt[0] * cnt[1] * cnt[2];
+    const long long sy = g.dims[2], sx = (long long)g.dims[1] * g.dims[2];
+    for (int t = lane; t < total; t += kWarp) {
+      const int kx = t / (cnt[1] * cnt[2]);
+      const int ky = (t / cnt[2]) % cnt[1];
+      const int kz = t % cnt[2];
+      const double xyz[3] = {samp[0][kx], samp[1][ky], samp[2][kz]};
+      int id[3];
+      bool inside = true;
+      for (int k = 0; k < 3; ++k) {
+        const double d = g.box[k];
+        const double x0 = dsub(xyz[k], dmul(d, floor(ddiv(dsub(xyz[k], g.min[k]), d))));
+        id[k] = (int)floor(ddiv(dsub(x0, g.min[k]), g.step[k]));
+        if (id[k] < 0 || id[k] >= g.dims[k]) inside = false;
+      }
+      const double e0 = dsub(xyz[0], c[0]), e1 = dsub(xyz[1], c[1]), e2 = dsub(xyz[2], c[2]);
+      const double s = dadd(dadd(dmul(e0, e0), dmul(e1, e1)), dmul(e2, e2));
+      if (s < pad2 && inside) em.put<FILL>((long long)id[0] * sx + (long long)id[1] * sy + id[2], a, ncell);
+    }
+    __syncwarp();
+  }
+}
+
+// --------------------------------------------------------------------------
+// Exclusive scan of the per-cell counts (three phases).
+// --------------------------------------------------------------------------
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x % kWarp, w = threadIdx.x / kWarp;
+  int x = v;
+  for (int off = 1; off < kWarp; off <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == kWarp - 1) s_warp[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < (int)(blockDim.x / kWarp) ? s_warp[lane] : 0;
+    for (int off = 1; off < kWarp; off <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, s, off);
+      if (lane >= off) s += y;
+    }
+    s_warp[lane] = s;
+  }
+  __syncthreads();
+  int base = w > 0 ? s_warp[w - 1] : 0;
+  *total = s_warp[blockDim.x / kWarp - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int* __restrict__ count,
+                                                                  const TableGeom* __restrict__ gp,
+                                                                  int* __restrict__ block_sums, long long cell_cap) {
+  __shared__ int s_warp[kWarp];
+  const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
+  const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
+  int v = 0;
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < ncell) v += count[base + k];
+  int total;
+  block_exclusive_scan(v, s_warp, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int* __restrict__ block_sums, int nblocks) {
+  __shared__ int s_warp[kWarp];
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < nblocks; b0 += kScanThreads) {
+    int i = b0 + threadIdx.x;
+    int v = i < nblocks ? block_sums[i] : 0;
+    int total;
+    int ex = block_exclusive_scan(v, s_warp, &total);
+    if (i < nblocks) block_sums[i] = ex + s_carry;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += total;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __restrict__ count,
+                                                                  TableGeom* __restrict__ gp,
+                                                                  const int* __restrict__ block_sums,
+                                                                  int* __restrict__ start, int* __restrict__ cursor,
+                                                                  long long cell_cap, long long entry_cap,
+                                                                  unsigned* __restrict__ status) {
+  __shared__ int s_warp[kWarp];
+  const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
+  const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int sum = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < ncell) ? count[base + k] : 0;
+    sum += v[k];
+  }
+  int total;
+  int ex = block_exclusive_scan(sum, s_warp, &total) + block_sums[blockIdx.x];
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < ncell) {
+      start[base + k] = ex;
+      cursor[base + k] = 0;
+    }
+    if (base + k == ncell - 1) {
+      start[ncell] = ex + v[k];
+      gp->total = (long long)ex + v[k];
+      if ((long long)ex + v[k] > entry_cap) atomicOr(status, kStatusTableEntries);
+    }
+    ex += v[k];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Per-cell rank sort (ascending atom index) and cap.
+// --------------------------------------------------------------------------
+constexpr int kSortWarps = 4;
+constexpr int kSortBuf = 512;  // per-warp shared staging; longer lists rank from global
+
+__global__ void __launch_bounds__(kSortWarps * kWarp) sort_cells_kernel(int* __restrict__ count,
+                                                                        const int* __restrict__ start,
+                                                                        int* __restrict__ entries,
+                                                                        const TableGeom* __restrict__ gp, int cap,
+                                                                        long long cell_cap, long long entry_cap,
+                                                                        unsigned* __restrict__ status) {
+  __shared__ int s_buf[kSortWarps][kSortBuf];
+  const int wib = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
+  if (gp->total > entry_cap) return;
+  int* buf = s_buf[wib];
+  for (long long c = (long long)blockIdx.x * kSortWarps + wib; c < ncell; c += (long long)gridDim.x * kSortWarps) {
+    const int cnt = count[c];
+    if (cnt == 0) continue;
+    const int s = start[c];
+    if (cnt > kSortBuf) {
+      if (cnt > kMaxSortSegment && lane == 0) atomicOr(status, kStatusSegmentTooLong);
+      if (cnt > kMaxSortSegment) continue;
+      // long list: ranks from global memory, results staged per lane
+      int vals[kMaxSortSegment / kWarp], ranks[kMaxSortSegment / kWarp];
+      int m = 0;
+      for (int p = lane; p < cnt; p += kWarp, ++m) {
+        const int v = entries[s + p];
+        int r = 0;
+        for (int q = 0; q < cnt; ++q) {
+          const int u = entries[s + q];
+          r += (u < v) || (u == v && q < p);
+        }
+        vals[m] = v;
+        ranks[m] = r;
+      }
+      __syncwarp();
+      for (int k = 0; k < m; ++k) entries[s + ranks[k]] = vals[k];
+    } else {
+      for (int p = lane; p < cnt; p += kWarp) buf[p] = entries[s + p];
+      __syncwarp();
+      for (int p = lane; p < cnt; p += kWarp) {
+        const int v = buf[p];
+        int r = 0;
+        for (int q = 0; q < cnt; ++q) {
+          const int u = buf[q];
+          r += (u < v) || (u == v && q < p);
+        }
+        entries[s + r] = v;
+      }
+    }
+    __syncwarp();
+    if (lane == 0 && cap > 0 && cnt > cap) count[c] = cap;
+  }
+}
+
+int grid_for(long long work, int per_block) {
+  long long b = (work + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > 1048576) b = 1048576;
+  return (int)b;
+}
+
+}  // namespace
+
+gbx_status launch_table_build(Context* ctx, const float4* pos) {
+  const gbx_config& c = ctx->cfg;
+  cudaStream_t st = ctx->stream;
+  table_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->d_radius, ctx->n, c.table_mode, c.grid_length,
+                                                c.table_buffer, c.switch_width, c.box[0], c.box[1], c.box[2],
+                                                ctx->d_geom, ctx->cell_cap, ctx->d_status);
+  const long long cells = ctx->cell_cap;
+  if (cells == 0) {
+    // sizing call: geometry only; the caller reads it back and allocates
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      ctx->last_error = std::string("table geometry launch: ") + cudaGetErrorString(e);
+      return GBX_ERR_CUDA;
+    }
+    return GBX_OK;
+  }
+  cudaMemsetAsync(ctx->d_cell_count, 0, sizeof(int) * cells, st);
+  Emit em{ctx->d_cell_count, ctx->d_cell_start, ctx->d_cell_cursor, ctx->d_entries, ctx->entry_cap, ctx->d_status};
+  const int threads = 256;
+  const int blocks = grid_for((long long)ctx->n * kWarp, threads);
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+      const int nb = grid_for(cells, kScanThreads * kScanItems);
+      scan_tiles_kernel<<<nb, kScanThreads, 0, st>>>(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums, cells);
+      scan_top_kernel<<<1, kScanThreads, 0, st>>>(ctx->d_block_sums, nb);
+      scan_apply_kernel<<<nb, kScanThreads, 0, st>>>(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums,
+                                                     ctx->d_cell_start, ctx->d_cell_cursor, cells, ctx->entry_cap,
+                                                     ctx->d_status);
+    }
+    const bool fill = pass == 1;
+    switch (c.table_mode) {
+      case GBX_TABLE_STANDALONE:
+        if (fill)
+          table_members_grid_kernel<GBX_TABLE_STANDALONE, true><<<blocks, threads, 0, st>>>(
+              pos, ctx->d_radius, ctx->n, ctx->d_geom, c.grid_length, c.table_buffer, em, cells);
+        else
+          table_members_grid_kernel<GBX_TABLE_STANDALONE, false><<<blocks, threads, 0, st>>>(
+              pos, ctx->d_radius, ctx->n, ctx->d_geom, c.grid_length, c.table_buffer, em, cells);
+        break;
+      case GBX_TABLE_GRID:
+        if (fill)
+          table_members_grid_kernel<GBX_TABLE_GRID, true><<<blocks, threads, 0, st>>>(
+              pos, ctx->d_radius, ctx->n, ctx->d_geom, c.grid_length, c.table_buffer, em, cells);
+        else
+          table_members_grid_kernel<GBX_TABLE_GRID, false><<<blocks, threads, 0, st>>>(
+              pos, ctx->d_radius, ctx->n, ctx->d_geom, c.grid_length, c.table_buffer, em, cells);
+        break;
+      default:
+        if (fill)
+          table_members_periodic_kernel<true><<<blocks, threads, 0, st>>>(pos, ctx->d_radius, ctx->n, ctx->d_geom,
+                                                                          c.table_buffer, em, cells, ctx->d_status);
+        else
+          table_members_periodic_kernel<false><<<blocks, threads, 0, st>>>(pos, ctx->d_radius, ctx->n, ctx->d_geom,
+                                                                           c.table_buffer, em, cells, ctx->d_status);
+        break;
+    }
+  }
+  sort_cells_kernel<<<grid_for(cells, kSortWarps), kSortWarps * kWarp, 0, st>>>(
+      ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries, ctx->d_geom, c.table_cap, cells, ctx->entry_cap,
+      ctx->d_status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ctx->last_error = std::string("table build launch: ") + cudaGetErrorString(e);
+    return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
+}  // namespace gbx

@@ -1,0 +1,245 @@
+"""CUDA path vs the FP64 oracle and the reference's golden vectors, through
+the C ABI.  Tolerances (FP32 arithmetic, FP64 Born-radius assembly):
+
+* lookup tables: bit-exact (counts and ascending lists)
+* Born radii: max relative error <= 1e-4
+* energy: relative error <= 2e-5
+* forces: relative RMS error <= 1e-4 (the benchmark spec's bound)
+"""
+import numpy as np
+import pytest
+
+from openmmcustomgbintegralforce_gb300._lib import Context, GBXError
+from openmmcustomgbintegralforce_gb300.globule import make_globule
+from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
+from oracle import oracle as O
+from tests.conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 2e-5
+F_TOL = 1e-4
+B_TOL = 1e-4
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def models_for(g):
+    box = box_for(g.positions, margin=1.0)
+    return {
+        "charmm_gbsw": GBModel.charmm_gbsw(),
+        "gbsw_integral": GBModel.gbsw_integral(),
+        "gbmv1": GBModel.gbmv1(box=box),
+        "gbmv2": GBModel.gbmv2(box=box),
+    }
+
+
+@pytest.fixture(scope="module")
+def glob1000():
+    return make_globule(1000, seed=11)
+
+
+@pytest.mark.parametrize("name", ["charmm_gbsw", "gbsw_integral", "gbmv1", "gbmv2"])
+def test_table_bit_exact(glob1000, name):
+    g = glob1000
+    m = models_for(g)[name]
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    ctx.execute_host(g.positions)
+    t = ctx.lookup_table()
+    ref = O.Oracle(m).table(g.positions, g.radius)
+    assert np.array_equal(t["dims"], ref["dims"])
+    assert np.array_equal(t["min"], ref["min"])
+    assert np.array_equal(t["counts"], ref["counts"])
+    assert np.array_equal(t["atoms"], ref["atoms"])
+
+
+@pytest.mark.parametrize("name", ["charmm_gbsw", "gbsw_integral", "gbmv1", "gbmv2"])
+def test_energy_forces_born_vs_oracle(glob1000, name):
+    g = glob1000
+    m = models_for(g)[name]
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    E, F = ctx.execute_host(g.positions)
+    ref = O.Oracle(m).energy_forces(g.positions, g.charge, g.radius)
+    B = ctx.born_radii()
+    I = ctx.integrals()
+    assert np.abs(B / ref["born"] - 1).max() < B_TOL
+    assert np.abs(I - ref["integrals"]).max() < 1e-5 * np.abs(ref["integrals"]).max()
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+
+
+def test_charmm_gbsw_vs_reference_golden():
+    """The reference's own CharmmGBSWForce outputs (1,000-atom globule)."""
+    gd = golden("gbsw_1000.npz")
+    n = len(gd["radius"])
+    ctx = Context(GBModel.charmm_gbsw(), n)
+    ctx.set_particle_parameters(gd["charge"], gd["radius"])
+    E, F = ctx.execute_host(gd["positions"])
+    assert abs(E / float(gd["energy"]) - 1) < E_TOL
+    assert rel_rms(F, gd["forces"]) < F_TOL
+    assert np.abs(ctx.born_radii() / gd["born"] - 1).max() < B_TOL
+
+
+def test_charmm_gbsw_table_vs_reference_golden():
+    gd = golden("gbsw_200.npz")
+    n = len(gd["radius"])
+    ctx = Context(GBModel.charmm_gbsw(), n)
+    ctx.set_particle_parameters(gd["charge"], gd["radius"])
+    ctx.execute_host(gd["positions"])
+    t = ctx.lookup_table()
+    assert np.array_equal(t["dims"], gd["table_dims"])
+    assert np.array_equal(t["counts"], gd["table_counts"])
+    assert np.array_equal(t["atoms"], gd["table_atoms"])
+
+
+def test_cutoff_quirk_vs_reference_golden():
+    gd = golden("gbsw_200_cutoff1.npz")
+    n = len(gd["radius"])
+    ctx = Context(GBModel.charmm_gbsw(cutoff=float(gd["cutoff"])), n)
+    ctx.set_particle_parameters(gd["charge"], gd["radius"])
+    E, F = ctx.execute_host(gd["positions"])
+    assert abs(E / float(gd["energy"]) - 1) < E_TOL
+    assert rel_rms(F, gd["forces"]) < F_TOL
+
+
+@pytest.mark.parametrize("tag", ["gbsw", "gbmv1", "gbmv2"])
+def test_integral_classes_vs_reference_golden(tag):
+    gd = golden("integrals_600.npz")
+    box = tuple(gd["box"])
+    m = {"gbsw": GBModel.gbsw_integral(), "gbmv1": GBModel.gbmv1(box=box), "gbmv2": GBModel.gbmv2(box=box)}[tag]
+    n = len(gd["radius"])
+    ctx = Context(m, n)
+    ctx.set_particle_parameters(gd["charge"], gd["radius"])
+    ctx.execute_host(gd["positions"])
+    t = ctx.lookup_table()
+    assert np.array_equal(t["counts"], gd[f"{tag}_table_counts"])
+    assert np.array_equal(t["atoms"], gd[f"{tag}_table_atoms"])
+    I = ctx.integrals()
+    ref = gd[f"{tag}_integrals"]
+    assert np.abs(I - ref).max() < 1e-5 * np.abs(ref).max()
+
+
+def test_bitwise_deterministic(glob1000):
+    g = glob1000
+    ctx = Context(GBModel.charmm_gbsw(), g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    E1, F1 = ctx.execute_host(g.positions)
+    E2, F2 = ctx.execute_host(g.positions)
+    assert E1 == E2
+    assert np.array_equal(F1, F2)
+
+
+def test_repeated_calls_do_not_accumulate(glob1000):
+    """The reference engine keeps stale accumulators between calls
+    (CharmmReferenceGBSW.cpp:235,562); each execute here is independent."""
+    g = glob1000
+    ctx = Context(GBModel.charmm_gbsw(), g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    rng = np.random.default_rng(0)
+    x2 = g.positions + rng.normal(0, 0.001, size=g.positions.shape)
+    ctx.execute_host(x2)
+    E, F = ctx.execute_host(g.positions)
+    ref = O.Oracle(GBModel.charmm_gbsw()).energy_forces(g.positions, g.charge, g.radius)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 33])
+def test_small_systems(n):
+    g = make_globule(max(n, 1), seed=2)
+    m = GBModel.charmm_gbsw()
+    ctx = Context(m, n)
+    ctx.set_particle_parameters(g.charge[:n], g.radius[:n])
+    E, F = ctx.execute_host(g.positions[:n])
+    ref = O.Oracle(m).energy_forces(g.positions[:n], g.charge[:n], g.radius[:n])
+    assert abs(E - ref["energy"]) <= E_TOL * abs(ref["energy"]) + 1e-6
+    assert np.abs(F - ref["forces"]).max() <= 1e-4 * (np.abs(ref["forces"]).max() + 1e-3)
+
+
+def test_invalid_inputs_raise():
+    g = make_globule(10, seed=1)
+    ctx = Context(GBModel.charmm_gbsw(), 10)
+    bad = g.radius.copy()
+    bad[3] = -1.0
+    with pytest.raises(GBXError):
+        ctx.set_particle_parameters(g.charge, bad)
+    x = g.positions.copy()
+    x[0, 0] = np.nan
+    ctx.set_particle_parameters(g.charge, g.radius)
+    with pytest.raises(GBXError):
+        ctx.execute_host(x)
+    with pytest.raises(GBXError):
+        ctx.set_particle_parameters(g.charge[:5], g.radius[:5])
+
+
+def test_adjoint_vs_oracle(glob1000):
+    g = glob1000
+    m = GBModel.charmm_gbsw()
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    out = ctx.adjoint(g.positions)
+    ref = O.Oracle(m).energy_forces(g.positions, g.charge, g.radius, adjoint=True)
+    assert abs(out["energy"] / ref["energy"] - 1) < E_TOL
+    assert rel_rms(out["forces"], ref["forces"]) < F_TOL
+    assert rel_rms(out["dEdq"], ref["dEdq"]) < 1e-4
+    assert rel_rms(out["dEdR"], ref["dEdR"]) < 1e-3
+    assert np.abs(out["dEdalpha"] / ref["dEdalpha"] - 1).max() < 1e-4
+
+
+def test_api_mirror_kernels(glob1000):
+    from openmmcustomgbintegralforce_gb300 import api
+
+    g = glob1000
+    f = api.CharmmGBSWForce()
+    for i in range(g.n):
+        f.addParticle(g.charge[i], g.radius[i], 1.0)
+    k = api.CalcCharmmGBSWForceKernel()
+    k.initialize(g.n, f)
+    E, F = k.execute(g.positions)
+    ref = O.Oracle(GBModel.charmm_gbsw()).energy_forces(g.positions, g.charge, g.radius)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    # updateParametersInContext
+    f.setParticleParameters(0, 0.0, g.radius[0], 1.0)
+    f.updateParametersInContext(k)
+    q = g.charge.copy()
+    q[0] = 0.0
+    E2, _ = k.execute(g.positions)
+    ref2 = O.Oracle(GBModel.charmm_gbsw()).energy_forces(g.positions, q, g.radius)
+    assert abs(E2 / ref2["energy"] - 1) < E_TOL
+
+    gm = api.canonical_gbmv_force(api.GBMVIntegralTypeII)
+    for i in range(g.n):
+        gm.addParticle([g.charge[i], g.radius[i]])
+    box = box_for(g.positions, margin=1.0)
+    kk = api.CalcCharmmGBMVForceKernel(box=box)
+    kk.initialize(g.n, gm)
+    E3, F3 = kk.execute(g.positions)
+    ref3 = O.Oracle(GBModel.gbmv2(box=box)).energy_forces(g.positions, g.charge, g.radius)
+    assert abs(E3 / ref3["energy"] - 1) < E_TOL
+    assert rel_rms(F3, ref3["forces"]) < F_TOL
+
+
+def test_device_buffers_match_host_path(glob1000):
+    torch = pytest.importorskip("torch")
+    g = glob1000
+    ctx = Context(GBModel.charmm_gbsw(), g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    E, F = ctx.execute_host(g.positions)
+    dev = torch.device("cuda:0")
+    posq = torch.zeros((g.n, 4), dtype=torch.float32, device=dev)
+    posq[:, :3] = torch.from_numpy(g.positions.astype(np.float32)).to(dev)
+    stride = ((g.n + 31) // 32) * 32
+    force = torch.zeros(3 * stride, dtype=torch.int64, device=dev)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    ctx.execute_device(posq.data_ptr(), force.data_ptr(), stride, energy.data_ptr(), 1 | 2 | 4,
+                       torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    fx = force.cpu().numpy().astype(np.float64) / 2.0 ** 32
+    Fd = np.stack([fx[:g.n], fx[stride:stride + g.n], fx[2 * stride:2 * stride + g.n]], axis=1)
+    assert float(energy.cpu()[0]) == E
+    assert np.array_equal(Fd, F)
