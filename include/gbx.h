@@ -92,8 +92,22 @@ typedef struct {
   double cutoff;        /* <= 0: full N^2 pair term */
   int cutoff_chain_quirk; /* drop chain terms beyond the cutoff (CharmmReferenceGBSW.cpp:291-292) */
   int skip_empty;       /* GBSW: an empty list means V = 1 */
-  int reserved[8];
+  int table_policy;     /* GBX_TABLE_POLICY_* */
+  int reserved_i;
+  double tight_grid_length; /* cell edge of the exact GBSW table (nm); <= 0: 0.1 */
+  int reserved[4];
 } gbx_config;
+
+/* Which table the integrals read.  The reference's standalone GBSW table
+ * (GBX_TABLE_STANDALONE) pads every cell by more than any switching shell
+ * can reach, so the volume it yields is the exact product over all atoms.
+ * AUTO then evaluates the integrals on a tighter table that provably holds
+ * the same atoms for every point (sphere-box membership with a safety
+ * margin, fully buried cells marked), which gives the same volumes with a
+ * fraction of the list work; the reference table is still built on request
+ * (gbx_build_lookup_table).  For the other table modes the list contents
+ * define the result, so the reference table is always used. */
+enum { GBX_TABLE_POLICY_AUTO = 0, GBX_TABLE_POLICY_REFERENCE = 1 };
 
 /* Library / error helpers. */
 GBX_API const char* gbx_status_string(gbx_status s);

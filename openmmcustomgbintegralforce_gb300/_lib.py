@@ -62,7 +62,10 @@ class GbxConfig(ctypes.Structure):
         ("cutoff", ctypes.c_double),
         ("cutoff_chain_quirk", ctypes.c_int),
         ("skip_empty", ctypes.c_int),
-        ("reserved", ctypes.c_int * 8),
+        ("table_policy", ctypes.c_int),
+        ("reserved_i", ctypes.c_int),
+        ("tight_grid_length", ctypes.c_double),
+        ("reserved", ctypes.c_int * 4),
     ]
 
     @staticmethod
@@ -86,6 +89,8 @@ class GbxConfig(ctypes.Structure):
         c.cutoff = m.cutoff
         c.cutoff_chain_quirk = 1 if m.cutoff_chain_quirk else 0
         c.skip_empty = 1 if m.skip_empty else 0
+        c.table_policy = 1 if m.reference_table else 0
+        c.tight_grid_length = m.tight_h
         return c
 
 

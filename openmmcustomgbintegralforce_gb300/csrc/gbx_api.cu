@@ -141,10 +141,18 @@ int choose_chunks(int n, int Q) {
   return c;
 }
 
+// Exact-table kernels run one warp per (atom, chunk) with lanes over points:
+// enough warps for ~48 per SM, and >= 64 points (2 per lane) per chunk.
+int choose_tight_chunks(int n, int Q) {
+  int c = (152 * 48 + n - 1) / n;
+  c = std::max(1, std::min(c, std::max(1, Q / 64)));
+  return c;
+}
+
 gbx_status alloc_atom_buffers(Context* ctx) {
   const int n = ctx->n;
   const int Q = ctx->cfg.n_radial * ctx->cfg.lebedev_order;
-  ctx->n_chunks = choose_chunks(n, Q);
+  ctx->n_chunks = ctx->use_tight ? choose_tight_chunks(n, Q) : choose_chunks(n, Q);
   GBX_TRY(dalloc(ctx, &ctx->d_radius, n));
   GBX_TRY(dalloc(ctx, &ctx->d_charge, n));
   GBX_TRY(dalloc(ctx, &ctx->d_par, n));
@@ -167,6 +175,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_status, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_work, 4));
   GBX_TRY(dalloc(ctx, &ctx->d_geom, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_tgeom, 1));
   GBX_CUDA(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
   GBX_CUDA(cudaMemset(ctx->d_work, 0, sizeof(unsigned long long) * 4));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_pos, sizeof(float4) * n));
@@ -201,7 +210,10 @@ gbx_status build_table_checked(Context* ctx, bool check) {
   for (int attempt = 0; attempt < 3; ++attempt) {
     GBX_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream));
     GBX_TRY(gbx::launch_table_build(ctx, ctx->d_pos));
-    if (!check && ctx->cell_cap > 0 && ctx->entry_cap > 0) return GBX_OK;
+    if (!check && ctx->cell_cap > 0 && ctx->entry_cap > 0) {
+      ctx->table_valid = true;
+      return GBX_OK;
+    }
     unsigned st = 0;
     gbx::TableGeom g;
     GBX_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
@@ -233,6 +245,61 @@ gbx_status build_table_checked(Context* ctx, bool check) {
   return GBX_ERR_TABLE_TOO_LARGE;
 }
 
+gbx_status grow_tight(Context* ctx, long long cells, long long entries) {
+  if (cells > ctx->tcell_cap) {
+    const long long cap = cells + cells / 4 + 1024;
+    GBX_TRY(dalloc(ctx, &ctx->d_tcount, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tstart, cap + 1));
+    GBX_TRY(dalloc(ctx, &ctx->d_tcursor, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tburied, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tblock_sums, cap / (1024 * 8) + 2));
+    ctx->tcell_cap = cap;
+  }
+  if (entries > ctx->tentry_cap) {
+    const long long cap = entries + entries / 4 + 4096;
+    if (cap > 0x7fffffffLL) {
+      ctx->last_error = "exact table would exceed 2^31 entries";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    GBX_TRY(dalloc(ctx, &ctx->d_tentry, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tindex, cap));
+    ctx->tentry_cap = cap;
+  }
+  return GBX_OK;
+}
+
+// Exact-table counterpart of build_table_checked.
+gbx_status build_tight_checked(Context* ctx, bool check) {
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    GBX_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream));
+    GBX_TRY(gbx::launch_tight_build(ctx, ctx->d_pos));
+    if (!check && ctx->tcell_cap > 0 && ctx->tentry_cap > 0) return GBX_OK;
+    unsigned st = 0;
+    gbx::TableGeom g;
+    GBX_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaMemcpyAsync(&g, ctx->d_tgeom, sizeof(g), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st & gbx::kStatusSegmentTooLong) {
+      ctx->last_error = "an exact-table cell holds more atoms than the sort supports";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    const bool cells_short = (st & gbx::kStatusTableCells) != 0;
+    const bool entries_short = (st & gbx::kStatusTableEntries) != 0;
+    if (!cells_short && !entries_short) {
+      ctx->tight_valid = true;
+      return GBX_OK;
+    }
+    if (cells_short && (g.ncell <= ctx->tcell_cap || g.ncell > ((long long)1 << 31))) {
+      ctx->last_error = "exact table geometry out of range, check atom positions";
+      return GBX_ERR_TABLE_TOO_LARGE;
+    }
+    long long entries = cells_short ? (long long)ctx->n * 128 : g.total;
+    GBX_TRY(grow_tight(ctx, g.ncell, std::max(entries, (long long)ctx->n)));
+  }
+  ctx->last_error = "exact table did not fit after resizing";
+  return GBX_ERR_TABLE_TOO_LARGE;
+}
+
 gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* force, int stride, double* energy,
                         bool check, bool adjoint, bool count_work) {
   int stage = 0;
@@ -244,7 +311,9 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_stage_positions(ctx, posq));
   GBX_TRY(mark());
-  GBX_TRY(build_table_checked(ctx, check));
+  ctx->table_valid = false;
+  if (ctx->use_tight) GBX_TRY(build_tight_checked(ctx, check || !ctx->tight_valid));
+  else GBX_TRY(build_table_checked(ctx, check));
   if (count_work) GBX_CUDA(cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * 4, ctx->stream));
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_integrals(ctx, ctx->d_pos, count_work));
@@ -392,6 +461,9 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
     delete ctx;
     return GBX_ERR_CUDA;
   }
+  ctx->use_tight = cfg->model == GBX_MODEL_GBSW && cfg->table_mode == GBX_TABLE_STANDALONE &&
+                   cfg->table_policy == GBX_TABLE_POLICY_AUTO;
+  ctx->tight_h = cfg->tight_grid_length > 0 ? cfg->tight_grid_length : 0.1;
   s = upload_quadrature(ctx);
   if (s == GBX_OK) s = alloc_atom_buffers(ctx);
   if (s == GBX_OK && cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) s = GBX_ERR_CUDA;
@@ -418,7 +490,9 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_cell_cursor, ctx->d_entries,
                   ctx->d_block_sums, ctx->d_reduce, ctx->d_pos, ctx->d_J, ctx->d_born, ctx->d_bornf, ctx->d_dBdJ,
                   ctx->d_integrals, ctx->d_dEdB_fx, ctx->d_dEdJ, ctx->d_energy_part, ctx->d_force_fx,
-                  ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work};
+                  ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
+                  ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
+                  ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)
@@ -495,7 +569,7 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
     GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
   }
   double* e = (flags & GBX_EXEC_ENERGY) ? energy : ctx->d_energy;
-  const bool check = (flags & GBX_EXEC_CHECK) || ctx->cell_cap == 0 || !ctx->table_valid;
+  const bool check = (flags & GBX_EXEC_CHECK) || (ctx->use_tight ? ctx->tcell_cap == 0 : ctx->cell_cap == 0);
   return run_pipeline(ctx, reinterpret_cast<const float4*>(posq), f, stride, e, check, false,
                       (flags & GBX_EXEC_COUNT_WORK) != 0);
 }
@@ -617,7 +691,12 @@ gbx_status gbx_get_lookup_table(gbx_context* handle, int dims[3], double mn[3], 
                                 int32_t* counts, int64_t* total, int32_t* atoms) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
-  if (!ctx->table_valid) return GBX_ERR_NOT_READY;
+  if (!ctx->table_valid) {
+    // the last execute integrated on the exact table: build the reference
+    // table from the positions it staged
+    if (!ctx->have_result) return GBX_ERR_NOT_READY;
+    GBX_TRY(build_table_checked(ctx, true));
+  }
   gbx::TableGeom g;
   GBX_CUDA(cudaStreamSynchronize(ctx->stream));
   GBX_CUDA(cudaMemcpy(&g, ctx->d_geom, sizeof(g), cudaMemcpyDeviceToHost));

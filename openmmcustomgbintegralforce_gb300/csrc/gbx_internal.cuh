@@ -89,6 +89,21 @@ struct Context {
   double* d_reduce = nullptr;    // geometry reduction scratch
   bool table_valid = false;
 
+  // exact GBSW table (GBX_TABLE_POLICY_AUTO on a standalone table):
+  // count[c] = -1 marks a cell every point of which is buried
+  bool use_tight = false;
+  double tight_h = 0.1;
+  TableGeom* d_tgeom = nullptr;
+  long long tcell_cap = 0, tentry_cap = 0;
+  int* d_tcount = nullptr;
+  int* d_tstart = nullptr;
+  int* d_tcursor = nullptr;
+  int* d_tburied = nullptr;
+  int* d_tblock_sums = nullptr;
+  float4* d_tentry = nullptr;    // (x, y, z, R') per list entry
+  int* d_tindex = nullptr;       // atom index per list entry
+  bool tight_valid = false;
+
   // per-step state
   float4* d_pos = nullptr;       // internal positions (x, y, z, 0)
   int n_chunks = 0;              // quadrature chunks per atom
@@ -145,6 +160,7 @@ __host__ __device__ __forceinline__ double fixed_to_double(unsigned long long v)
 
 gbx_status launch_stage_positions(Context* ctx, const float4* posq);
 gbx_status launch_table_build(Context* ctx, const float4* pos);
+gbx_status launch_tight_build(Context* ctx, const float4* pos);
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);

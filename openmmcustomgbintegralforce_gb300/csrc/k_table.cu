@@ -16,13 +16,12 @@
 #include <math.h>
 
 #include "gbx_internal.cuh"
+#include "scan.cuh"
 
 namespace gbx {
 namespace {
 
 constexpr int kGeomThreads = 1024;
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 8;
 constexpr int kMaxSamples = 96;  // samples per axis in the periodic branch
 
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
@@ -287,95 +286,6 @@ __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, co
 }
 
 // --------------------------------------------------------------------------
-// Exclusive scan of the per-cell counts (three phases).
-// --------------------------------------------------------------------------
-__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* total) {
-  const int lane = threadIdx.x % kWarp, w = threadIdx.x / kWarp;
-  int x = v;
-  for (int off = 1; off < kWarp; off <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, off);
-    if (lane >= off) x += y;
-  }
-  if (lane == kWarp - 1) s_warp[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    int s = lane < (int)(blockDim.x / kWarp) ? s_warp[lane] : 0;
-    for (int off = 1; off < kWarp; off <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, s, off);
-      if (lane >= off) s += y;
-    }
-    s_warp[lane] = s;
-  }
-  __syncthreads();
-  int base = w > 0 ? s_warp[w - 1] : 0;
-  *total = s_warp[blockDim.x / kWarp - 1];
-  __syncthreads();
-  return base + x - v;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int* __restrict__ count,
-                                                                  const TableGeom* __restrict__ gp,
-                                                                  int* __restrict__ block_sums, long long cell_cap) {
-  __shared__ int s_warp[kWarp];
-  const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
-  const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
-  int v = 0;
-  for (int k = 0; k < kScanItems; ++k)
-    if (base + k < ncell) v += count[base + k];
-  int total;
-  block_exclusive_scan(v, s_warp, &total);
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int* __restrict__ block_sums, int nblocks) {
-  __shared__ int s_warp[kWarp];
-  __shared__ int s_carry;
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (int b0 = 0; b0 < nblocks; b0 += kScanThreads) {
-    int i = b0 + threadIdx.x;
-    int v = i < nblocks ? block_sums[i] : 0;
-    int total;
-    int ex = block_exclusive_scan(v, s_warp, &total);
-    if (i < nblocks) block_sums[i] = ex + s_carry;
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __restrict__ count,
-                                                                  TableGeom* __restrict__ gp,
-                                                                  const int* __restrict__ block_sums,
-                                                                  int* __restrict__ start, int* __restrict__ cursor,
-                                                                  long long cell_cap, long long entry_cap,
-                                                                  unsigned* __restrict__ status) {
-  __shared__ int s_warp[kWarp];
-  const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
-  const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
-  int v[kScanItems];
-  int sum = 0;
-  for (int k = 0; k < kScanItems; ++k) {
-    v[k] = (base + k < ncell) ? count[base + k] : 0;
-    sum += v[k];
-  }
-  int total;
-  int ex = block_exclusive_scan(sum, s_warp, &total) + block_sums[blockIdx.x];
-  for (int k = 0; k < kScanItems; ++k) {
-    if (base + k < ncell) {
-      start[base + k] = ex;
-      cursor[base + k] = 0;
-    }
-    if (base + k == ncell - 1) {
-      start[ncell] = ex + v[k];
-      gp->total = (long long)ex + v[k];
-      if ((long long)ex + v[k] > entry_cap) atomicOr(status, kStatusTableEntries);
-    }
-    ex += v[k];
-  }
-}
-
-// --------------------------------------------------------------------------
 // Per-cell rank sort (ascending atom index) and cap.
 // --------------------------------------------------------------------------
 constexpr int kSortWarps = 4;
@@ -462,14 +372,9 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
   const int threads = 256;
   const int blocks = grid_for((long long)ctx->n * kWarp, threads);
   for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1) {
-      const int nb = grid_for(cells, kScanThreads * kScanItems);
-      scan_tiles_kernel<<<nb, kScanThreads, 0, st>>>(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums, cells);
-      scan_top_kernel<<<1, kScanThreads, 0, st>>>(ctx->d_block_sums, nb);
-      scan_apply_kernel<<<nb, kScanThreads, 0, st>>>(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums,
-                                                     ctx->d_cell_start, ctx->d_cell_cursor, cells, ctx->entry_cap,
-                                                     ctx->d_status);
-    }
+    if (pass == 1)
+      launch_scan(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums, ctx->d_cell_start, ctx->d_cell_cursor, cells,
+                  ctx->entry_cap, ctx->d_status, st);
     const bool fill = pass == 1;
     switch (c.table_mode) {
       case GBX_TABLE_STANDALONE:

@@ -1,0 +1,271 @@
+// Exact GBSW lookup table.
+//
+// The GBSW volume of a point is V(p) = 0 if some atom buries it
+// (|p - x_j| <= R'_j - w), else the product of u_j over the atoms whose
+// switching shell holds it (R'_j - w < |p - x_j| < R'_j + w)
+// (CharmmReferenceGBSW.cpp:616-639).  The reference's standalone table pads
+// every grid point by buffer + maxR + w + (sqrt3/2) h + 1e-6 (:454-455), more
+// than any shell reaches from anywhere in the queried cell, so its lists give
+// exactly this V.  This table gives the same V with far shorter lists:
+//
+//   * cell c (edge h, default 0.1 nm) lists atom j when the distance from
+//     x_j to the cell's box is below R'_j + w + eps;
+//   * a cell whose farthest corner lies within R'_j - w - eps of some x_j is
+//     buried: V = 0 for every point in it, no list is read;
+//   * the grid spans the atoms' bounding box plus max(R') + w + h, so a
+//     point outside it touches no shell (V = 1).
+//
+// eps (2e-5 nm plus 2 ulp of the largest coordinate) covers the FP32
+// rounding of both the build and the point-to-cell assignment, so every
+// atom a point needs is in the list of whichever neighbouring cell its FP32
+// coordinates select.  Entries are stored inline (x, y, z, R') and sorted by
+// the distance from the cell centre to the atom's burying sphere, so a
+// buried point usually stops at its first entry.
+#include <math.h>
+
+#include "gbx_internal.cuh"
+#include "scan.cuh"
+
+namespace gbx {
+namespace {
+
+constexpr int kGeomThreads = 1024;
+constexpr int kSortWarps = 4;
+constexpr int kSortBuf = 256;
+
+__global__ void __launch_bounds__(kGeomThreads) tight_geom_kernel(const float4* __restrict__ pos, int n, double h,
+                                                                  double w, TableGeom* __restrict__ g,
+                                                                  long long cell_cap, unsigned* __restrict__ status) {
+  __shared__ float s_min[3][kGeomThreads / kWarp], s_max[3][kGeomThreads / kWarp], s_r[kGeomThreads / kWarp];
+  const int t = threadIdx.x;
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY}, rmax = 0.f;
+  for (int a = t; a < n; a += blockDim.x) {
+    const float4 p = pos[a];
+    mn[0] = fminf(mn[0], p.x);
+    mn[1] = fminf(mn[1], p.y);
+    mn[2] = fminf(mn[2], p.z);
+    mx[0] = fmaxf(mx[0], p.x);
+    mx[1] = fmaxf(mx[1], p.y);
+    mx[2] = fmaxf(mx[2], p.z);
+    rmax = fmaxf(rmax, p.w);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+    }
+    rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+  }
+  if (t % kWarp == 0) {
+    for (int k = 0; k < 3; ++k) {
+      s_min[k][t / kWarp] = mn[k];
+      s_max[k][t / kWarp] = mx[k];
+    }
+    s_r[t / kWarp] = rmax;
+  }
+  __syncthreads();
+  if (t != 0) return;
+  for (int ww = 0; ww < kGeomThreads / kWarp; ++ww) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fminf(mn[k], s_min[k][ww]);
+      mx[k] = fmaxf(mx[k], s_max[k][ww]);
+    }
+    rmax = fmaxf(rmax, s_r[ww]);
+  }
+  TableGeom G;
+  const double margin = (double)rmax + w + h;
+  long long ncell = 1;
+  double amax = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    G.min[k] = (double)mn[k] - margin;
+    G.dims[k] = (int)ceil(((double)mx[k] - (double)mn[k] + 2.0 * margin) / h) + 1;
+    if (!(G.dims[k] >= 1 && G.dims[k] <= 65536)) {
+      atomicOr(status, kStatusTableCells);
+      G.dims[k] = 1;
+    }
+    G.max[k] = G.min[k] + G.dims[k] * h;
+    G.step[k] = h;
+    G.box[k] = 0.0;
+    ncell *= G.dims[k];
+    amax = fmax(amax, fmax(fabs((double)mn[k]), fabs((double)mx[k])));
+  }
+  G.mode = -1;
+  G.L = h;
+  // membership margin: FP32 rounding of cell coordinates and distances
+  G.pad = 2e-5 + 4.0 * 1.1920929e-7 * (amax + 2.0 * margin);
+  G.total = 0;
+  G.ncell = ncell;
+  if (ncell > cell_cap) atomicOr(status, kStatusTableCells);
+  *g = G;
+}
+
+struct TightArgs {
+  const float4* pos;  // x, y, z, R'
+  int n;
+  const TableGeom* geom;
+  float w;
+  int* count;
+  const int* start;
+  int* cursor;
+  int* buried;
+  float4* entry;
+  int* index;
+  long long cell_cap, entry_cap;
+  unsigned* status;
+};
+
+template <bool FILL>
+__global__ void tight_members_kernel(TightArgs a) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  const TableGeom& g = *a.geom;
+  if (g.ncell > a.cell_cap) return;
+  const float h = (float)g.step[0];
+  const float inv_h = (float)(1.0 / g.step[0]);
+  const float eps = (float)g.pad;
+  const long long sx = (long long)g.dims[1] * g.dims[2], sy = g.dims[2];
+  for (int at = warp; at < a.n; at += (gridDim.x * blockDim.x) / kWarp) {
+    const float4 p = a.pos[at];
+    // coordinates relative to the grid origin
+    const float x[3] = {(float)((double)p.x - g.min[0]), (float)((double)p.y - g.min[1]),
+                        (float)((double)p.z - g.min[2])};
+    const float reach = p.w + a.w + eps;
+    const float bury = p.w - a.w - eps;
+    int b[3], e[3];
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+      b[k] = max(0, (int)floorf((x[k] - reach) * inv_h));
+      e[k] = min(g.dims[k] - 1, (int)floorf((x[k] + reach) * inv_h));
+      if (!(e[k] >= b[k] && e[k] - b[k] < 256)) ok = false;
+    }
+    if (!ok) {
+      if (lane == 0) atomicOr(a.status, kStatusTableCells);
+      continue;
+    }
+    const int ny = e[1] - b[1] + 1, nz = e[2] - b[2] + 1;
+    const int total = (e[0] - b[0] + 1) * ny * nz;
+    for (int t = lane; t < total; t += kWarp) {
+      const int c[3] = {b[0] + t / (ny * nz), b[1] + (t / nz) % ny, b[2] + t % nz};
+      float near2 = 0.f, far2 = 0.f;
+      for (int k = 0; k < 3; ++k) {
+        const float lo = c[k] * h, hi = lo + h;
+        const float dn = fmaxf(fmaxf(lo - x[k], x[k] - hi), 0.f);
+        const float df = fmaxf(x[k] - lo, hi - x[k]);
+        near2 = fmaf(dn, dn, near2);
+        far2 = fmaf(df, df, far2);
+      }
+      if (!(near2 < reach * reach)) continue;
+      const long long cell = c[0] * sx + c[1] * sy + c[2];
+      if (!FILL) {
+        atomicAdd(&a.count[cell], 1);
+        if (bury > 0.f && far2 <= bury * bury) atomicOr(&a.buried[cell], 1);
+      } else {
+        const int slot = atomicAdd(&a.cursor[cell], 1);
+        const long long o = (long long)a.start[cell] + slot;
+        if (o < a.entry_cap) {
+          a.entry[o] = p;
+          a.index[o] = at;
+        } else {
+          atomicOr(a.status, kStatusTableEntries);
+        }
+      }
+    }
+  }
+}
+
+// Sort each list by (distance from the cell centre to the atom's burying
+// sphere, atom index) -- a deterministic order whatever the fill order was --
+// and mark buried cells with count -1.
+__global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __restrict__ count,
+                                                                        const int* __restrict__ start,
+                                                                        const int* __restrict__ buried,
+                                                                        float4* __restrict__ entry,
+                                                                        int* __restrict__ index,
+                                                                        const TableGeom* __restrict__ gp, float w,
+                                                                        long long cell_cap, long long entry_cap,
+                                                                        unsigned* __restrict__ status) {
+  __shared__ float4 s_e[kSortWarps][kSortBuf];
+  __shared__ int s_i[kSortWarps][kSortBuf];
+  __shared__ float s_k[kSortWarps][kSortBuf];
+  const int wib = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const TableGeom& g = *gp;
+  if (g.ncell > cell_cap || g.total > entry_cap) return;
+  const long long ncell = g.ncell;
+  const long long sx = (long long)g.dims[1] * g.dims[2];
+  for (long long c = (long long)blockIdx.x * kSortWarps + wib; c < ncell; c += (long long)gridDim.x * kSortWarps) {
+    const int cnt = count[c];
+    if (cnt == 0) continue;
+    if (buried[c]) {
+      if (lane == 0) count[c] = -1;
+      continue;
+    }
+    if (cnt > kSortBuf) {
+      if (lane == 0) atomicOr(status, kStatusSegmentTooLong);
+      continue;
+    }
+    const int s = start[c];
+    const int cx = (int)(c / sx), cy = (int)((c / g.dims[2]) % g.dims[1]), cz = (int)(c % g.dims[2]);
+    const double ctr[3] = {g.min[0] + (cx + 0.5) * g.step[0], g.min[1] + (cy + 0.5) * g.step[1],
+                           g.min[2] + (cz + 0.5) * g.step[2]};
+    for (int q = lane; q < cnt; q += kWarp) {
+      const float4 e = entry[s + q];
+      s_e[wib][q] = e;
+      s_i[wib][q] = index[s + q];
+      const float dx = (float)((double)e.x - ctr[0]), dy = (float)((double)e.y - ctr[1]),
+                  dz = (float)((double)e.z - ctr[2]);
+      s_k[wib][q] = sqrtf(dx * dx + dy * dy + dz * dz) - (e.w - w);
+    }
+    __syncwarp();
+    for (int q = lane; q < cnt; q += kWarp) {
+      const float kq = s_k[wib][q];
+      const int iq = s_i[wib][q];
+      int r = 0;
+      for (int o = 0; o < cnt; ++o) {
+        const float ko = s_k[wib][o];
+        r += (ko < kq) || (ko == kq && s_i[wib][o] < iq);
+      }
+      entry[s + r] = s_e[wib][q];
+      index[s + r] = iq;
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+gbx_status launch_tight_build(Context* ctx, const float4* pos) {
+  cudaStream_t st = ctx->stream;
+  const double h = ctx->tight_h;
+  tight_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->n, h, ctx->cfg.switch_width, ctx->d_tgeom, ctx->tcell_cap,
+                                                ctx->d_status);
+  const long long cells = ctx->tcell_cap;
+  if (cells > 0) {
+    cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * cells, st);
+    cudaMemsetAsync(ctx->d_tburied, 0, sizeof(int) * cells, st);
+    TightArgs a{pos,           ctx->n,          ctx->d_tgeom,   (float)ctx->cfg.switch_width,
+                ctx->d_tcount, ctx->d_tstart,   ctx->d_tcursor, ctx->d_tburied,
+                ctx->d_tentry, ctx->d_tindex,   cells,          ctx->tentry_cap,
+                ctx->d_status};
+    const int threads = 256;
+    long long blocks = ((long long)ctx->n * kWarp + threads - 1) / threads;
+    if (blocks > 65535) blocks = 65535;
+    tight_members_kernel<false><<<(int)blocks, threads, 0, st>>>(a);
+    launch_scan(ctx->d_tcount, ctx->d_tgeom, ctx->d_tblock_sums, ctx->d_tstart, ctx->d_tcursor, cells,
+                ctx->tentry_cap, ctx->d_status, st);
+    tight_members_kernel<true><<<(int)blocks, threads, 0, st>>>(a);
+    long long sb = (cells + kSortWarps - 1) / kSortWarps;
+    if (sb > 1048576) sb = 1048576;
+    tight_sort_kernel<<<(int)sb, kSortWarps * kWarp, 0, st>>>(ctx->d_tcount, ctx->d_tstart, ctx->d_tburied,
+                                                               ctx->d_tentry, ctx->d_tindex, ctx->d_tgeom,
+                                                               (float)ctx->cfg.switch_width, cells, ctx->tentry_cap,
+                                                               ctx->d_status);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ctx->last_error = std::string("tight table launch: ") + cudaGetErrorString(e);
+    return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
+}  // namespace gbx

@@ -145,6 +145,27 @@ __device__ __forceinline__ float gbsw_volume(const ModelConst& m, const float4* 
   return V;
 }
 
+// The same volume reading inline (x, y, z, R') entries of the exact table.
+template <class W>
+__device__ __forceinline__ float gbsw_volume_inline(const ModelConst& m, const float4* __restrict__ list, int cnt,
+                                                    const float4 xi, const float4 v, W& wk) {
+  float V = 1.0f;
+  for (int l = 0; l < cnt; ++l) {
+    const float4 a = __ldg(list + l);
+    const float dx = (a.x - xi.x) - v.x, dy = (a.y - xi.y) - v.y, dz = (a.z - xi.z) - v.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float lo = a.w - m.sw, hi = a.w + m.sw;
+    wk.eval();
+    if (r2 <= lo * lo) return 0.0f;
+    if (r2 < hi * hi) {
+      wk.shell();
+      const float dr = sqrtf(r2) - a.w;
+      V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+    }
+  }
+  return V;
+}
+
 // GBMV-I, GBMVIntegralTypeI.cpp:155-173: S = sum_j exp(gamma_j r^4).
 template <class W>
 __device__ __forceinline__ float gbmv1_sum(const float4* __restrict__ pos, const int* __restrict__ list, int cnt,
@@ -413,6 +434,194 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// GBSW on the exact table (k_tight.cu).  One warp per (atom, quadrature
+// chunk), lanes over quadrature points: the atom is warp-uniform, the
+// per-atom sums are fixed-shape warp reductions, and the atoms a warp's
+// lanes scatter forces to in one instruction are spread around the sphere.
+// ---------------------------------------------------------------------------
+struct TightTable {
+  const TableGeom* geom;
+  const int* count;   // -1: buried cell
+  const int* start;
+  const float4* entry;
+  const int* index;
+};
+
+struct TightQuery {
+  float xr[3];  // atom position relative to the grid origin
+  float inv_h;
+  int dims[3];
+};
+
+__device__ __forceinline__ TightQuery make_tight_query(const TableGeom& g, const float4 xi) {
+  TightQuery t;
+  t.xr[0] = (float)((double)xi.x - g.min[0]);
+  t.xr[1] = (float)((double)xi.y - g.min[1]);
+  t.xr[2] = (float)((double)xi.z - g.min[2]);
+  t.inv_h = (float)(1.0 / g.step[0]);
+  t.dims[0] = g.dims[0];
+  t.dims[1] = g.dims[1];
+  t.dims[2] = g.dims[2];
+  return t;
+}
+
+// cell of x_i + v, or -1 outside the grid (no shell reaches there)
+__device__ __forceinline__ long long tight_cell(const TightQuery& t, const float4 v) {
+  const int cx = (int)floorf((t.xr[0] + v.x) * t.inv_h);
+  const int cy = (int)floorf((t.xr[1] + v.y) * t.inv_h);
+  const int cz = (int)floorf((t.xr[2] + v.z) * t.inv_h);
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= t.dims[0] || cy >= t.dims[1] || cz >= t.dims[2]) return -1;
+  return ((long long)cx * t.dims[1] + cy) * t.dims[2] + cz;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kThreads) tight_integral_kernel(const float4* __restrict__ pos, int n,
+                                                                  TightTable tab, Quad quad, ModelConst m,
+                                                                  int chunk, int n_chunks,
+                                                                  float* __restrict__ Jpart,
+                                                                  unsigned long long* __restrict__ work) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (warp >= n * n_chunks) return;
+  const int i = warp % n, c = warp / n;
+  const TableGeom& geom = *tab.geom;
+  const float4 xi = pos[i];
+  const TightQuery tq = make_tight_query(geom, xi);
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  float J4 = 0.0f, J7 = 0.0f;
+  Work<COUNT> wk;
+  for (int q = q0 + lane; q < q1; q += kWarp) {
+    const float4 v = quad.qv[q];
+    const float2 w = quad.qw[q];
+    const long long cell = tight_cell(tq, v);
+    float V = 1.0f;
+    if (cell >= 0) {
+      const int cnt = tab.count[cell];
+      if (cnt < 0) {
+        V = 0.0f;
+      } else if (cnt > 0) {
+        V = gbsw_volume_inline(m, tab.entry + tab.start[cell], cnt, xi, v, wk);
+      }
+    }
+    J4 = fmaf(w.x, V, J4);
+    J7 = fmaf(w.y, V, J7);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    J4 += __shfl_xor_sync(0xffffffffu, J4, off);
+    J7 += __shfl_xor_sync(0xffffffffu, J7, off);
+  }
+  if (lane == 0) {
+    Jpart[(size_t)c * n + i] = J4;
+    Jpart[((size_t)n_chunks + c) * n + i] = J7;
+  }
+  if constexpr (COUNT) {
+    unsigned long long e = wk.e, sh = wk.s;
+    for (int off = 16; off > 0; off >>= 1) {
+      e += __shfl_xor_sync(0xffffffffu, e, off);
+      sh += __shfl_xor_sync(0xffffffffu, sh, off);
+    }
+    if (lane == 0) {
+      atomicAdd(&work[0], e);
+      atomicAdd(&work[1], sh);
+    }
+  }
+}
+
+template <bool ADJ>
+__global__ void __launch_bounds__(kThreads) tight_chain_kernel(const float4* __restrict__ pos, int n,
+                                                               TightTable tab, Quad quad, ModelConst m, int chunk,
+                                                               int n_chunks, const float2* __restrict__ dEdJ,
+                                                               unsigned long long* __restrict__ force, int stride,
+                                                               unsigned long long* __restrict__ dEdR) {
+  constexpr int kKeep = 4;  // in-shell entries remembered from the first pass
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (warp >= n * n_chunks) return;
+  const int i = warp % n, c = warp / n;
+  const TableGeom& geom = *tab.geom;
+  const float4 xi = pos[i];
+  const float2 de = dEdJ[i];
+  const TightQuery tq = make_tight_query(geom, xi);
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  const bool quirk = m.cutoff_chain_quirk && m.cutoff2 > 0.0f;
+  float fix = 0.f, fiy = 0.f, fiz = 0.f;
+  for (int q = q0 + lane; q < q1; q += kWarp) {
+    const float4 v = quad.qv[q];
+    const float2 w = quad.qw[q];
+    const float cq = fmaf(de.x, w.x, de.y * w.y);
+    const long long cell = tight_cell(tq, v);
+    if (cell < 0 || cq == 0.0f) continue;
+    const int cnt = tab.count[cell];
+    if (cnt <= 0) continue;  // buried (V = 0) or no shell (V = 1): no gradient
+    const int s = tab.start[cell];
+    // pass 1: volume, remembering the first in-shell entries
+    float V = 1.0f;
+    int keep[kKeep];
+    int nk = 0, nshell = 0;
+    for (int l = 0; l < cnt; ++l) {
+      const float4 a = __ldg(tab.entry + s + l);
+      const float dx = (a.x - xi.x) - v.x, dy = (a.y - xi.y) - v.y, dz = (a.z - xi.z) - v.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float lo = a.w - m.sw, hi = a.w + m.sw;
+      if (r2 <= lo * lo) {
+        V = 0.0f;
+        break;
+      }
+      if (r2 < hi * hi) {
+        const float dr = sqrtf(r2) - a.w;
+        V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+        if (nk < kKeep) keep[nk++] = l;
+        ++nshell;
+      }
+    }
+    if (V == 0.0f || nshell == 0) continue;
+    // pass 2: d V / d x_k = (V / u_k) u'_k d_k / r_k for each in-shell atom k
+    const int scan = nshell <= kKeep ? nk : cnt;
+    for (int t = 0; t < scan; ++t) {
+      const int l = nshell <= kKeep ? keep[t] : t;
+      const float4 a = __ldg(tab.entry + s + l);
+      const float dx = (a.x - xi.x) - v.x, dy = (a.y - xi.y) - v.y, dz = (a.z - xi.z) - v.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float lo = a.w - m.sw, hi = a.w + m.sw;
+      if (!(r2 > lo * lo && r2 < hi * hi)) continue;
+      const float r = sqrtf(r2);
+      const float dr = r - a.w;
+      const float u = fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+      const float du = fmaf(-3.0f * m.c3 * dr, dr, m.c1);
+      const float Vu = __fdividef(V, u);
+      const int k = __ldg(tab.index + s + l);
+      if (ADJ) red_add_fixed(&dEdR[k], cq * Vu * du * (-0.9520f));
+      if (k == i) continue;
+      const float gs = cq * Vu * du / r;
+      const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+      if (!quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= m.cutoff2) {
+        red_add_fixed(&force[k], -gs * dx);
+        red_add_fixed(&force[k + stride], -gs * dy);
+        red_add_fixed(&force[k + 2 * stride], -gs * dz);
+      }
+      fix = fmaf(gs, dx, fix);
+      fiy = fmaf(gs, dy, fiy);
+      fiz = fmaf(gs, dz, fiz);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    fix += __shfl_xor_sync(0xffffffffu, fix, off);
+    fiy += __shfl_xor_sync(0xffffffffu, fiy, off);
+    fiz += __shfl_xor_sync(0xffffffffu, fiz, off);
+  }
+  if (lane == 0) {
+    red_add_fixed(&force[i], fix);
+    red_add_fixed(&force[i + stride], fiy);
+    red_add_fixed(&force[i + 2 * stride], fiz);
+  }
+}
+
+int tight_blocks(const Context* ctx) {
+  const long long warps = (long long)ctx->n * ctx->n_chunks;
+  return (int)((warps * kWarp + kThreads - 1) / kThreads);
+}
+
 template <int MODEL>
 gbx_status launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, const Table& t,
                               const Quad& qd, bool count_work) {
@@ -446,6 +655,25 @@ gbx_status launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, 
 
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
   const ModelConst m = make_model_const(ctx);
+  if (ctx->use_tight) {
+    const TightTable tt{ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tentry, ctx->d_tindex};
+    const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
+    const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
+    if (count_work)
+      tight_integral_kernel<true><<<tight_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, tt, qd, m, chunk,
+                                                                                   ctx->n_chunks, ctx->d_J,
+                                                                                   ctx->d_work);
+    else
+      tight_integral_kernel<false><<<tight_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, tt, qd, m, chunk,
+                                                                                    ctx->n_chunks, ctx->d_J,
+                                                                                    nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      ctx->last_error = std::string("integral launch: ") + cudaGetErrorString(e);
+      return GBX_ERR_CUDA;
+    }
+    return GBX_OK;
+  }
   const Table t{ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries};
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   gbx_status s;
@@ -464,6 +692,23 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
 
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint) {
   const ModelConst m = make_model_const(ctx);
+  if (ctx->use_tight) {
+    const TightTable tt{ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tentry, ctx->d_tindex};
+    const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
+    const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
+    if (adjoint)
+      tight_chain_kernel<true><<<tight_blocks(ctx), kThreads, 0, ctx->stream>>>(
+          pos, ctx->n, tt, qd, m, chunk, ctx->n_chunks, ctx->d_dEdJ, force, stride, ctx->d_dEdR_fx);
+    else
+      tight_chain_kernel<false><<<tight_blocks(ctx), kThreads, 0, ctx->stream>>>(
+          pos, ctx->n, tt, qd, m, chunk, ctx->n_chunks, ctx->d_dEdJ, force, stride, ctx->d_dEdR_fx);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      ctx->last_error = std::string("chain launch: ") + cudaGetErrorString(e);
+      return GBX_ERR_CUDA;
+    }
+    return GBX_OK;
+  }
   const Table t{ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries};
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   gbx_status s;

@@ -58,6 +58,8 @@ class GBModel:
     cutoff_chain_quirk: bool = True   # CharmmReferenceGBSW.cpp:291-292
     skip_empty: bool = True
     standalone_sums: bool = True
+    reference_table: bool = False     # device: always integrate on the reference table
+    tight_h: float = 0.1              # device: cell edge of the exact GBSW table (nm)
 
     def replace(self, **kw) -> "GBModel":
         return dataclasses.replace(self, **kw)

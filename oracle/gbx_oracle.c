@@ -462,6 +462,7 @@ int orc_integrals(const orc_config* cfg, const orc_table* t, int n, const double
   double evals = 0, shell = 0, pts = 0, act = 0;
 #pragma omp parallel for schedule(static) num_threads(nthreads_of(cfg)) reduction(+ : evals, shell, pts, act)
   for (int i = 0; i < n; ++i) {
+    if (cfg->atom_stride > 1 && i % cfg->atom_stride) continue;
     for (int q = 0; q < cfg->nq; ++q) {
       double p[3];
       for (int k = 0; k < 3; ++k) p[k] = pos[3 * i + k] + cfg->qoff[3 * q + k];
@@ -513,6 +514,7 @@ static int chain_walk(const orc_config* cfg, const orc_table* t, int n, const do
     double* DR = rbuf ? rbuf + (size_t)tid * n : NULL;
 #pragma omp for schedule(static)
     for (int i = 0; i < n; ++i) {
+      if (cfg->atom_stride > 1 && i % cfg->atom_stride) continue;
       for (int q = 0; q < cfg->nq; ++q) {
         double c = 0.0;
         for (int k = 0; k < cfg->n_int; ++k) c += dEdI[k * n + i] * order_weight(cfg, k, q);
@@ -601,6 +603,7 @@ int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const dou
     double* DQ = qbuf + (size_t)tid * n;
 #pragma omp for schedule(dynamic, 16)
     for (int i = 0; i < n; ++i) {
+      if (cfg->atom_stride > 1 && i % cfg->atom_stride) continue;
       for (int j = i; j < n; ++j) {
         double d[3];
         double r = delta_r(pos + 3 * i, pos + 3 * j, d);

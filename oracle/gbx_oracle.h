@@ -59,6 +59,9 @@ typedef struct {
   int standalone_sums; /* accumulate as CharmmReferenceGBSW.cpp:586-589 ((w*f)/(r*r), (w*f)/r^5 by
                           repeated products) instead of GBSWIntegral.cpp:144-145 (w/pow(r,n-2))*f */
   int nthreads;       /* OpenMP threads, <= 0 -> all */
+  int atom_stride;    /* timing samples: only atoms i % stride == 0 run their
+                         points, chain rule and pair rows (<= 1: all atoms).
+                         The results are then partial; the cost scales by stride. */
 } orc_config;
 
 typedef struct {

@@ -48,6 +48,7 @@ class OrcConfig(ctypes.Structure):
         ("skip_empty", ctypes.c_int),
         ("standalone_sums", ctypes.c_int),
         ("nthreads", ctypes.c_int),
+        ("atom_stride", ctypes.c_int),
     ]
 
 
@@ -112,7 +113,7 @@ def _ptr(a):
 class Oracle:
     """FP64 evaluation of one model on host arrays."""
 
-    def __init__(self, model, quadrature=None, nthreads: int = 0):
+    def __init__(self, model, quadrature=None, nthreads: int = 0, atom_stride: int = 1):
         from openmmcustomgbintegralforce_gb300.quadrature import tensor_quadrature
 
         self.model = model
@@ -149,6 +150,7 @@ class Oracle:
         c.skip_empty = 1 if model.skip_empty else 0
         c.standalone_sums = 1 if model.standalone_sums else 0
         c.nthreads = nthreads
+        c.atom_stride = atom_stride
         self.cfg = c
 
     def table(self, pos, radius):

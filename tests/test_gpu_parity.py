@@ -123,6 +123,31 @@ def test_integral_classes_vs_reference_golden(tag):
     assert np.abs(I - ref).max() < 1e-5 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("cutoff", [0.0, 1.0])
+def test_exact_table_matches_reference_table(glob1000, cutoff):
+    """The exact GBSW table yields the same volumes as the reference's
+    standalone table: identical to FP32 rounding of the product order."""
+    g = glob1000
+    m = GBModel.charmm_gbsw(n_radial=24, lebedev=50, cutoff=cutoff)
+    a = Context(m, g.n)
+    b = Context(m.replace(reference_table=True), g.n)
+    for c in (a, b):
+        c.set_particle_parameters(g.charge, g.radius)
+    Ea, Fa = a.execute_host(g.positions)
+    Eb, Fb = b.execute_host(g.positions)
+    assert abs(Ea / Eb - 1) < 1e-6
+    assert rel_rms(Fa, Fb) < 1e-5
+    assert np.abs(a.born_radii() / b.born_radii() - 1).max() < 1e-5
+    # exact-table work is a fraction of the reference's list work
+    a.execute_host(g.positions, count_work=True)
+    b.execute_host(g.positions, count_work=True)
+    assert a.work()["volume_evals"] < 0.5 * b.work()["volume_evals"]
+    # the reference table is still available, bit-exact, after an exact-table run
+    t = a.lookup_table()
+    ref = O.Oracle(m).table(g.positions, g.radius)
+    assert np.array_equal(t["counts"], ref["counts"]) and np.array_equal(t["atoms"], ref["atoms"])
+
+
 def test_bitwise_deterministic(glob1000):
     g = glob1000
     ctx = Context(GBModel.charmm_gbsw(), g.n)
