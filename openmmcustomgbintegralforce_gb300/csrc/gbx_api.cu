@@ -133,17 +133,10 @@ gbx_status upload_quadrature(Context* ctx) {
   return GBX_OK;
 }
 
+// The volume kernels run one warp per (atom, chunk of quadrature points)
+// with lanes over points: enough warps for ~48 per SM on 152 SMs, and
+// >= 64 points (2 per lane) per chunk.
 int choose_chunks(int n, int Q) {
-  // >= ~48 resident warps per SM on 152 SMs; each chunk keeps >= 16 points
-  const int groups = (n + gbx::kWarp - 1) / gbx::kWarp;
-  int c = (152 * 48 + groups - 1) / groups;
-  c = std::max(1, std::min(c, std::max(1, Q / 16)));
-  return c;
-}
-
-// Exact-table kernels run one warp per (atom, chunk) with lanes over points:
-// enough warps for ~48 per SM, and >= 64 points (2 per lane) per chunk.
-int choose_tight_chunks(int n, int Q) {
   int c = (152 * 48 + n - 1) / n;
   c = std::max(1, std::min(c, std::max(1, Q / 64)));
   return c;
@@ -152,7 +145,7 @@ int choose_tight_chunks(int n, int Q) {
 gbx_status alloc_atom_buffers(Context* ctx) {
   const int n = ctx->n;
   const int Q = ctx->cfg.n_radial * ctx->cfg.lebedev_order;
-  ctx->n_chunks = ctx->use_tight ? choose_tight_chunks(n, Q) : choose_chunks(n, Q);
+  ctx->n_chunks = choose_chunks(n, Q);
   GBX_TRY(dalloc(ctx, &ctx->d_radius, n));
   GBX_TRY(dalloc(ctx, &ctx->d_charge, n));
   GBX_TRY(dalloc(ctx, &ctx->d_par, n));
@@ -199,6 +192,8 @@ gbx_status grow_table(Context* ctx, long long cells, long long entries) {
       return GBX_ERR_TABLE_TOO_LARGE;
     }
     GBX_TRY(dalloc(ctx, &ctx->d_entries, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_entry4, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_entry_par, cap));
     ctx->entry_cap = cap;
   }
   return GBX_OK;
@@ -466,7 +461,9 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
   ctx->tight_h = cfg->tight_grid_length > 0 ? cfg->tight_grid_length : 0.1;
   s = upload_quadrature(ctx);
   if (s == GBX_OK) s = alloc_atom_buffers(ctx);
-  if (s == GBX_OK && cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) s = GBX_ERR_CUDA;
+  if (s == GBX_OK && cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    s = GBX_ERR_CUDA;
+  ctx->stream = ctx->own_stream;
   if (s != GBX_OK) {
     gbx_destroy(reinterpret_cast<gbx_context*>(ctx));
     return s;
@@ -492,14 +489,14 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_integrals, ctx->d_dEdB_fx, ctx->d_dEdJ, ctx->d_energy_part, ctx->d_force_fx,
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
-                  ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex};
+                  ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)
     if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
   if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
   if (ctx->h_force_fx) cudaFreeHost(ctx->h_force_fx);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return GBX_OK;
 }
@@ -560,7 +557,7 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
   if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
   if ((flags & GBX_EXEC_FORCES) && (!force_fixed || force_stride < ctx->n)) return GBX_ERR_INVALID_ARGUMENT;
   if ((flags & GBX_EXEC_ENERGY) && !energy) return GBX_ERR_INVALID_ARGUMENT;
-  ctx->stream = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   unsigned long long* f = force_fixed;
   int stride = force_stride;
   if (!(flags & GBX_EXEC_FORCES)) {
@@ -580,6 +577,7 @@ namespace {
 
 gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work) {
   const int n = ctx->n;
+  ctx->stream = ctx->own_stream;
   for (int i = 0; i < n; ++i)
     ctx->h_pos[i] = make_float4((float)positions[3 * i], (float)positions[3 * i + 1], (float)positions[3 * i + 2], 0.f);
   GBX_CUDA(cudaMemcpyAsync(ctx->d_pos, ctx->h_pos, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -682,7 +680,7 @@ gbx_status gbx_get_dEdB(gbx_context* handle, double* dEdB) {
 gbx_status gbx_build_lookup_table(gbx_context* handle, const void* posq, void* stream) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
-  ctx->stream = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   GBX_TRY(gbx::launch_stage_positions(ctx, reinterpret_cast<const float4*>(posq)));
   return build_table_checked(ctx, true);
 }

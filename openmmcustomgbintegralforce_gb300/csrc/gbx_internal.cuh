@@ -84,7 +84,9 @@ struct Context {
   int* d_cell_count = nullptr;   // uncapped count -> final (capped) count
   int* d_cell_start = nullptr;   // [cell_cap+1]
   int* d_cell_cursor = nullptr;
-  int* d_entries = nullptr;      // [entry_cap]
+  int* d_entries = nullptr;      // [entry_cap] atom indices, ascending per cell
+  float4* d_entry4 = nullptr;    // [entry_cap] inline copies (x, y, z, main parameter)
+  float2* d_entry_par = nullptr; // [entry_cap] inline secondary parameters
   int* d_block_sums = nullptr;
   double* d_reduce = nullptr;    // geometry reduction scratch
   bool table_valid = false;
@@ -133,7 +135,8 @@ struct Context {
   // host staging
   float4* h_pos = nullptr;                 // pinned
   unsigned long long* h_force_fx = nullptr; // pinned
-  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;  // created and destroyed by the context
+  cudaStream_t stream = nullptr;      // stream of the current call (the caller's or own_stream)
 };
 
 // --------------------------------------------------------------------------

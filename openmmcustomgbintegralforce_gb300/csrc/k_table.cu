@@ -342,6 +342,20 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) sort_cells_kernel(int* __r
   }
 }
 
+// Inline copies of each listed atom's position and parameters, so the
+// volume kernels stream a cell's list without a dependent gather.
+__global__ void denormalize_kernel(const int* __restrict__ entries, const TableGeom* __restrict__ gp,
+                                   const float4* __restrict__ pos, const float2* __restrict__ par,
+                                   float4* __restrict__ entry4, float2* __restrict__ entry_par, long long entry_cap) {
+  const long long total = gp->total <= entry_cap ? gp->total : 0;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int j = entries[e];
+    entry4[e] = pos[j];
+    entry_par[e] = par[j];
+  }
+}
+
 int grid_for(long long work, int per_block) {
   long long b = (work + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -406,6 +420,8 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
   sort_cells_kernel<<<grid_for(cells, kSortWarps), kSortWarps * kWarp, 0, st>>>(
       ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries, ctx->d_geom, c.table_cap, cells, ctx->entry_cap,
       ctx->d_status);
+  denormalize_kernel<<<grid_for(ctx->entry_cap, 256), 256, 0, st>>>(ctx->d_entries, ctx->d_geom, pos, ctx->d_par,
+                                                                    ctx->d_entry4, ctx->d_entry_par, ctx->entry_cap);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("table build launch: ") + cudaGetErrorString(e);
