@@ -44,7 +44,8 @@ typedef enum {
   GBX_ERR_NONFINITE = 5,      /* a Born radius or the energy came out NaN/Inf */
   GBX_ERR_TABLE_TOO_LARGE = 6, /* lookup grid would exceed its limits (reference: length > 1000 nm) */
   GBX_ERR_NOT_READY = 7,      /* result queried before an execute */
-  GBX_ERR_TIMEOUT = 8         /* a device-side wait gave up (batched persistent kernel) */
+  GBX_ERR_TIMEOUT = 8,        /* a device-side wait gave up (batched persistent kernel) */
+  GBX_ERR_EXCEEDS_STATIC_SCRATCH = 9 /* gbx_pair_noalloc: more atoms than its static scratch holds */
 } gbx_status;
 
 /* Volume models: CharmmGBMVForce::GBIntegralType (CharmmGBMVForce.h:99-104). */
@@ -178,6 +179,27 @@ GBX_API gbx_status gbx_get_work(gbx_context* ctx, double* volume_evals, double* 
  * reference. */
 GBX_API gbx_status gbx_set_timing(gbx_context* ctx, int enable);
 GBX_API gbx_status gbx_get_stage_times(gbx_context* ctx, double* ms, int max_stages, int* num_stages);
+
+/* Allocation-free GB pair term, for callers that cannot let a library
+ * allocate device memory (an engine that owns all device memory through its
+ * own pool, or a step loop that must not block or fail in cudaMalloc).  No
+ * counterpart in the reference.  It computes the same pair energy (including
+ * the 1/2 pref q^2/B self terms), pair forces and dE/dB as gbx_execute's pair
+ * stage, from caller-supplied device arrays: posq float4[n] (x, y, z, -),
+ * charge float[n], born float[n] (Born radii, nm).  force_fixed (fixed point,
+ * stride as in gbx_execute) and *energy are ADDED to; dEdB double[n] is
+ * written when not NULL.  cutoff <= 0: all pairs.
+ *
+ * Nothing is allocated: the scratch is one static device array of about
+ * 1 MiB that every GPU loading the library holds until exit, which limits
+ * num_atoms to 65536 (larger sizes return GBX_ERR_EXCEEDS_STATIC_SCRATCH).
+ * All calls on a device share that array, so calls whose kernels overlap on
+ * the GPU (different streams, host threads) race: serialise them.  The first
+ * call on each device looks the array's device address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture. */
+GBX_API gbx_status gbx_pair_noalloc(const void* posq, const float* charge, const float* born, int num_atoms,
+                                    double prefactor, double cutoff, unsigned long long* force_fixed,
+                                    int force_stride, double* energy, double* dEdB, void* stream);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,7 @@ GBX_OK = 0
 STATUS_NAMES = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported",
     5: "non-finite result", 6: "lookup table too large", 7: "no result yet", 8: "device wait timed out",
+    9: "more atoms than the static scratch of gbx_pair_noalloc holds",
 }
 EXEC_FORCES, EXEC_ENERGY, EXEC_CHECK, EXEC_COUNT_WORK = 1, 2, 4, 8
 
@@ -25,7 +26,7 @@ EXPORTED = (
     "gbx_status_string", "gbx_version", "gbx_config_preset", "gbx_create", "gbx_destroy", "gbx_last_error",
     "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
-    "gbx_adjoint_host", "gbx_get_work", "gbx_set_timing", "gbx_get_stage_times",
+    "gbx_adjoint_host", "gbx_get_work", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
@@ -130,6 +131,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_get_work.argtypes = [vp, vp, vp, vp]
     L.gbx_set_timing.argtypes = [vp, ci]
     L.gbx_get_stage_times.argtypes = [vp, vp, ci, vp]
+    L.gbx_pair_noalloc.argtypes = [vp, vp, vp, ci, cd, cd, vp, ci, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("gbx_status_string", "gbx_version"):
             getattr(L, name).restype = ci

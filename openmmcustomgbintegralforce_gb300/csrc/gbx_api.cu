@@ -376,6 +376,7 @@ const char* gbx_status_string(gbx_status s) {
     case GBX_ERR_TABLE_TOO_LARGE: return "lookup table too large";
     case GBX_ERR_NOT_READY: return "no result yet";
     case GBX_ERR_TIMEOUT: return "device wait timed out";
+    case GBX_ERR_EXCEEDS_STATIC_SCRATCH: return "more atoms than the static scratch of gbx_pair_noalloc holds (65536)";
   }
   return "unknown status";
 }

@@ -143,6 +143,31 @@ int pair_segments(int n) {
   return s;
 }
 
+// The same kernel on caller-supplied buffers (used by the allocation-free
+// entry point): energy_part needs pair_energy_parts(n, pair_segments(n))
+// doubles and dEdB must be zero on entry.
+cudaError_t launch_pair_raw(const float4* pos, const float* charge, const float2* born, int n, float pref,
+                            float cutoff2, unsigned long long* force, int stride, unsigned long long* dEdB,
+                            double* energy_part, cudaStream_t stream) {
+  PairArgs a;
+  a.pos = pos;
+  a.charge = charge;
+  a.born = born;
+  a.n = n;
+  a.segments = pair_segments(n);
+  a.pref = pref;
+  a.cutoff2 = cutoff2;
+  a.force = force;
+  a.stride = stride;
+  a.dEdB = dEdB;
+  a.energy_part = energy_part;
+  a.dEdq = nullptr;
+  dim3 grid((n + kPairThreads - 1) / kPairThreads, a.segments);
+  if (cutoff2 > 0) pair_kernel<true, false><<<grid, kPairThreads, 0, stream>>>(a);
+  else pair_kernel<false, false><<<grid, kPairThreads, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint) {
   PairArgs a;
   a.pos = pos;
