@@ -182,6 +182,7 @@ gbx_status grow_table(Context* ctx, long long cells, long long entries) {
     GBX_TRY(dalloc(ctx, &ctx->d_cell_count, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_cell_start, cap + 1));
     GBX_TRY(dalloc(ctx, &ctx->d_cell_cursor, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_cell2, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_block_sums, cap / (1024 * 8) + 2));
     ctx->cell_cap = cap;
   }
@@ -247,6 +248,7 @@ gbx_status grow_tight(Context* ctx, long long cells, long long entries) {
     GBX_TRY(dalloc(ctx, &ctx->d_tstart, cap + 1));
     GBX_TRY(dalloc(ctx, &ctx->d_tcursor, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_tburied, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tcell, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_tblock_sums, cap / (1024 * 8) + 2));
     ctx->tcell_cap = cap;
   }
@@ -490,7 +492,8 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_integrals, ctx->d_dEdB_fx, ctx->d_dEdJ, ctx->d_energy_part, ctx->d_force_fx,
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
-                  ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par};
+                  ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
+                  ctx->d_cell2, ctx->d_tcell};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)

@@ -84,6 +84,7 @@ struct Context {
   int* d_cell_count = nullptr;   // uncapped count -> final (capped) count
   int* d_cell_start = nullptr;   // [cell_cap+1]
   int* d_cell_cursor = nullptr;
+  int2* d_cell2 = nullptr;       // [cell_cap] (capped count, start) for the volume kernels
   int* d_entries = nullptr;      // [entry_cap] atom indices, ascending per cell
   float4* d_entry4 = nullptr;    // [entry_cap] inline copies (x, y, z, main parameter)
   float2* d_entry_par = nullptr; // [entry_cap] inline secondary parameters
@@ -101,6 +102,7 @@ struct Context {
   int* d_tstart = nullptr;
   int* d_tcursor = nullptr;
   int* d_tburied = nullptr;
+  int2* d_tcell = nullptr;       // (count or -1 if buried, start)
   int* d_tblock_sums = nullptr;
   float4* d_tentry = nullptr;    // (x, y, z, R') per list entry
   int* d_tindex = nullptr;       // atom index per list entry
@@ -143,9 +145,13 @@ struct Context {
 // Device helpers
 // --------------------------------------------------------------------------
 
+// round(v * 2^32) as a 64-bit integer.  Scaling by a power of two is exact
+// in FP32, so converting the float directly gives the same integer as the
+// FP64 route without touching the (slow) FP64 pipe.
+__device__ __forceinline__ long long float_to_fixed(float v) { return __float2ll_rn(v * 4294967296.0f); }
+
 __device__ __forceinline__ void red_add_fixed(unsigned long long* addr, float v) {
-  long long q = __double2ll_rn((double)v * kFixedScale);
-  atomicAdd(addr, (unsigned long long)q);
+  atomicAdd(addr, (unsigned long long)float_to_fixed(v));
 }
 
 __device__ __forceinline__ void red_add_fixed_d(unsigned long long* addr, double v) {

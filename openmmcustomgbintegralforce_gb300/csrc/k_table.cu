@@ -294,6 +294,7 @@ constexpr int kSortBuf = 512;  // per-warp shared staging; longer lists rank fro
 __global__ void __launch_bounds__(kSortWarps * kWarp) sort_cells_kernel(int* __restrict__ count,
                                                                         const int* __restrict__ start,
                                                                         int* __restrict__ entries,
+                                                                        int2* __restrict__ cell,
                                                                         const TableGeom* __restrict__ gp, int cap,
                                                                         long long cell_cap, long long entry_cap,
                                                                         unsigned* __restrict__ status) {
@@ -304,8 +305,9 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) sort_cells_kernel(int* __r
   int* buf = s_buf[wib];
   for (long long c = (long long)blockIdx.x * kSortWarps + wib; c < ncell; c += (long long)gridDim.x * kSortWarps) {
     const int cnt = count[c];
-    if (cnt == 0) continue;
     const int s = start[c];
+    if (lane == 0) cell[c] = make_int2(cap > 0 && cnt > cap ? cap : cnt, s);
+    if (cnt == 0) continue;
     if (cnt > kSortBuf) {
       if (cnt > kMaxSortSegment && lane == 0) atomicOr(status, kStatusSegmentTooLong);
       if (cnt > kMaxSortSegment) continue;
@@ -418,7 +420,7 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
     }
   }
   sort_cells_kernel<<<grid_for(cells, kSortWarps), kSortWarps * kWarp, 0, st>>>(
-      ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries, ctx->d_geom, c.table_cap, cells, ctx->entry_cap,
+      ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries, ctx->d_cell2, ctx->d_geom, c.table_cap, cells, ctx->entry_cap,
       ctx->d_status);
   denormalize_kernel<<<grid_for(ctx->entry_cap, 256), 256, 0, st>>>(ctx->d_entries, ctx->d_geom, pos, ctx->d_par,
                                                                     ctx->d_entry4, ctx->d_entry_par, ctx->entry_cap);

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
                                                                         const int* __restrict__ buried,
                                                                         float4* __restrict__ entry,
                                                                         int* __restrict__ index,
+                                                                        int2* __restrict__ cell,
                                                                         const TableGeom* __restrict__ gp, float w,
                                                                         long long cell_cap, long long entry_cap,
                                                                         unsigned* __restrict__ status) {
@@ -194,16 +195,23 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
   const long long sx = (long long)g.dims[1] * g.dims[2];
   for (long long c = (long long)blockIdx.x * kSortWarps + wib; c < ncell; c += (long long)gridDim.x * kSortWarps) {
     const int cnt = count[c];
-    if (cnt == 0) continue;
-    if (buried[c]) {
-      if (lane == 0) count[c] = -1;
+    const int s = start[c];
+    if (cnt == 0) {
+      if (lane == 0) cell[c] = make_int2(0, s);
       continue;
     }
+    if (buried[c]) {
+      if (lane == 0) {
+        count[c] = -1;
+        cell[c] = make_int2(-1, s);
+      }
+      continue;
+    }
+    if (lane == 0) cell[c] = make_int2(cnt, s);
     if (cnt > kSortBuf) {
       if (lane == 0) atomicOr(status, kStatusSegmentTooLong);
       continue;
     }
-    const int s = start[c];
     const int cx = (int)(c / sx), cy = (int)((c / g.dims[2]) % g.dims[1]), cz = (int)(c % g.dims[2]);
     const double ctr[3] = {g.min[0] + (cx + 0.5) * g.step[0], g.min[1] + (cy + 0.5) * g.step[1],
                            g.min[2] + (cz + 0.5) * g.step[2]};
@@ -256,7 +264,7 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
     long long sb = (cells + kSortWarps - 1) / kSortWarps;
     if (sb > 1048576) sb = 1048576;
     tight_sort_kernel<<<(int)sb, kSortWarps * kWarp, 0, st>>>(ctx->d_tcount, ctx->d_tstart, ctx->d_tburied,
-                                                               ctx->d_tentry, ctx->d_tindex, ctx->d_tgeom,
+                                                               ctx->d_tentry, ctx->d_tindex, ctx->d_tcell, ctx->d_tgeom,
                                                                (float)ctx->cfg.switch_width, cells, ctx->tentry_cap,
                                                                ctx->d_status);
   }

@@ -41,8 +41,7 @@ struct Quad {
 // Inline list entries of either table.
 struct Entries {
   const TableGeom* geom;
-  const int* count;    // exact table: -1 marks a buried cell
-  const int* start;
+  const int2* cell;    // (count, start); exact table: count -1 marks a buried cell
   const float4* e;     // (x, y, z, main model parameter)
   const float2* par;   // secondary model parameters (reference table only)
   const int* index;    // atom index of each entry
@@ -172,7 +171,7 @@ __device__ __forceinline__ float gbsw_volume(const ModelConst& m, const float4* 
     if (r2 <= lo * lo) return 0.0f;
     if (r2 < hi * hi) {
       wk.shell();
-      const float dr = sqrtf(r2) - a.w;
+      const float dr = r2 * rsqrtf(r2) - a.w;
       V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
     }
   }
@@ -237,9 +236,10 @@ __device__ __forceinline__ float solvent_fraction(const ModelConst& m, const Ent
                                                   const float4 xi, const float4 v, W& wk) {
   int cnt = 0, s = 0;
   if (cell >= 0) {
-    cnt = t.count[cell];
+    const int2 cs = __ldg(t.cell + cell);
+    cnt = cs.x;
     if (cnt < 0) return 0.0f;  // buried cell (exact table)
-    s = t.start[cell];
+    s = cs.y;
   }
   if (MODEL == GBX_MODEL_GBSW) return cnt > 0 ? gbsw_volume(m, t.e + s, cnt, xi, v, wk) : 1.0f;
   float p;
@@ -311,79 +311,27 @@ struct ChainOut {
   float cutoff2;
 };
 
-// Per-CTA force accumulator.  The warps of one CTA work on neighbouring
-// atoms, whose quadrature points are shaped by largely the same atoms k, so
-// the contributions to F_k are summed in shared memory (open addressing on
-// the atom index, 64-bit fixed point) and flushed to the global buffer once
-// per distinct k.  Each contribution is rounded to fixed point exactly as a
-// direct global add would be, so the result is bit-identical to one.
-constexpr int kChainThreads = 256;
-constexpr int kHashBits = 11;
-constexpr int kHashSlots = 1 << kHashBits;
-constexpr int kHashProbes = 32;
-constexpr size_t kHashBytes = kHashSlots * (sizeof(int) + 3 * sizeof(unsigned long long));
-
-struct ForceHash {
-  int* key;                     // atom index, -1 empty
-  unsigned long long* val;      // [3][kHashSlots]
-  __device__ __forceinline__ void init(char* smem) {
-    val = reinterpret_cast<unsigned long long*>(smem);
-    key = reinterpret_cast<int*>(smem + 3 * kHashSlots * sizeof(unsigned long long));
-    for (int s = threadIdx.x; s < kHashSlots; s += blockDim.x) {
-      key[s] = -1;
-      val[s] = val[kHashSlots + s] = val[2 * kHashSlots + s] = 0ull;
-    }
-  }
-  __device__ __forceinline__ void add(const ChainOut& o, int k, float gx, float gy, float gz) {
-    const long long fx = __double2ll_rn(-(double)gx * kFixedScale);
-    const long long fy = __double2ll_rn(-(double)gy * kFixedScale);
-    const long long fz = __double2ll_rn(-(double)gz * kFixedScale);
-    unsigned h = ((unsigned)k * 0x9E3779B1u) >> (32 - kHashBits);
-    for (int p = 0; p < kHashProbes; ++p) {
-      const int old = atomicCAS(&key[h], -1, k);
-      if (old == -1 || old == k) {
-        atomicAdd(&val[h], (unsigned long long)fx);
-        atomicAdd(&val[kHashSlots + h], (unsigned long long)fy);
-        atomicAdd(&val[2 * kHashSlots + h], (unsigned long long)fz);
-        return;
-      }
-      h = (h + 1) & (kHashSlots - 1);
-    }
-    atomicAdd(&o.force[k], (unsigned long long)fx);
-    atomicAdd(&o.force[k + o.stride], (unsigned long long)fy);
-    atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
-  }
-  __device__ __forceinline__ void flush(const ChainOut& o) {
-    for (int s = threadIdx.x; s < kHashSlots; s += blockDim.x) {
-      const int k = key[s];
-      if (k < 0) continue;
-      atomicAdd(&o.force[k], val[s]);
-      atomicAdd(&o.force[k + o.stride], val[kHashSlots + s]);
-      atomicAdd(&o.force[k + 2 * o.stride], val[2 * kHashSlots + s]);
-    }
-  }
-};
+__device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, float gy, float gz) {
+  red_add_fixed(&o.force[k], -gx);
+  red_add_fixed(&o.force[k + o.stride], -gy);
+  red_add_fixed(&o.force[k + 2 * o.stride], -gz);
+}
 
 template <int MODEL, class Q, bool ADJ>
-__global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
-                                                              Quad quad, ModelConst m, int chunk, int n_chunks,
-                                                              const float2* __restrict__ dEdJ, ChainOut out) {
+__global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
+                                                         Quad quad, ModelConst m, int chunk, int n_chunks,
+                                                         const float2* __restrict__ dEdJ, ChainOut out) {
   constexpr int kKeep = 4;  // GBSW: in-shell entries remembered from the volume pass
-  extern __shared__ __align__(16) char smem[];
-  ForceHash hash;
-  hash.init(smem);
-  __syncthreads();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
-  const bool warp_active = warp < n * n_chunks;
-  const int i = warp_active ? warp % n : 0, c = warp_active ? warp / n : 0;
+  if (warp >= n * n_chunks) return;
+  const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
-  const float2 de = warp_active ? dEdJ[i] : make_float2(0.f, 0.f);
+  const float2 de = dEdJ[i];
   Q query;
   query.init(*tab.geom, xi, quad.qoff);
-  const int q0 = c * chunk, q1 = warp_active ? min(m.nq, q0 + chunk) : q0;
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float fix = 0.f, fiy = 0.f, fiz = 0.f;
-  auto push_force = [&](const ChainOut& o, int k, float gx, float gy, float gz) { hash.add(o, k, gx, gy, gz); };
   for (int q = q0 + lane; q < q1; q += kWarp) {
     const float4 v = quad.qv[q];
     const float2 w = quad.qw[q];
@@ -391,9 +339,10 @@ __global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __re
     if (cq == 0.0f) continue;
     const long long cell = query.cell(xi, v, q);
     if (cell < 0) continue;
-    const int cnt = tab.count[cell];
+    const int2 cs = __ldg(tab.cell + cell);
+    const int cnt = cs.x;
     if (cnt <= 0) continue;  // buried or empty: no atom shapes the point
-    const int s = tab.start[cell];
+    const int s = cs.y;
     const float4* E = tab.e + s;
     if (MODEL == GBX_MODEL_GBSW) {
       float V = 1.0f;
@@ -409,7 +358,7 @@ __global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __re
           break;
         }
         if (r2 < hi * hi) {
-          const float dr = sqrtf(r2) - a.w;
+          const float dr = r2 * rsqrtf(r2) - a.w;
           V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
           if (nk < kKeep) keep[nk++] = l;
           ++nshell;
@@ -424,8 +373,8 @@ __global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __re
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         const float lo = a.w - m.sw, hi = a.w + m.sw;
         if (!(r2 > lo * lo && r2 < hi * hi)) continue;
-        const float r = sqrtf(r2);
-        const float dr = r - a.w;
+        const float inv_r = rsqrtf(r2);
+        const float dr = r2 * inv_r - a.w;
         const float u = fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
         const float du = fmaf(-3.0f * m.c3 * dr, dr, m.c1);
         const float Vu = __fdividef(V, u);
@@ -433,7 +382,7 @@ __global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __re
         // dV/dR_k = -(V/u) u' dR'/dR with R' = (R + 0.03) 0.952
         if (ADJ) red_add_fixed(&out.dEdR[k], cq * Vu * du * (-0.9520f));
         if (k == i) continue;
-        const float gs = cq * Vu * du / r;
+        const float gs = cq * Vu * du * inv_r;
         const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
         if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2)
           push_force(out, k, gs * d.x, gs * d.y, gs * d.z);
@@ -509,19 +458,17 @@ __global__ void __launch_bounds__(kChainThreads) chain_kernel(const float4* __re
     fiy += __shfl_xor_sync(0xffffffffu, fiy, off);
     fiz += __shfl_xor_sync(0xffffffffu, fiz, off);
   }
-  if (lane == 0 && warp_active) {
+  if (lane == 0) {
     red_add_fixed(&out.force[i], fix);
     red_add_fixed(&out.force[i + out.stride], fiy);
     red_add_fixed(&out.force[i + 2 * out.stride], fiz);
   }
-  __syncthreads();
-  hash.flush(out);
 }
 
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
-    return Entries{ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tentry, nullptr, ctx->d_tindex};
-  return Entries{ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries};
+    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex};
+  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries};
 }
 
 int volume_blocks(const Context* ctx) {
@@ -548,12 +495,8 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
   ChainOut o{force, stride, ctx->d_dEdR_fx, m.cutoff_chain_quirk && m.cutoff2 > 0.0f, m.cutoff2};
-  // per device; a cheap host-side call
-  cudaFuncSetAttribute(chain_kernel<MODEL, Q, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHashBytes);
-  const long long warps = (long long)ctx->n * ctx->n_chunks;
-  const int blocks = (int)((warps * kWarp + kChainThreads - 1) / kChainThreads);
-  chain_kernel<MODEL, Q, ADJ><<<blocks, kChainThreads, kHashBytes, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
-                                                                                  ctx->n_chunks, ctx->d_dEdJ, o);
+  chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
+                                                                                ctx->n_chunks, ctx->d_dEdJ, o);
 }
 
 gbx_status launch_status(Context* ctx, const char* what) {
