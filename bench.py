@@ -49,6 +49,12 @@ FLOPS_GBSW_EVAL = 10.0
 FLOPS_GBSW_SHELL = 8.0
 # per quadrature point: point = x + v 3, cell index 6, two weighted sums 4
 FLOPS_POINT = 13.0
+# GBSW chain rule per listed atom (reduceIntegralForce.cu:45-65 with
+# computeGBSWForce.cu:10-25): delta 3, r^2 5, shell bounds 2 -> 10 flops +
+# 1 sqrt; inside the shell u 7, du/dr 2, dI/dr 3, factor 1, times delta 3,
+# force on i and on the listed atom 6 -> +22 flops; per point as above.
+FLOPS_CHAIN_EVAL = 10.0
+FLOPS_CHAIN_SHELL = 22.0
 # unique pair (CharmmReferenceGBSW.cpp:248-282): delta+r^2 8, D 3, exp arg 1,
 # f^2 2, 1/f^3 2, energy 3, dG/dr 4 + force 6, dG/dB 2x5 -> 39 flops + exp, rsqrt
 FLOPS_PAIR = 39.0
@@ -317,6 +323,10 @@ def main():
     pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
     cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
             "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12}
+    if model.model == 0:
+        chain_flops = FLOPS_CHAIN_EVAL * work["chain_list_evals"] + FLOPS_CHAIN_SHELL * work["chain_derivative_evals"] + \
+            FLOPS_POINT * points
+        cand["chain_rule"] = chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12
     dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
     achieved = cand.get(dominant)
     roofline = {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -326,6 +336,8 @@ def main():
                 "per_stage_tflops": cand, "stage_ms": stage_ms,
                 "work": {"volume_evals": work["volume_evals"], "shell_evals": work["shell_evals"],
                          "points": points, "pairs": n * (n - 1) / 2.0,
+                         "chain_list_evals": work["chain_list_evals"],
+                         "chain_derivative_evals": work["chain_derivative_evals"],
                          "executed_volume_evals": executed["volume_evals"],
                          "executed_shell_evals": executed["shell_evals"],
                          "note": "volume_evals/shell_evals: the reference algorithm's list work on this input "

@@ -172,6 +172,29 @@ GBX_API gbx_status gbx_adjoint_host(gbx_context* ctx, const double* positions, d
  * reference. */
 GBX_API gbx_status gbx_get_work(gbx_context* ctx, double* volume_evals, double* shell_evals, double* pairs);
 
+/* Chain-rule work of the same run: every listed atom of every quadrature
+ * point (the reference chain kernel walks whole lists,
+ * platforms/cuda/src/kernels/reduceIntegralForce.cu:45-65), and of those the
+ * ones inside a GBSW switching shell (all of them for GBMV).  Diagnostics for
+ * roofline accounting; no counterpart in the reference. */
+GBX_API gbx_status gbx_get_chain_work(gbx_context* ctx, double* list_evals, double* derivative_evals);
+
+/* GBSW forces: the integral pass writes one 16-byte record per (point,
+ * in-shell atom) for the chain rule, so that the chain rule does not re-walk
+ * every point's cell list.  Each warp (atom x quadrature chunk) owns per_warp
+ * records.  per_warp < 0: automatic (the default; first half a warp's points,
+ * then 1.125x the largest need seen), 0: no records (the chain rule walks the
+ * lists), > 0: that fixed size.  A warp whose records do not fit walks its
+ * lists instead, with bit-identical results, so the size only affects speed.
+ * No counterpart in the reference. */
+GBX_API gbx_status gbx_set_chain_records(gbx_context* ctx, int per_warp);
+
+/* Records of the last execute: written (-1 if it kept none), the largest
+ * per-warp need, the per-warp size and the warps that did not fit.
+ * Synchronises the context's stream. */
+GBX_API gbx_status gbx_get_chain_records(gbx_context* ctx, long long* written, int* max_need, int* per_warp,
+                                         int* overflowed);
+
 /* Per-stage device times (ms) of the last execute, from CUDA events recorded
  * on the execute stream when timing is enabled.  Stages: 0 position staging,
  * 1 lookup table, 2 integrals, 3 Born radii, 4 pair term, 5 chain prep,

@@ -26,7 +26,8 @@ EXPORTED = (
     "gbx_status_string", "gbx_version", "gbx_config_preset", "gbx_create", "gbx_destroy", "gbx_last_error",
     "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
-    "gbx_adjoint_host", "gbx_get_work", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
+    "gbx_adjoint_host", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
+    "gbx_get_chain_records", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
@@ -129,6 +130,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_get_lookup_table.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.gbx_adjoint_host.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.gbx_get_work.argtypes = [vp, vp, vp, vp]
+    L.gbx_get_chain_work.argtypes = [vp, vp, vp]
+    L.gbx_set_chain_records.argtypes = [vp, ci]
+    L.gbx_get_chain_records.argtypes = [vp, vp, vp, vp, vp]
     L.gbx_set_timing.argtypes = [vp, ci]
     L.gbx_get_stage_times.argtypes = [vp, vp, ci, vp]
     L.gbx_pair_noalloc.argtypes = [vp, vp, vp, ci, cd, cd, vp, ci, vp, vp, vp]
@@ -235,7 +239,20 @@ class Context:
     def work(self):
         v, s, p = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.gbx_get_work(self.h, ctypes.byref(v), ctypes.byref(s), ctypes.byref(p)))
-        return {"volume_evals": v.value, "shell_evals": s.value, "pairs": p.value}
+        fe, fs = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.gbx_get_chain_work(self.h, ctypes.byref(fe), ctypes.byref(fs)))
+        return {"volume_evals": v.value, "shell_evals": s.value, "pairs": p.value,
+                "chain_list_evals": fe.value, "chain_derivative_evals": fs.value}
+
+    def set_chain_records(self, per_warp: int):
+        """-1: automatic, 0: no chain records, > 0: records per (atom, quadrature chunk) warp."""
+        self._check(self.lib.gbx_set_chain_records(self.h, int(per_warp)))
+
+    def chain_records(self):
+        w, mx, R, over = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.gbx_get_chain_records(self.h, ctypes.byref(w), ctypes.byref(mx), ctypes.byref(R),
+                                                   ctypes.byref(over)))
+        return {"written": w.value, "max_need": mx.value, "per_warp": R.value, "overflowed": over.value}
 
     def set_timing(self, enable: bool = True):
         self._check(self.lib.gbx_set_timing(self.h, 1 if enable else 0))

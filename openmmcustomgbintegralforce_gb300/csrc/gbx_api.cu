@@ -167,12 +167,81 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_alpha_grad, 2));
   GBX_TRY(dalloc(ctx, &ctx->d_status, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_work, 4));
+  GBX_TRY(dalloc(ctx, &ctx->d_rmax, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_geom, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_tgeom, 1));
   GBX_CUDA(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
   GBX_CUDA(cudaMemset(ctx->d_work, 0, sizeof(unsigned long long) * 4));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_pos, sizeof(float4) * n));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_force_fx, sizeof(unsigned long long) * 3 * n));
+  GBX_CUDA(cudaMallocHost((void**)&ctx->h_rmax, sizeof(unsigned)));
+  *ctx->h_rmax = 0;
+  GBX_CUDA(cudaEventCreateWithFlags(&ctx->srec_ev, cudaEventDisableTiming));
+  return GBX_OK;
+}
+
+// (Re)allocates the chain-record buffer for R records per warp, within half
+// of the free device memory; on failure the context runs without records.
+gbx_status alloc_records(Context* ctx, int R) {
+  if (ctx->d_srec) {
+    GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_srec);
+  }
+  ctx->d_srec = nullptr;
+  ctx->srec_R = 0;
+  const long long warps = (long long)ctx->n * ctx->n_chunks;
+  if (R <= 0) return GBX_OK;
+  if (warps != ctx->srec_warps || !ctx->d_rcount) {
+    GBX_TRY(dalloc(ctx, &ctx->d_rcount, (size_t)warps));
+    ctx->srec_warps = warps;
+  }
+  size_t free_b = 0, total_b = 0;
+  GBX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const long long fit = (long long)(free_b / 2 / sizeof(int4)) / warps;
+  if ((long long)R > fit) R = (int)(fit / 32 * 32);
+  if (R <= 0 || cudaMalloc((void**)&ctx->d_srec, sizeof(int4) * (size_t)warps * R) != cudaSuccess) {
+    (void)cudaGetLastError();
+    ctx->d_srec = nullptr;
+    ctx->srec_auto = false;
+    return GBX_OK;
+  }
+  ctx->srec_R = R;
+  return GBX_OK;
+}
+
+// Decides whether this call records the GBSW chain rule's work and sizes the
+// per-warp regions from the largest need the device reported (read without
+// blocking; first guess half a warp's points).  Warps whose records do not
+// fit walk their lists in the chain rule instead, with the same result.
+gbx_status prepare_records(Context* ctx, bool wanted) {
+  ctx->records = false;
+  if (!wanted || ctx->cfg.model != GBX_MODEL_GBSW) return GBX_OK;
+  const long long warps = (long long)ctx->n * ctx->n_chunks;
+  if (ctx->srec_auto) {
+    long long need = 0;
+    if (ctx->srec_pending) {
+      const cudaError_t q = cudaEventQuery(ctx->srec_ev);
+      if (q == cudaSuccess) {
+        ctx->srec_pending = false;
+        const long long seen = *ctx->h_rmax;
+        if (seen > ctx->srec_R) need = seen + seen / 8 + 32;
+      } else if (q == cudaErrorNotReady) {
+        (void)cudaGetLastError();
+      } else {
+        GBX_CUDA(q);
+      }
+    }
+    if ((ctx->srec_R == 0 || warps != ctx->srec_warps) && need == 0 && !ctx->srec_pending) {
+      const long long points = ((long long)ctx->q_w.size() + ctx->n_chunks - 1) / ctx->n_chunks;
+      need = points / 2 + 32;
+    }
+    if (need > 0x40000000LL) need = 0x40000000LL;
+    if (need > ctx->srec_R || (need > 0 && warps != ctx->srec_warps))
+      GBX_TRY(alloc_records(ctx, (int)((need + 31) / 32 * 32)));
+  }
+  if (ctx->srec_R == 0 || warps != ctx->srec_warps) return GBX_OK;
+  ctx->records = true;
+  GBX_CUDA(cudaMemsetAsync(ctx->d_rmax, 0, sizeof(unsigned), ctx->stream));
   return GBX_OK;
 }
 
@@ -298,7 +367,7 @@ gbx_status build_tight_checked(Context* ctx, bool check) {
 }
 
 gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* force, int stride, double* energy,
-                        bool check, bool adjoint, bool count_work) {
+                        bool check, bool adjoint, bool count_work, bool forces = true) {
   int stage = 0;
   auto mark = [&]() -> gbx_status {
     if (ctx->timing) GBX_CUDA(cudaEventRecord(ctx->ev[stage], ctx->stream));
@@ -312,6 +381,8 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   if (ctx->use_tight) GBX_TRY(build_tight_checked(ctx, check || !ctx->tight_valid));
   else GBX_TRY(build_table_checked(ctx, check));
   if (count_work) GBX_CUDA(cudaMemsetAsync(ctx->d_work, 0, sizeof(unsigned long long) * 4, ctx->stream));
+  const bool chain = forces || adjoint;
+  GBX_TRY(prepare_records(ctx, chain && !adjoint && !count_work));
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_integrals(ctx, ctx->d_pos, count_work));
   GBX_TRY(mark());
@@ -325,7 +396,12 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_chain_prep(ctx, adjoint));
   GBX_TRY(mark());
-  GBX_TRY(gbx::launch_chain(ctx, ctx->d_pos, force, stride, adjoint));
+  if (chain) GBX_TRY(gbx::launch_chain(ctx, ctx->d_pos, force, stride, adjoint));
+  if (ctx->records && ctx->srec_auto && !ctx->srec_pending) {
+    GBX_CUDA(cudaMemcpyAsync(ctx->h_rmax, ctx->d_rmax, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GBX_CUDA(cudaEventRecord(ctx->srec_ev, ctx->stream));
+    ctx->srec_pending = true;
+  }
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_energy_reduce(ctx, energy, adjoint));
   GBX_TRY(mark());
@@ -493,13 +569,15 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell};
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)
     if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
   if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
   if (ctx->h_force_fx) cudaFreeHost(ctx->h_force_fx);
+  if (ctx->h_rmax) cudaFreeHost(ctx->h_rmax);
+  if (ctx->srec_ev) cudaEventDestroy(ctx->srec_ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return GBX_OK;
@@ -572,7 +650,7 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
   double* e = (flags & GBX_EXEC_ENERGY) ? energy : ctx->d_energy;
   const bool check = (flags & GBX_EXEC_CHECK) || (ctx->use_tight ? ctx->tcell_cap == 0 : ctx->cell_cap == 0);
   return run_pipeline(ctx, reinterpret_cast<const float4*>(posq), f, stride, e, check, false,
-                      (flags & GBX_EXEC_COUNT_WORK) != 0);
+                      (flags & GBX_EXEC_COUNT_WORK) != 0, (flags & GBX_EXEC_FORCES) != 0);
 }
 
 }  // extern "C"
@@ -759,6 +837,56 @@ gbx_status gbx_get_work(gbx_context* handle, double* volume_evals, double* shell
   if (volume_evals) *volume_evals = (double)w[0];
   if (shell_evals) *shell_evals = (double)w[1];
   if (pairs) *pairs = (double)ctx->n * (double)(ctx->n - 1);
+  return GBX_OK;
+}
+
+gbx_status gbx_set_chain_records(gbx_context* handle, int per_warp) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->srec_pending = false;
+  ctx->srec_auto = per_warp < 0;
+  GBX_TRY(alloc_records(ctx, per_warp > 0 ? per_warp : 0));
+  if (per_warp > 0 && ctx->srec_R != per_warp) {
+    ctx->last_error = "cannot allocate the chain-record buffer";
+    return GBX_ERR_OUT_OF_MEMORY;
+  }
+  return GBX_OK;
+}
+
+gbx_status gbx_get_chain_records(gbx_context* handle, long long* written, int* max_need, int* per_warp,
+                                 int* overflowed) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  long long w = -1;
+  int mx = 0, over = 0;
+  if (ctx->records) {
+    std::vector<int> cnt((size_t)ctx->srec_warps);
+    GBX_CUDA(cudaMemcpy(cnt.data(), ctx->d_rcount, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost));
+    w = 0;
+    for (int c : cnt) {
+      const int need = c >= 0 ? c : -1 - c;
+      if (c >= 0) w += c;
+      else ++over;
+      mx = need > mx ? need : mx;
+    }
+  }
+  if (written) *written = w;
+  if (max_need) *max_need = mx;
+  if (per_warp) *per_warp = ctx->srec_R;
+  if (overflowed) *overflowed = over;
+  return GBX_OK;
+}
+
+gbx_status gbx_get_chain_work(gbx_context* handle, double* list_evals, double* derivative_evals) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  unsigned long long w[4];
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(w, ctx->d_work, sizeof(w), cudaMemcpyDeviceToHost));
+  if (list_evals) *list_evals = (double)w[2];
+  if (derivative_evals) *derivative_evals = (double)w[3];
   return GBX_OK;
 }
 

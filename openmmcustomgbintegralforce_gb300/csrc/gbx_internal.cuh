@@ -127,6 +127,19 @@ struct Context {
   double* d_alpha_grad = nullptr; // adjoint [2]
   unsigned* d_status = nullptr;
   unsigned long long* d_work = nullptr;  // [4] evaluation counters
+
+  // GBSW chain-rule records (k, i, q, V u_k'/u_k) written by the integral
+  // pass: warp w (atom, quadrature chunk) owns records [w R, (w + 1) R)
+  bool records = false;          // this call writes and reads records
+  bool srec_auto = true;         // size R from the largest need seen
+  int4* d_srec = nullptr;
+  int srec_R = 0;                // records per warp (0: no buffer)
+  long long srec_warps = 0;      // warps the buffer was sized for
+  int* d_rcount = nullptr;       // [warps] records written, or -1 - needed
+  unsigned* d_rmax = nullptr;    // largest per-warp need of the call
+  unsigned* h_rmax = nullptr;    // pinned copy of the last d_rmax
+  cudaEvent_t srec_ev = nullptr;
+  bool srec_pending = false;     // srec_ev recorded and not yet read
   bool have_result = false;
 
   // optional per-stage timing (CUDA events on the execute stream)

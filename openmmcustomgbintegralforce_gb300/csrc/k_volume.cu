@@ -142,7 +142,8 @@ struct Work {
 };
 template <>
 struct Work<true> {
-  unsigned long long e = 0, s = 0;
+  unsigned long long e = 0, s = 0;    // the volume pass: list walk with the first-burying-atom exit
+  unsigned long long fe = 0, fs = 0;  // the chain pass: every listed atom of every point
   __device__ __forceinline__ void eval() { ++e; }
   __device__ __forceinline__ void shell() { ++s; }
 };
@@ -231,6 +232,29 @@ __device__ __forceinline__ float gbmv2_S(const ModelConst& m, const Gbmv2State& 
   return m.s0 * s.s1 * s.s2 / s3sq;
 }
 
+// Chain-pass work of one point, counted only for roofline accounting: the
+// reference chain kernel (reduceIntegralForce.cu:45-65) visits the whole cell
+// list of every point, with the derivative work inside the switching shell.
+template <int MODEL>
+__device__ __forceinline__ void count_chain_work(const ModelConst& m, const Entries& t, long long cell,
+                                                 const float4 xi, const float4 v, Work<true>& wk) {
+  if (cell < 0) return;
+  const int2 cs = __ldg(t.cell + cell);
+  if (cs.x <= 0) return;
+  wk.fe += cs.x;
+  if constexpr (MODEL != GBX_MODEL_GBSW) {
+    wk.fs += cs.x;
+  } else {
+    for (int l = 0; l < cs.x; ++l) {
+      const float4 a = __ldg(t.e + cs.y + l);
+      const float3 d = delta(a, xi, v);
+      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      const float lo = a.w - m.sw, hi = a.w + m.sw;
+      wk.fs += (r2 > lo * lo && r2 < hi * hi) ? 1 : 0;
+    }
+  }
+}
+
 template <int MODEL, class W>
 __device__ __forceinline__ float solvent_fraction(const ModelConst& m, const Entries& t, long long cell,
                                                   const float4 xi, const float4 v, W& wk) {
@@ -269,7 +293,9 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
   for (int q = q0 + lane; q < q1; q += kWarp) {
     const float4 v = quad.qv[q];
     const float2 w = quad.qw[q];
-    const float s = solvent_fraction<MODEL>(m, tab, query.cell(xi, v, q), xi, v, wk);
+    const long long cell = query.cell(xi, v, q);
+    const float s = solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
+    if constexpr (COUNT) count_chain_work<MODEL>(m, tab, cell, xi, v, wk);
     J4 = fmaf(w.x, s, J4);
     J7 = fmaf(w.y, s, J7);
   }
@@ -282,15 +308,175 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
     Jpart[((size_t)n_chunks + c) * n + i] = J7;
   }
   if constexpr (COUNT) {
-    unsigned long long e = wk.e, sh = wk.s;
+    unsigned long long e = wk.e, sh = wk.s, fe = wk.fe, fs = wk.fs;
     for (int off = 16; off > 0; off >>= 1) {
       e += __shfl_xor_sync(0xffffffffu, e, off);
       sh += __shfl_xor_sync(0xffffffffu, sh, off);
+      fe += __shfl_xor_sync(0xffffffffu, fe, off);
+      fs += __shfl_xor_sync(0xffffffffu, fs, off);
     }
     if (lane == 0) {
       atomicAdd(&work[0], e);
       atomicAdd(&work[1], sh);
+      atomicAdd(&work[2], fe);
+      atomicAdd(&work[3], fs);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GBSW integral pass that also records the chain rule's work.  For each point
+// with V > 0 it writes one record (k, i, q, V u_k'/u_k) per in-shell atom
+// k != i: everything of dV/dx_k that does not depend on the Born radii.  The
+// chain rule then reads these records instead of re-walking every point's
+// list with most lanes of the warp idle.  Warp w owns records
+// [w R, (w + 1) R); the records of one batch of 32 points are contiguous, so
+// the stores coalesce.  count[w] = records written, or -1 - needed when they
+// did not fit (the chain rule walks that warp's lists instead).
+// ---------------------------------------------------------------------------
+constexpr int kKeep = 4;  // in-shell atoms remembered from the walk
+
+struct ShellSink {
+  int4* rec;
+  int* count;          // [warps]
+  unsigned* max_seen;  // largest per-warp need of this call
+  int R;               // records per warp
+};
+
+__device__ __forceinline__ float shell_g(const ModelConst& m, float V, float dr) {
+  const float u = fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+  const float du = fmaf(-3.0f * m.c3 * dr, dr, m.c1);
+  return __fdividef(V, u) * du;
+}
+
+// True if list entry l is atom i itself: its inline position is bitwise
+// atom i's, and only then is the index read.
+__device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const int* __restrict__ index, int l, int i) {
+  return a.x == xi.x && a.y == xi.y && a.z == xi.z && __ldg(index + l) == i;
+}
+
+struct Kept {
+  int l[kKeep];
+  float dr[kKeep];
+};
+
+// Remembers in-shell entry number t (list position l) while t < kKeep;
+// unrolled so the arrays stay in registers.
+__device__ __forceinline__ void keep_entry(Kept& kp, int t, int l, float dr) {
+#pragma unroll
+  for (int u = 0; u < kKeep; ++u)
+    if (t == u) {
+      kp.l[u] = l;
+      kp.dr[u] = dr;
+    }
+}
+
+// Writes the point's records to dst[0..nrec).
+__device__ __forceinline__ void emit_point(int4* dst, const ModelConst& m, const float4* __restrict__ list,
+                                           const int* __restrict__ index, int cnt, int i, int q, const float4 xi,
+                                           const float4 v, float V, int nrec, const Kept& kp) {
+  if (nrec <= kKeep) {
+    int k[kKeep];
+#pragma unroll
+    for (int u = 0; u < kKeep; ++u) k[u] = u < nrec ? __ldg(index + kp.l[u]) : 0;
+#pragma unroll
+    for (int u = 0; u < kKeep; ++u)
+      if (u < nrec) dst[u] = make_int4(k[u], i, q, __float_as_int(shell_g(m, V, kp.dr[u])));
+    return;
+  }
+  int t = 0;
+  for (int l = 0; l < cnt && t < nrec; ++l) {
+    const float4 a = __ldg(list + l);
+    const float3 d = delta(a, xi, v);
+    const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+    const float lo = a.w - m.sw, hi = a.w + m.sw;
+    if (r2 > lo * lo && r2 < hi * hi && !is_self(a, xi, index, l, i))
+      dst[t++] = make_int4(__ldg(index + l), i, q, __float_as_int(shell_g(m, V, r2 * rsqrtf(r2) - a.w)));
+  }
+}
+
+template <class Q>
+__global__ void __launch_bounds__(kThreads) integral_emit_kernel(const float4* __restrict__ pos, int n, Entries tab,
+                                                                 Quad quad, ModelConst m, int chunk, int n_chunks,
+                                                                 float* __restrict__ Jpart, ShellSink sink) {
+  __shared__ unsigned s_max[kThreads / kWarp];
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  const int wib = threadIdx.x / kWarp;
+  int fill = 0;  // warp-uniform: records this warp produced (may exceed R)
+  if (warp < n * n_chunks) {
+    const int i = warp % n, c = warp / n;
+    int4* region = sink.rec + (size_t)warp * sink.R;
+    const float4 xi = pos[i];
+    Q query;
+    query.init(*tab.geom, xi, quad.qoff);
+    const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+    float J4 = 0.0f, J7 = 0.0f;
+    for (int qb = q0; qb < q1; qb += kWarp) {
+      const int q = qb + lane;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      float V = 1.0f;
+      int nrec = 0, cnt = 0, s = 0;
+      Kept kp;
+      if (q < q1) {
+        v = quad.qv[q];
+        const float2 w = quad.qw[q];
+        const long long cell = query.cell(xi, v, q);
+        if (cell >= 0) {
+          const int2 cs = __ldg(tab.cell + cell);
+          cnt = cs.x;
+          s = cs.y;
+        }
+        if (cnt < 0) {
+          V = 0.0f;  // buried cell
+        } else {
+          const float4* E = tab.e + s;
+          for (int l = 0; l < cnt; ++l) {
+            const float4 a = __ldg(E + l);
+            const float3 d = delta(a, xi, v);
+            const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+            const float lo = a.w - m.sw, hi = a.w + m.sw;
+            if (r2 <= lo * lo) {
+              V = 0.0f;
+              break;
+            }
+            if (r2 < hi * hi) {
+              const float dr = r2 * rsqrtf(r2) - a.w;
+              V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+              if (!is_self(a, xi, tab.index + s, l, i)) keep_entry(kp, nrec++, l, dr);
+            }
+          }
+        }
+        J4 = fmaf(w.x, V, J4);
+        J7 = fmaf(w.y, V, J7);
+      }
+      if (V == 0.0f) nrec = 0;
+      int incl = nrec;  // warp-inclusive scan of the record counts
+      for (int off = 1; off < kWarp; off <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += u;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, kWarp - 1);
+      if (nrec > 0 && fill + total <= sink.R)
+        emit_point(region + fill + incl - nrec, m, tab.e + s, tab.index + s, cnt, i, q, xi, v, V, nrec, kp);
+      fill += total;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      J4 += __shfl_xor_sync(0xffffffffu, J4, off);
+      J7 += __shfl_xor_sync(0xffffffffu, J7, off);
+    }
+    if (lane == 0) {
+      Jpart[(size_t)c * n + i] = J4;
+      Jpart[((size_t)n_chunks + c) * n + i] = J7;
+      sink.count[warp] = fill <= sink.R ? fill : -1 - fill;
+    }
+  }
+  if (lane == 0) s_max[wib] = (unsigned)fill;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned mx = 0;
+    for (int k = 0; k < kThreads / kWarp; ++k) mx = max(mx, s_max[k]);
+    if (mx > 0) atomicMax(sink.max_seen, mx);
   }
 }
 
@@ -311,6 +497,13 @@ struct ChainOut {
   float cutoff2;
 };
 
+// Records of the emitting integral pass (rec == nullptr: none this call).
+struct ChainRecords {
+  const int4* rec;
+  const int* count;
+  int R;
+};
+
 __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, float gy, float gz) {
   red_add_fixed(&o.force[k], -gx);
   red_add_fixed(&o.force[k + o.stride], -gy);
@@ -320,136 +513,158 @@ __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, f
 template <int MODEL, class Q, bool ADJ>
 __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                          Quad quad, ModelConst m, int chunk, int n_chunks,
-                                                         const float2* __restrict__ dEdJ, ChainOut out) {
-  constexpr int kKeep = 4;  // GBSW: in-shell entries remembered from the volume pass
+                                                         const float2* __restrict__ dEdJ, ChainOut out,
+                                                         ChainRecords rr) {
+  constexpr int kWalkKeep = 4;  // GBSW: in-shell entries remembered from the volume pass
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (warp >= n * n_chunks) return;
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   const float2 de = dEdJ[i];
-  Q query;
-  query.init(*tab.geom, xi, quad.qoff);
-  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
-  float fix = 0.f, fiy = 0.f, fiz = 0.f;
-  for (int q = q0 + lane; q < q1; q += kWarp) {
-    const float4 v = quad.qv[q];
-    const float2 w = quad.qw[q];
-    const float cq = fmaf(de.x, w.x, de.y * w.y);
-    if (cq == 0.0f) continue;
-    const long long cell = query.cell(xi, v, q);
-    if (cell < 0) continue;
-    const int2 cs = __ldg(tab.cell + cell);
-    const int cnt = cs.x;
-    if (cnt <= 0) continue;  // buried or empty: no atom shapes the point
-    const int s = cs.y;
-    const float4* E = tab.e + s;
-    if (MODEL == GBX_MODEL_GBSW) {
-      float V = 1.0f;
-      int keep[kKeep];
-      int nk = 0, nshell = 0;
-      for (int l = 0; l < cnt; ++l) {
-        const float4 a = __ldg(E + l);
-        const float3 d = delta(a, xi, v);
-        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-        const float lo = a.w - m.sw, hi = a.w + m.sw;
-        if (r2 <= lo * lo) {
-          V = 0.0f;
-          break;
+  // F_i as fixed-point integers: every contribution is rounded on its own, so
+  // the record and the list-walk paths give the same bits
+  long long fix = 0, fiy = 0, fiz = 0;
+  const int nrec = rr.count ? rr.count[warp] : -1;
+  if (MODEL == GBX_MODEL_GBSW && !ADJ && nrec >= 0) {
+    const int4* region = rr.rec + (size_t)warp * rr.R;
+    for (int t = lane; t < nrec; t += kWarp) {
+      const int4 rc = region[t];
+      const int k = rc.x;
+      const float4 a = pos[k], v = quad.qv[rc.z];
+      const float2 w = quad.qw[rc.z];
+      const float cq = fmaf(de.x, w.x, de.y * w.y);
+      const float3 d = delta(a, xi, v);
+      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      const float gs = cq * __int_as_float(rc.w) * rsqrtf(r2);
+      const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
+      const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+      if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2) push_force(out, k, gx, gy, gz);
+      fix += float_to_fixed(gx);
+      fiy += float_to_fixed(gy);
+      fiz += float_to_fixed(gz);
+    }
+  } else {
+    Q query;
+    query.init(*tab.geom, xi, quad.qoff);
+    const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+    for (int q = q0 + lane; q < q1; q += kWarp) {
+      const float4 v = quad.qv[q];
+      const float2 w = quad.qw[q];
+      const float cq = fmaf(de.x, w.x, de.y * w.y);
+      if (cq == 0.0f) continue;
+      const long long cell = query.cell(xi, v, q);
+      if (cell < 0) continue;
+      const int2 cs = __ldg(tab.cell + cell);
+      const int cnt = cs.x;
+      if (cnt <= 0) continue;  // buried or empty: no atom shapes the point
+      const int s = cs.y;
+      const float4* E = tab.e + s;
+      if (MODEL == GBX_MODEL_GBSW) {
+        float V = 1.0f;
+        int keep[kWalkKeep];
+        int nk = 0, nshell = 0;
+        for (int l = 0; l < cnt; ++l) {
+          const float4 a = __ldg(E + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float lo = a.w - m.sw, hi = a.w + m.sw;
+          if (r2 <= lo * lo) {
+            V = 0.0f;
+            break;
+          }
+          if (r2 < hi * hi) {
+            const float dr = r2 * rsqrtf(r2) - a.w;
+            V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+            if (nk < kWalkKeep) keep[nk++] = l;
+            ++nshell;
+          }
         }
-        if (r2 < hi * hi) {
-          const float dr = r2 * rsqrtf(r2) - a.w;
-          V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-          if (nk < kKeep) keep[nk++] = l;
-          ++nshell;
+        if (V == 0.0f || nshell == 0) continue;
+        const int scan = nshell <= kWalkKeep ? nk : cnt;
+        for (int t = 0; t < scan; ++t) {
+          const int l = nshell <= kWalkKeep ? keep[t] : t;
+          const float4 a = __ldg(E + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float lo = a.w - m.sw, hi = a.w + m.sw;
+          if (!(r2 > lo * lo && r2 < hi * hi)) continue;
+          // the same expressions as the record path (shell_g, then c g / r)
+          const float g = shell_g(m, V, r2 * rsqrtf(r2) - a.w);
+          const int k = __ldg(tab.index + s + l);
+          // dV/dR_k = -(V/u) u' dR'/dR with R' = (R + 0.03) 0.952
+          if (ADJ) red_add_fixed(&out.dEdR[k], cq * g * (-0.9520f));
+          if (k == i) continue;
+          const float gs = cq * g * rsqrtf(r2);
+          const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
+          const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+          if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2) push_force(out, k, gx, gy, gz);
+          fix += float_to_fixed(gx);
+          fiy += float_to_fixed(gy);
+          fiz += float_to_fixed(gz);
         }
-      }
-      if (V == 0.0f || nshell == 0) continue;
-      const int scan = nshell <= kKeep ? nk : cnt;
-      for (int t = 0; t < scan; ++t) {
-        const int l = nshell <= kKeep ? keep[t] : t;
-        const float4 a = __ldg(E + l);
-        const float3 d = delta(a, xi, v);
-        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-        const float lo = a.w - m.sw, hi = a.w + m.sw;
-        if (!(r2 > lo * lo && r2 < hi * hi)) continue;
-        const float inv_r = rsqrtf(r2);
-        const float dr = r2 * inv_r - a.w;
-        const float u = fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-        const float du = fmaf(-3.0f * m.c3 * dr, dr, m.c1);
-        const float Vu = __fdividef(V, u);
-        const int k = __ldg(tab.index + s + l);
-        // dV/dR_k = -(V/u) u' dR'/dR with R' = (R + 0.03) 0.952
-        if (ADJ) red_add_fixed(&out.dEdR[k], cq * Vu * du * (-0.9520f));
-        if (k == i) continue;
-        const float gs = cq * Vu * du * inv_r;
-        const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
-        if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2)
-          push_force(out, k, gs * d.x, gs * d.y, gs * d.z);
-        fix = fmaf(gs, d.x, fix);
-        fiy = fmaf(gs, d.y, fiy);
-        fiz = fmaf(gs, d.z, fiz);
-      }
-    } else if (MODEL == GBX_MODEL_GBMV1) {
-      Work<false> wk;
-      float p;
-      logistic_solvent(m.beta, m.lambda, gbmv1_sum(E, cnt, xi, v, wk), p);
-      const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
-      if (cS == 0.0f) continue;
-      for (int l = 0; l < cnt; ++l) {
-        const float4 a = __ldg(E + l);
-        const float3 d = delta(a, xi, v);
-        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-        const float r4 = r2 * r2;
-        const float e = __expf(a.w * r4);
-        const int k = __ldg(tab.index + s + l);
-        if (ADJ) red_add_fixed(&out.dEdR[k], cS * e * r4 * (-4.0f * a.w / __ldg(&tab.par[s + l].x)));
-        if (k == i) continue;
-        const float gs = cS * 4.0f * a.w * e * r2;  // dS/d(delta) = 4 gamma e r^2 delta
-        push_force(out, k, gs * d.x, gs * d.y, gs * d.z);
-        fix = fmaf(gs, d.x, fix);
-        fiy = fmaf(gs, d.y, fiy);
-        fiz = fmaf(gs, d.z, fiz);
-      }
-    } else {
-      Work<false> wk;
-      const Gbmv2State st = gbmv2_sums(E, tab.par + s, cnt, xi, v, wk);
-      const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
-      float p;
-      logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
-      const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p)) * m.s0;
-      if (cS == 0.0f) continue;
-      const float inv3 = 1.0f / s3sq;
-      const float t1 = st.s2 * inv3;                  // d s1 term
-      const float t2 = st.s1 * inv3;                  // d s2 term
-      const float t3 = -st.s1 * st.s2 * inv3 * inv3;  // d s3^2 term
-      for (int l = 0; l < cnt; ++l) {
-        const float4 a = __ldg(E + l);
-        const float2 pk = __ldg(tab.par + s + l);
-        const float3 d = delta(a, xi, v);
-        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-        const float T = fmaf(100.0f, r2, pk.x);
-        const float CT = __fdividef(a.w, T);
-        const float F = CT * CT;
-        const float dFf = -400.0f * F * __fdividef(1.0f, T);  // dF/d(delta) = dFf delta
-        const float vd = st.vx * d.x + st.vy * d.y + st.vz * d.z;
-        const int k = __ldg(tab.index + s + l);
-        if (ADJ) {
-          const float R = pk.y;
-          const float Cp = 10.0f * m.p1, Tp = Cp - 200.0f * R;
-          const float dFdR = 2.0f * CT * __fdividef(Cp * T - a.w * Tp, T * T);
-          red_add_fixed(&out.dEdR[k], cS * (t1 * dFdR + t2 * (r2 * 2.0f * F * dFdR) + t3 * (2.0f * vd * dFdR)));
+      } else if (MODEL == GBX_MODEL_GBMV1) {
+        Work<false> wk;
+        float p;
+        logistic_solvent(m.beta, m.lambda, gbmv1_sum(E, cnt, xi, v, wk), p);
+        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
+        if (cS == 0.0f) continue;
+        for (int l = 0; l < cnt; ++l) {
+          const float4 a = __ldg(E + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float r4 = r2 * r2;
+          const float e = __expf(a.w * r4);
+          const int k = __ldg(tab.index + s + l);
+          if (ADJ) red_add_fixed(&out.dEdR[k], cS * e * r4 * (-4.0f * a.w / __ldg(&tab.par[s + l].x)));
+          if (k == i) continue;
+          const float gs = cS * 4.0f * a.w * e * r2;  // dS/d(delta) = 4 gamma e r^2 delta
+          const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
+          push_force(out, k, gx, gy, gz);
+          fix += float_to_fixed(gx);
+          fiy += float_to_fixed(gy);
+          fiz += float_to_fixed(gz);
         }
-        if (k == i) continue;
-        // dS/d(delta_k) / s0 = t1 dFf d + t2 2F (F + dFf r^2) d + 2 t3 (F v + vd dFf d)
-        const float sc = t1 * dFf + t2 * 2.0f * F * fmaf(dFf, r2, F) + t3 * 2.0f * vd * dFf;
-        const float gx = cS * fmaf(sc, d.x, t3 * 2.0f * F * st.vx);
-        const float gy = cS * fmaf(sc, d.y, t3 * 2.0f * F * st.vy);
-        const float gz = cS * fmaf(sc, d.z, t3 * 2.0f * F * st.vz);
-        push_force(out, k, gx, gy, gz);
-        fix += gx;
-        fiy += gy;
-        fiz += gz;
+      } else {
+        Work<false> wk;
+        const Gbmv2State st = gbmv2_sums(E, tab.par + s, cnt, xi, v, wk);
+        const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
+        float p;
+        logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
+        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p)) * m.s0;
+        if (cS == 0.0f) continue;
+        const float inv3 = 1.0f / s3sq;
+        const float t1 = st.s2 * inv3;                  // d s1 term
+        const float t2 = st.s1 * inv3;                  // d s2 term
+        const float t3 = -st.s1 * st.s2 * inv3 * inv3;  // d s3^2 term
+        for (int l = 0; l < cnt; ++l) {
+          const float4 a = __ldg(E + l);
+          const float2 pk = __ldg(tab.par + s + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float T = fmaf(100.0f, r2, pk.x);
+          const float CT = __fdividef(a.w, T);
+          const float F = CT * CT;
+          const float dFf = -400.0f * F * __fdividef(1.0f, T);  // dF/d(delta) = dFf delta
+          const float vd = st.vx * d.x + st.vy * d.y + st.vz * d.z;
+          const int k = __ldg(tab.index + s + l);
+          if (ADJ) {
+            const float R = pk.y;
+            const float Cp = 10.0f * m.p1, Tp = Cp - 200.0f * R;
+            const float dFdR = 2.0f * CT * __fdividef(Cp * T - a.w * Tp, T * T);
+            red_add_fixed(&out.dEdR[k], cS * (t1 * dFdR + t2 * (r2 * 2.0f * F * dFdR) + t3 * (2.0f * vd * dFdR)));
+          }
+          if (k == i) continue;
+          // dS/d(delta_k) / s0 = t1 dFf d + t2 2F (F + dFf r^2) d + 2 t3 (F v + vd dFf d)
+          const float sc = t1 * dFf + t2 * 2.0f * F * fmaf(dFf, r2, F) + t3 * 2.0f * vd * dFf;
+          const float gx = cS * fmaf(sc, d.x, t3 * 2.0f * F * st.vx);
+          const float gy = cS * fmaf(sc, d.y, t3 * 2.0f * F * st.vy);
+          const float gz = cS * fmaf(sc, d.z, t3 * 2.0f * F * st.vz);
+          push_force(out, k, gx, gy, gz);
+          fix += float_to_fixed(gx);
+          fiy += float_to_fixed(gy);
+          fiz += float_to_fixed(gz);
+        }
       }
     }
   }
@@ -459,9 +674,9 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
     fiz += __shfl_xor_sync(0xffffffffu, fiz, off);
   }
   if (lane == 0) {
-    red_add_fixed(&out.force[i], fix);
-    red_add_fixed(&out.force[i + out.stride], fiy);
-    red_add_fixed(&out.force[i + 2 * out.stride], fiz);
+    atomicAdd(&out.force[i], (unsigned long long)fix);
+    atomicAdd(&out.force[i + out.stride], (unsigned long long)fiy);
+    atomicAdd(&out.force[i + 2 * out.stride], (unsigned long long)fiz);
   }
 }
 
@@ -481,7 +696,11 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   const Entries t = entries_of(ctx);
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
-  if (count_work)
+  if (MODEL == GBX_MODEL_GBSW && ctx->records && !count_work)
+    integral_emit_kernel<Q><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J,
+        ShellSink{ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->srec_R});
+  else if (count_work)
     integral_kernel<MODEL, Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work);
   else
@@ -495,8 +714,10 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
   ChainOut o{force, stride, ctx->d_dEdR_fx, m.cutoff_chain_quirk && m.cutoff2 > 0.0f, m.cutoff2};
+  const bool records = MODEL == GBX_MODEL_GBSW && !ADJ && ctx->records;
+  const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R};
   chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
-                                                                                ctx->n_chunks, ctx->d_dEdJ, o);
+                                                                                ctx->n_chunks, ctx->d_dEdJ, o, rr);
 }
 
 gbx_status launch_status(Context* ctx, const char* what) {
