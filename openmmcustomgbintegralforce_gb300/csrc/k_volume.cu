@@ -326,13 +326,14 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
 
 // ---------------------------------------------------------------------------
 // GBSW integral pass that also records the chain rule's work.  For each point
-// with V > 0 it writes one record (k, i, q, V u_k'/u_k) per in-shell atom
+// with V > 0 it writes one record (e, i, q, V u_k'/u_k) per in-shell atom
 // k != i: everything of dV/dx_k that does not depend on the Born radii.  The
 // chain rule then reads these records instead of re-walking every point's
 // list with most lanes of the warp idle.  Warp w owns records
-// [w R, (w + 1) R); the records of one batch of 32 points are contiguous, so
-// the stores coalesce.  count[w] = records written, or -1 - needed when they
-// did not fit (the chain rule walks that warp's lists instead).
+// [w R, (w + 1) R), filled in the order points finish; count[w] = records
+// written, or -1 - needed when they did not fit (the chain rule walks that
+// warp's lists instead).  Records are stored evict-first: they are read once,
+// and the lookup table must stay in L2.
 // ---------------------------------------------------------------------------
 constexpr int kKeep = 4;  // in-shell atoms remembered from the walk
 
@@ -355,129 +356,158 @@ __device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const i
   return a.x == xi.x && a.y == xi.y && a.z == xi.z && __ldg(index + l) == i;
 }
 
-struct Kept {
-  int l[kKeep];
-  float dr[kKeep];
-};
-
-// Remembers in-shell entry number t (list position l) while t < kKeep;
-// unrolled so the arrays stay in registers.
-__device__ __forceinline__ void keep_entry(Kept& kp, int t, int l, float dr) {
-#pragma unroll
-  for (int u = 0; u < kKeep; ++u)
-    if (t == u) {
-      kp.l[u] = l;
-      kp.dr[u] = dr;
-    }
-}
-
-// Writes the point's records to dst[0..nrec).
-__device__ __forceinline__ void emit_point(int4* dst, const ModelConst& m, const float4* __restrict__ list,
-                                           const int* __restrict__ index, int cnt, int i, int q, const float4 xi,
-                                           const float4 v, float V, int nrec, const Kept& kp) {
+// Writes the point's records to dst[0..nrec): (table entry position, i, q,
+// V u'/u) -- the chain rule reads the atom's index and position from the
+// entry, so nothing here waits on a load.  keep[u * kWarp] holds (list
+// position, dr) of the lane's in-shell entry u, u < kKeep.
+__device__ __forceinline__ void emit_point_kept(int4* dst, const ModelConst& m, const Entries& tab, int s, int cnt,
+                                                int i, int q, const float4 xi, const float4 v, float V, int nrec,
+                                                const float2* keep) {
   if (nrec <= kKeep) {
-    int k[kKeep];
-#pragma unroll
-    for (int u = 0; u < kKeep; ++u) k[u] = u < nrec ? __ldg(index + kp.l[u]) : 0;
-#pragma unroll
-    for (int u = 0; u < kKeep; ++u)
-      if (u < nrec) dst[u] = make_int4(k[u], i, q, __float_as_int(shell_g(m, V, kp.dr[u])));
+    for (int u = 0; u < nrec; ++u) {
+      const float2 e = keep[u * kWarp];
+      __stcs(dst + u, make_int4(s + __float_as_int(e.x), i, q, __float_as_int(shell_g(m, V, e.y))));
+    }
     return;
   }
   int t = 0;
   for (int l = 0; l < cnt && t < nrec; ++l) {
-    const float4 a = __ldg(list + l);
+    const float4 a = __ldg(tab.e + s + l);
     const float3 d = delta(a, xi, v);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     const float lo = a.w - m.sw, hi = a.w + m.sw;
-    if (r2 > lo * lo && r2 < hi * hi && !is_self(a, xi, index, l, i))
-      dst[t++] = make_int4(__ldg(index + l), i, q, __float_as_int(shell_g(m, V, r2 * rsqrtf(r2) - a.w)));
+    if (r2 > lo * lo && r2 < hi * hi && !is_self(a, xi, tab.index + s, l, i))
+      __stcs(dst + t++, make_int4(s + l, i, q, __float_as_int(shell_g(m, V, r2 * rsqrtf(r2) - a.w))));
   }
 }
 
-template <class Q>
-__global__ void __launch_bounds__(kThreads) integral_emit_kernel(const float4* __restrict__ pos, int n, Entries tab,
+// GBSW integrals with lanes refilled from a queue.  A warp classifies a
+// stage of kStage points at once (empty cell: V = 1; buried cell: V = 0) and
+// queues the points that have a list; then every lane evaluates one list
+// entry per iteration and takes the next queued point as soon as its own is
+// finished, so a long list keeps one lane busy instead of the whole warp
+// waiting on it.  The walk per point is the sequential one of gbsw_volume
+// (same order, same early exit).  J is summed in an order fixed by the input
+// alone, so runs are bit-reproducible.  With EMIT the finished points write
+// their chain records (see integral records above).
+constexpr int kStage = 256;
+
+template <class Q, bool EMIT>
+__global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                                  Quad quad, ModelConst m, int chunk, int n_chunks,
                                                                  float* __restrict__ Jpart, ShellSink sink) {
-  __shared__ unsigned s_max[kThreads / kWarp];
+  __shared__ int3 s_queue[kThreads / kWarp][kStage];  // (q, list start, list length)
+  __shared__ float2 s_keep[kThreads / kWarp][EMIT ? kKeep * kWarp : 1];
+  __shared__ int s_fill[kThreads / kWarp];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
-  int fill = 0;  // warp-uniform: records this warp produced (may exceed R)
+  const unsigned lt = (1u << lane) - 1u;
+  int fill = 0;  // records this warp produced (may exceed R)
+  if (lane == 0) s_fill[wib] = 0;
+  __syncwarp();
   if (warp < n * n_chunks) {
+    int3* queue = s_queue[wib];
+    float2* keep = s_keep[wib] + (EMIT ? lane : 0);
     const int i = warp % n, c = warp / n;
-    int4* region = sink.rec + (size_t)warp * sink.R;
+    int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
     const float4 xi = pos[i];
     Q query;
     query.init(*tab.geom, xi, quad.qoff);
     const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
     float J4 = 0.0f, J7 = 0.0f;
-    for (int qb = q0; qb < q1; qb += kWarp) {
-      const int q = qb + lane;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      float V = 1.0f;
-      int nrec = 0, cnt = 0, s = 0;
-      Kept kp;
-      if (q < q1) {
-        v = quad.qv[q];
-        const float2 w = quad.qw[q];
-        const long long cell = query.cell(xi, v, q);
-        if (cell >= 0) {
-          const int2 cs = __ldg(tab.cell + cell);
-          cnt = cs.x;
-          s = cs.y;
+    for (int base = q0; base < q1; base += kStage) {
+      int nq = 0;  // warp-uniform queue length
+#pragma unroll 4
+      for (int k = 0; k < kStage / kWarp; ++k) {
+        const int q = base + k * kWarp + lane;
+        int2 cs = make_int2(-1, 0);
+        if (q < q1) {
+          const float4 v = quad.qv[q];
+          const long long cell = query.cell(xi, v, q);
+          cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
+          if (cs.x == 0) {
+            const float2 w = quad.qw[q];
+            J4 += w.x;
+            J7 += w.y;
+          }
         }
-        if (cnt < 0) {
-          V = 0.0f;  // buried cell
-        } else {
-          const float4* E = tab.e + s;
-          for (int l = 0; l < cnt; ++l) {
-            const float4 a = __ldg(E + l);
-            const float3 d = delta(a, xi, v);
-            const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-            const float lo = a.w - m.sw, hi = a.w + m.sw;
-            if (r2 <= lo * lo) {
-              V = 0.0f;
-              break;
-            }
+        const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
+        if (cs.x > 0) queue[nq + __popc(qm & lt)] = make_int3(q, cs.y, cs.x);
+        nq += __popc(qm);
+      }
+      __syncwarp();
+      int head = 0, q = 0, s = 0, cnt = 0, l = 0, nrec = 0;
+      bool has = false;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 w = make_float2(0.f, 0.f);
+      float V = 1.0f;
+      while (true) {
+        const unsigned need = __ballot_sync(0xffffffffu, !has);
+        if (!has) {
+          const int idx = head + __popc(need & lt);
+          if (idx < nq) {
+            const int3 e = queue[idx];
+            q = e.x;
+            s = e.y;
+            cnt = e.z;
+            l = 0;
+            nrec = 0;
+            V = 1.0f;
+            has = true;
+            v = quad.qv[q];
+            w = quad.qw[q];
+          }
+        }
+        head += __popc(need);
+        if (__ballot_sync(0xffffffffu, has) == 0u) break;
+        bool fin = false;
+        if (has) {
+          const float4 a = __ldg(tab.e + s + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float lo = a.w - m.sw, hi = a.w + m.sw;
+          if (r2 <= lo * lo) {
+            V = 0.0f;
+            fin = true;
+          } else {
             if (r2 < hi * hi) {
               const float dr = r2 * rsqrtf(r2) - a.w;
               V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-              if (!is_self(a, xi, tab.index + s, l, i)) keep_entry(kp, nrec++, l, dr);
+              if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
+                if (nrec < kKeep) keep[nrec * kWarp] = make_float2(__int_as_float(l), dr);
+                ++nrec;
+              }
             }
+            fin = ++l == cnt;
           }
         }
-        J4 = fmaf(w.x, V, J4);
-        J7 = fmaf(w.y, V, J7);
+        if (fin) {
+          J4 = fmaf(w.x, V, J4);
+          J7 = fmaf(w.y, V, J7);
+          has = false;
+        }
+        if (EMIT && fin && V != 0.0f && nrec > 0) {
+          // slots in any order: the chain rule's sums do not depend on it
+          const int slot = atomicAdd(&s_fill[wib], nrec);
+          if (slot + nrec <= sink.R) emit_point_kept(region + slot, m, tab, s, cnt, i, q, xi, v, V, nrec, keep);
+        }
       }
-      if (V == 0.0f) nrec = 0;
-      int incl = nrec;  // warp-inclusive scan of the record counts
-      for (int off = 1; off < kWarp; off <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += u;
-      }
-      const int total = __shfl_sync(0xffffffffu, incl, kWarp - 1);
-      if (nrec > 0 && fill + total <= sink.R)
-        emit_point(region + fill + incl - nrec, m, tab.e + s, tab.index + s, cnt, i, q, xi, v, V, nrec, kp);
-      fill += total;
+      __syncwarp();  // the next stage rewrites the queue
     }
     for (int off = 16; off > 0; off >>= 1) {
       J4 += __shfl_xor_sync(0xffffffffu, J4, off);
       J7 += __shfl_xor_sync(0xffffffffu, J7, off);
     }
+    __syncwarp();
+    fill = s_fill[wib];
     if (lane == 0) {
       Jpart[(size_t)c * n + i] = J4;
       Jpart[((size_t)n_chunks + c) * n + i] = J7;
-      sink.count[warp] = fill <= sink.R ? fill : -1 - fill;
+      if (EMIT) sink.count[warp] = fill <= sink.R ? fill : -1 - fill;
     }
   }
-  if (lane == 0) s_max[wib] = (unsigned)fill;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned mx = 0;
-    for (int k = 0; k < kThreads / kWarp; ++k) mx = max(mx, s_max[k]);
-    if (mx > 0) atomicMax(sink.max_seen, mx);
-  }
+  if (EMIT && lane == 0 && fill > 0) atomicMax(sink.max_seen, (unsigned)fill);
 }
 
 // ---------------------------------------------------------------------------
@@ -529,9 +559,9 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   if (MODEL == GBX_MODEL_GBSW && !ADJ && nrec >= 0) {
     const int4* region = rr.rec + (size_t)warp * rr.R;
     for (int t = lane; t < nrec; t += kWarp) {
-      const int4 rc = region[t];
-      const int k = rc.x;
-      const float4 a = pos[k], v = quad.qv[rc.z];
+      const int4 rc = __ldcs(region + t);
+      const float4 a = __ldg(tab.e + rc.x), v = quad.qv[rc.z];
+      const int k = __ldg(tab.index + rc.x);
       const float2 w = quad.qw[rc.z];
       const float cq = fmaf(de.x, w.x, de.y * w.y);
       const float3 d = delta(a, xi, v);
@@ -696,10 +726,13 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   const Entries t = entries_of(ctx);
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
+  const ShellSink sink{ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->srec_R};
   if (MODEL == GBX_MODEL_GBSW && ctx->records && !count_work)
-    integral_emit_kernel<Q><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
-        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J,
-        ShellSink{ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->srec_R});
+    gbsw_integral_kernel<Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
+  else if (MODEL == GBX_MODEL_GBSW && !count_work)
+    gbsw_integral_kernel<Q, false><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
   else if (count_work)
     integral_kernel<MODEL, Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work);
