@@ -179,10 +179,10 @@ GBX_API gbx_status gbx_get_work(gbx_context* ctx, double* volume_evals, double* 
  * roofline accounting; no counterpart in the reference. */
 GBX_API gbx_status gbx_get_chain_work(gbx_context* ctx, double* list_evals, double* derivative_evals);
 
-/* GBSW forces: the integral pass writes one 16-byte record per (point,
- * in-shell atom) for the chain rule, so that the chain rule does not re-walk
- * every point's cell list.  Each warp (atom x quadrature chunk) owns per_warp
- * records.  per_warp < 0: automatic (the default; first half a warp's points,
+/* GBSW forces: the integral pass writes one 16-byte record (q, V, mask of
+ * the shaping list entries) per quadrature point that an atom other than its
+ * own shapes, so that the chain rule visits only those entries instead of
+ * re-walking every point's cell list.  Each warp (atom x quadrature chunk) owns per_warp records.  per_warp < 0: automatic (the default; first half a warp's points,
  * then 1.125x the largest need seen), 0: no records (the chain rule walks the
  * lists), > 0: that fixed size.  A warp whose records do not fit walks its
  * lists instead, with bit-identical results, so the size only affects speed.

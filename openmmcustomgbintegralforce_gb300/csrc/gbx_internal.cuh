@@ -128,9 +128,9 @@ struct Context {
   unsigned* d_status = nullptr;
   unsigned long long* d_work = nullptr;  // [4] evaluation counters
 
-  // GBSW chain-rule records (e, i, q, V u_k'/u_k), e = table entry of atom k,
-  // written by the integral pass: warp w (atom, quadrature chunk) owns
-  // records [w R, (w + 1) R)
+  // GBSW chain-rule records (q, V, shaping-entry mask) of the points an atom
+  // other than i shapes, written by the integral pass: warp w (atom,
+  // quadrature chunk) owns records [w R, (w + 1) R)
   bool records = false;          // this call writes and reads records
   bool srec_auto = true;         // size R from the largest need seen
   int4* d_srec = nullptr;

@@ -325,18 +325,16 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
 }
 
 // ---------------------------------------------------------------------------
-// GBSW integral pass that also records the chain rule's work.  For each point
-// with V > 0 it writes one record (e, i, q, V u_k'/u_k) per in-shell atom
-// k != i: everything of dV/dx_k that does not depend on the Born radii.  The
-// chain rule then reads these records instead of re-walking every point's
-// list with most lanes of the warp idle.  Warp w owns records
-// [w R, (w + 1) R), filled in the order points finish; count[w] = records
-// written, or -1 - needed when they did not fit (the chain rule walks that
-// warp's lists instead).  Records are stored evict-first: they are read once,
-// and the lookup table must stay in L2.
+// GBSW integral pass that also records which points the chain rule needs:
+// (q, V, mask) for every point with V > 0 shaped by an atom other than i,
+// bit l of mask set for each such in-shell list entry l.  The chain rule
+// then visits only those entries, with lanes spread over them.  Warp w owns
+// records [w R, (w + 1) R), filled in the order points finish; count[w] =
+// points recorded, or -1 - needed when they did not fit or a list was longer
+// than 64 (the chain rule walks that warp's lists instead).  Records are
+// stored evict-first: they are read once, and the lookup table must stay in
+// L2.
 // ---------------------------------------------------------------------------
-constexpr int kKeep = 4;  // in-shell atoms remembered from the walk
-
 struct ShellSink {
   int4* rec;
   int* count;          // [warps]
@@ -356,31 +354,6 @@ __device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const i
   return a.x == xi.x && a.y == xi.y && a.z == xi.z && __ldg(index + l) == i;
 }
 
-// Writes the point's records to dst[0..nrec): (table entry position, i, q,
-// V u'/u) -- the chain rule reads the atom's index and position from the
-// entry, so nothing here waits on a load.  keep[u * kWarp] holds (list
-// position, dr) of the lane's in-shell entry u, u < kKeep.
-__device__ __forceinline__ void emit_point_kept(int4* dst, const ModelConst& m, const Entries& tab, int s, int cnt,
-                                                int i, int q, const float4 xi, const float4 v, float V, int nrec,
-                                                const float2* keep) {
-  if (nrec <= kKeep) {
-    for (int u = 0; u < nrec; ++u) {
-      const float2 e = keep[u * kWarp];
-      __stcs(dst + u, make_int4(s + __float_as_int(e.x), i, q, __float_as_int(shell_g(m, V, e.y))));
-    }
-    return;
-  }
-  int t = 0;
-  for (int l = 0; l < cnt && t < nrec; ++l) {
-    const float4 a = __ldg(tab.e + s + l);
-    const float3 d = delta(a, xi, v);
-    const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-    const float lo = a.w - m.sw, hi = a.w + m.sw;
-    if (r2 > lo * lo && r2 < hi * hi && !is_self(a, xi, tab.index + s, l, i))
-      __stcs(dst + t++, make_int4(s + l, i, q, __float_as_int(shell_g(m, V, r2 * rsqrtf(r2) - a.w))));
-  }
-}
-
 // GBSW integrals with lanes refilled from a queue.  A warp classifies a
 // stage of kStage points at once (empty cell: V = 1; buried cell: V = 0) and
 // queues the points that have a list; then every lane evaluates one list
@@ -388,8 +361,7 @@ __device__ __forceinline__ void emit_point_kept(int4* dst, const ModelConst& m, 
 // finished, so a long list keeps one lane busy instead of the whole warp
 // waiting on it.  The walk per point is the sequential one of gbsw_volume
 // (same order, same early exit).  J is summed in an order fixed by the input
-// alone, so runs are bit-reproducible.  With EMIT the finished points write
-// their chain records (see integral records above).
+// alone, so runs are bit-reproducible.
 constexpr int kStage = 256;
 
 template <class Q, bool EMIT>
@@ -397,117 +369,120 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
                                                                  Quad quad, ModelConst m, int chunk, int n_chunks,
                                                                  float* __restrict__ Jpart, ShellSink sink) {
   __shared__ int3 s_queue[kThreads / kWarp][kStage];  // (q, list start, list length)
-  __shared__ float2 s_keep[kThreads / kWarp][EMIT ? kKeep * kWarp : 1];
   __shared__ int s_fill[kThreads / kWarp];
+  __shared__ int s_long[kThreads / kWarp];  // a shaping entry beyond list position 63
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
   const unsigned lt = (1u << lane) - 1u;
-  int fill = 0;  // records this warp produced (may exceed R)
-  if (lane == 0) s_fill[wib] = 0;
+  if (lane == 0) {
+    s_fill[wib] = 0;
+    s_long[wib] = 0;
+  }
   __syncwarp();
-  if (warp < n * n_chunks) {
-    int3* queue = s_queue[wib];
-    float2* keep = s_keep[wib] + (EMIT ? lane : 0);
-    const int i = warp % n, c = warp / n;
-    int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
-    const float4 xi = pos[i];
-    Q query;
-    query.init(*tab.geom, xi, quad.qoff);
-    const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
-    float J4 = 0.0f, J7 = 0.0f;
-    for (int base = q0; base < q1; base += kStage) {
-      int nq = 0;  // warp-uniform queue length
+  if (warp >= n * n_chunks) return;
+  int3* queue = s_queue[wib];
+  const int i = warp % n, c = warp / n;
+  int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
+  const float4 xi = pos[i];
+  Q query;
+  query.init(*tab.geom, xi, quad.qoff);
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  float J4 = 0.0f, J7 = 0.0f;
+  for (int base = q0; base < q1; base += kStage) {
+    int nq = 0;  // warp-uniform queue length
 #pragma unroll 4
-      for (int k = 0; k < kStage / kWarp; ++k) {
-        const int q = base + k * kWarp + lane;
-        int2 cs = make_int2(-1, 0);
-        if (q < q1) {
-          const float4 v = quad.qv[q];
-          const long long cell = query.cell(xi, v, q);
-          cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
-          if (cs.x == 0) {
-            const float2 w = quad.qw[q];
-            J4 += w.x;
-            J7 += w.y;
-          }
-        }
-        const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
-        if (cs.x > 0) queue[nq + __popc(qm & lt)] = make_int3(q, cs.y, cs.x);
-        nq += __popc(qm);
-      }
-      __syncwarp();
-      int head = 0, q = 0, s = 0, cnt = 0, l = 0, nrec = 0;
-      bool has = false;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      float2 w = make_float2(0.f, 0.f);
-      float V = 1.0f;
-      while (true) {
-        const unsigned need = __ballot_sync(0xffffffffu, !has);
-        if (!has) {
-          const int idx = head + __popc(need & lt);
-          if (idx < nq) {
-            const int3 e = queue[idx];
-            q = e.x;
-            s = e.y;
-            cnt = e.z;
-            l = 0;
-            nrec = 0;
-            V = 1.0f;
-            has = true;
-            v = quad.qv[q];
-            w = quad.qw[q];
-          }
-        }
-        head += __popc(need);
-        if (__ballot_sync(0xffffffffu, has) == 0u) break;
-        bool fin = false;
-        if (has) {
-          const float4 a = __ldg(tab.e + s + l);
-          const float3 d = delta(a, xi, v);
-          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-          const float lo = a.w - m.sw, hi = a.w + m.sw;
-          if (r2 <= lo * lo) {
-            V = 0.0f;
-            fin = true;
-          } else {
-            if (r2 < hi * hi) {
-              const float dr = r2 * rsqrtf(r2) - a.w;
-              V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-              if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
-                if (nrec < kKeep) keep[nrec * kWarp] = make_float2(__int_as_float(l), dr);
-                ++nrec;
-              }
-            }
-            fin = ++l == cnt;
-          }
-        }
-        if (fin) {
-          J4 = fmaf(w.x, V, J4);
-          J7 = fmaf(w.y, V, J7);
-          has = false;
-        }
-        if (EMIT && fin && V != 0.0f && nrec > 0) {
-          // slots in any order: the chain rule's sums do not depend on it
-          const int slot = atomicAdd(&s_fill[wib], nrec);
-          if (slot + nrec <= sink.R) emit_point_kept(region + slot, m, tab, s, cnt, i, q, xi, v, V, nrec, keep);
+    for (int k = 0; k < kStage / kWarp; ++k) {
+      const int q = base + k * kWarp + lane;
+      int2 cs = make_int2(-1, 0);
+      if (q < q1) {
+        const float4 v = quad.qv[q];
+        const long long cell = query.cell(xi, v, q);
+        cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
+        if (cs.x == 0) {
+          const float2 w = quad.qw[q];
+          J4 += w.x;
+          J7 += w.y;
         }
       }
-      __syncwarp();  // the next stage rewrites the queue
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      J4 += __shfl_xor_sync(0xffffffffu, J4, off);
-      J7 += __shfl_xor_sync(0xffffffffu, J7, off);
+      const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
+      if (cs.x > 0) queue[nq + __popc(qm & lt)] = make_int3(q, cs.y, cs.x);
+      nq += __popc(qm);
     }
     __syncwarp();
-    fill = s_fill[wib];
-    if (lane == 0) {
-      Jpart[(size_t)c * n + i] = J4;
-      Jpart[((size_t)n_chunks + c) * n + i] = J7;
-      if (EMIT) sink.count[warp] = fill <= sink.R ? fill : -1 - fill;
+    int head = 0, q = 0, s = 0, cnt = 0, l = 0;
+    bool has = false;
+    unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 w = make_float2(0.f, 0.f);
+    float V = 1.0f;
+    while (true) {
+      const unsigned need = __ballot_sync(0xffffffffu, !has);
+      if (!has) {
+        const int idx = head + __popc(need & lt);
+        if (idx < nq) {
+          const int3 e = queue[idx];
+          q = e.x;
+          s = e.y;
+          cnt = e.z;
+          l = 0;
+          shaped = 0;
+          V = 1.0f;
+          has = true;
+          v = quad.qv[q];
+          w = quad.qw[q];
+        }
+      }
+      head += __popc(need);
+      if (__ballot_sync(0xffffffffu, has) == 0u) break;
+      bool fin = false;
+      if (has) {
+        const float4 a = __ldg(tab.e + s + l);
+        const float3 d = delta(a, xi, v);
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        const float lo = a.w - m.sw, hi = a.w + m.sw;
+        if (r2 <= lo * lo) {
+          V = 0.0f;
+          fin = true;
+        } else {
+          if (r2 < hi * hi) {
+            const float dr = r2 * rsqrtf(r2) - a.w;
+            V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+            if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
+              if (l < 64) shaped |= 1ull << l;
+              else s_long[wib] = 1;
+            }
+          }
+          fin = ++l == cnt;
+        }
+      }
+      if (fin) {
+        J4 = fmaf(w.x, V, J4);
+        J7 = fmaf(w.y, V, J7);
+        has = false;
+        if (EMIT && shaped != 0ull && V != 0.0f) {
+          const int slot = atomicAdd(&s_fill[wib], 1);  // any order: the chain rule's sums do not depend on it
+          if (slot < sink.R)
+            __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
+        }
+      }
+    }
+    __syncwarp();  // the next stage rewrites the queue
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    J4 += __shfl_xor_sync(0xffffffffu, J4, off);
+    J7 += __shfl_xor_sync(0xffffffffu, J7, off);
+  }
+  __syncwarp();
+  const int fill = s_fill[wib];
+  if (lane == 0) {
+    Jpart[(size_t)c * n + i] = J4;
+    Jpart[((size_t)n_chunks + c) * n + i] = J7;
+    if (EMIT) {
+      sink.count[warp] = fill <= sink.R && !s_long[wib] ? fill : -1 - fill;
+      if (fill > 0) atomicMax(sink.max_seen, (unsigned)fill);
     }
   }
-  if (EMIT && lane == 0 && fill > 0) atomicMax(sink.max_seen, (unsigned)fill);
 }
 
 // ---------------------------------------------------------------------------
@@ -529,7 +504,7 @@ struct ChainOut {
 
 // Records of the emitting integral pass (rec == nullptr: none this call).
 struct ChainRecords {
-  const int4* rec;
+  const int4* rec;  // (q, V, mask low, mask high) per recorded point
   const int* count;
   int R;
 };
@@ -555,28 +530,66 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   // F_i as fixed-point integers: every contribution is rounded on its own, so
   // the record and the list-walk paths give the same bits
   long long fix = 0, fiy = 0, fiz = 0;
-  const int nrec = rr.count ? rr.count[warp] : -1;
-  if (MODEL == GBX_MODEL_GBSW && !ADJ && nrec >= 0) {
+  Q query;
+  query.init(*tab.geom, xi, quad.qoff);
+  const int npts = rr.count ? rr.count[warp] : -1;
+  if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
+    // recorded points, 32 at a time; lanes over their shaping entries
     const int4* region = rr.rec + (size_t)warp * rr.R;
-    for (int t = lane; t < nrec; t += kWarp) {
-      const int4 rc = __ldcs(region + t);
-      const float4 a = __ldg(tab.e + rc.x), v = quad.qv[rc.z];
-      const int k = __ldg(tab.index + rc.x);
-      const float2 w = quad.qw[rc.z];
-      const float cq = fmaf(de.x, w.x, de.y * w.y);
-      const float3 d = delta(a, xi, v);
-      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-      const float gs = cq * __int_as_float(rc.w) * rsqrtf(r2);
-      const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
-      const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
-      if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2) push_force(out, k, gx, gy, gz);
-      fix += float_to_fixed(gx);
-      fiy += float_to_fixed(gy);
-      fiz += float_to_fixed(gz);
+    for (int b = 0; b < npts; b += kWarp) {
+      unsigned mlo = 0u, mhi = 0u;
+      int st = 0;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      float V = 0.0f, cq = 0.0f;
+      if (b + lane < npts) {
+        const int4 pr = __ldcs(region + b + lane);
+        V = __int_as_float(pr.y);
+        mlo = (unsigned)pr.z;
+        mhi = (unsigned)pr.w;
+        v = quad.qv[pr.x];
+        const float2 w = quad.qw[pr.x];
+        cq = fmaf(de.x, w.x, de.y * w.y);
+        st = __ldg(tab.cell + query.cell(xi, v, pr.x)).y;  // a recorded point has a list
+      }
+      const int len = __popc(mlo) + __popc(mhi);
+      int incl = len;
+      for (int off = 1; off < kWarp; off <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += u;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, kWarp - 1);
+      for (int r = 0; r < total; r += kWarp) {
+        const int p = r + lane;
+        int o = 0;  // owner: the points whose entries end at or before p
+        for (int step = 16; step > 0; step >>= 1)
+          if (__shfl_sync(0xffffffffu, incl, o + step - 1) <= p) o += step;
+        const int oend = __shfl_sync(0xffffffffu, incl, o), olen = __shfl_sync(0xffffffffu, len, o);
+        const unsigned olo = __shfl_sync(0xffffffffu, mlo, o), ohi = __shfl_sync(0xffffffffu, mhi, o);
+        const int ost = __shfl_sync(0xffffffffu, st, o);
+        const float4 ov = make_float4(__shfl_sync(0xffffffffu, v.x, o), __shfl_sync(0xffffffffu, v.y, o),
+                                      __shfl_sync(0xffffffffu, v.z, o), 0.0f);
+        const float oV = __shfl_sync(0xffffffffu, V, o), ocq = __shfl_sync(0xffffffffu, cq, o);
+        if (p >= total) continue;
+        const int nth = p - (oend - olen);  // nth shaping entry of the owner
+        const int nlo = __popc(olo);
+        const int l = nth < nlo ? (int)__fns(olo, 0, nth + 1) : 32 + (int)__fns(ohi, 0, nth - nlo + 1);
+        const int e = ost + l;
+        const float4 a = __ldg(tab.e + e);
+        const float3 d = delta(a, xi, ov);
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        // the same expressions as the list walk below
+        const float g = shell_g(m, oV, r2 * rsqrtf(r2) - a.w);
+        const float gs = ocq * g * rsqrtf(r2);
+        const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
+        const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+        if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2)
+          push_force(out, __ldg(tab.index + e), gx, gy, gz);
+        fix += float_to_fixed(gx);
+        fiy += float_to_fixed(gy);
+        fiz += float_to_fixed(gz);
+      }
     }
   } else {
-    Q query;
-    query.init(*tab.geom, xi, quad.qoff);
     const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
     for (int q = q0 + lane; q < q1; q += kWarp) {
       const float4 v = quad.qv[q];

@@ -49,8 +49,11 @@ def test_records_match_list_walk_and_oracle(glob, model):
     (walk, _), info = run(g, model, 0)
     assert info["written"] == -1
     (auto1, auto2), info = run(g, model, -1)
-    assert info["written"] > 0 and info["overflowed"] == 0
-    assert info["max_need"] <= info["per_warp"]
+    assert info["written"] > 0 and info["max_need"] <= info["per_warp"]
+    # the reference table's uncapped lists can exceed the 64-entry record
+    # mask; those warps walk their lists
+    if not model.reference_table:
+        assert info["overflowed"] == 0
     # records and list walk round every contribution the same way: same bits
     assert same(auto1, walk) and same(auto2, walk)
     ref = O.Oracle(model).energy_forces(g.positions, g.charge, g.radius)
