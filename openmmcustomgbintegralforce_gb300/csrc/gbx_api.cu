@@ -158,7 +158,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_integrals, 2 * (size_t)n));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdB_fx, n));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdJ, n));
-  ctx->energy_parts = gbx::pair_energy_parts(n, gbx::pair_segments(n));
+  ctx->energy_parts = gbx::pair_sym_parts(n);
   GBX_TRY(dalloc(ctx, &ctx->d_energy_part, ctx->energy_parts));
   GBX_TRY(dalloc(ctx, &ctx->d_force_fx, 3 * (size_t)n));
   GBX_TRY(dalloc(ctx, &ctx->d_energy, 1));

@@ -188,6 +188,7 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
 int pair_energy_parts(int n, int segments);
+int pair_sym_parts(int n);
 int pair_segments(int n);
 ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);

@@ -97,7 +97,15 @@ __global__ void __launch_bounds__(kRedThreads) energy_reduce_kernel(const double
                                                                     double* __restrict__ alpha_grad) {
   __shared__ double s[3][kRedThreads];
   double e = 0, a0 = 0, a1 = 0;
-  for (int k = threadIdx.x; k < nparts; k += kRedThreads) e += parts[k];
+  {
+    // four independent chains (loads in flight), combined in a fixed order
+    double e4[4] = {0, 0, 0, 0};
+    int k = threadIdx.x;
+    for (; k + 3 * kRedThreads < nparts; k += 4 * kRedThreads)
+      for (int u = 0; u < 4; ++u) e4[u] += parts[k + u * kRedThreads];
+    for (; k < nparts; k += kRedThreads) e4[0] += parts[k];
+    e = (e4[0] + e4[1]) + (e4[2] + e4[3]);
+  }
   if (alpha_terms)
     for (int k = threadIdx.x; k < n; k += kRedThreads) {
       a0 += alpha_terms[2 * k];

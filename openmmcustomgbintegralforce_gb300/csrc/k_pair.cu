@@ -129,7 +129,224 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric scheme (the context path): every unordered pair once.  A warp
+// owns an i-block of 64 atoms (two per lane: 64 b + lane and 64 b + 32 + lane)
+// and a run of 32-atom j-tiles above the block.  A j-tile's atoms and their
+// force / dE/dB accumulators rotate one lane per step through shuffles, so
+// after 32 steps every (i, j) pair of the tile was evaluated once and each
+// lane again holds the complete j-side sums of its own j atom.  Pairs inside
+// an i-block, and the self terms, are done by pair_block_kernel.  Every sum
+// runs in a fixed order; i- and j-side sums are rounded to fixed point once
+// per tile and added as integers.
+// ---------------------------------------------------------------------------
+constexpr int kSymI = 64;       // atoms per i-block
+constexpr int kSymChunk = 32;   // j-tiles per warp unit
+constexpr int kSymThreads = 128;
+
+struct SymArgs {
+  const float4* pos;
+  const float* charge;
+  const float2* born;
+  int n;
+  float pref;
+  float cutoff2;  // <= 0: none
+  unsigned long long* force;
+  int stride;
+  unsigned long long* dEdB;
+  unsigned long long* dEdq;
+  double* energy_part;  // [nblocks * chunks] units, then [nblocks] blocks
+  int nblocks, ntiles, chunks;
+};
+
+struct PAtom {
+  float x, y, z, q, B, invB;
+};
+
+struct PAcc {
+  float fx, fy, fz, db, dq;
+};
+
+__device__ __forceinline__ PAtom load_patom(const SymArgs& a, int k) {
+  PAtom t{0.f, 0.f, 0.f, 0.f, 1.f, 1.f};  // padding atom: no charge
+  if (k < a.n) {
+    const float4 p = a.pos[k];
+    const float2 b = a.born[k];
+    t = PAtom{p.x, p.y, p.z, a.charge[k], b.x, b.y};
+  }
+  return t;
+}
+
+// One pair.  kDi = -log2(e) / (4 B_i), kBi = 1 / (4 B_i), pqi = pref q_i.
+// Adds dG/dx_i to ai (force on i: g d, d = x_j - x_i) and dG/dB_i / (-1/2)
+// to ai.db; with SYM also the j side to aj.
+template <bool SYM, bool CUTOFF, bool ADJ>
+__device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, float kBi, const PAtom& J, float kBj,
+                                       float pref, float cutoff2, PAcc& ai, PAcc& aj, float& esum) {
+  const float dx = J.x - I.x, dy = J.y - I.y, dz = J.z - I.z;
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  if (CUTOFF && r2 > cutoff2) return;
+  const float ex = exp2f(r2 * (kDi * J.invB));  // e^-D, D = r^2 / (4 B_i B_j)
+  const float invf = rsqrtf(fmaf(I.B * J.B, ex, r2));
+  const float e = pqi * J.q * invf;
+  esum += e;
+  const float c = e * invf * invf;  // pref q_i q_j / f^3
+  const float g = c * fmaf(0.25f, ex, -1.0f);
+  ai.fx = fmaf(g, dx, ai.fx);
+  ai.fy = fmaf(g, dy, ai.fy);
+  ai.fz = fmaf(g, dz, ai.fz);
+  const float cex = c * ex;
+  ai.db = fmaf(cex, fmaf(r2, kBi, J.B), ai.db);
+  if (ADJ) ai.dq = fmaf(pref * J.q, invf, ai.dq);
+  if (SYM) {
+    aj.fx = fmaf(-g, dx, aj.fx);
+    aj.fy = fmaf(-g, dy, aj.fy);
+    aj.fz = fmaf(-g, dz, aj.fz);
+    aj.db = fmaf(cex, fmaf(r2, kBj, I.B), aj.db);
+    if (ADJ) aj.dq = fmaf(pref * I.q, invf, aj.dq);
+  }
+}
+
+struct PFixed {
+  long long fx = 0, fy = 0, fz = 0, db = 0, dq = 0;
+  __device__ __forceinline__ void add(const PAcc& v) {
+    fx += float_to_fixed(v.fx);
+    fy += float_to_fixed(v.fy);
+    fz += float_to_fixed(v.fz);
+    db += float_to_fixed(-0.5f * v.db);
+    dq += float_to_fixed(v.dq);
+  }
+};
+
+template <bool ADJ>
+__device__ __forceinline__ void push_atom(const SymArgs& a, int k, const PFixed& f) {
+  if (k >= a.n) return;
+  atomicAdd(&a.force[k], (unsigned long long)f.fx);
+  atomicAdd(&a.force[k + a.stride], (unsigned long long)f.fy);
+  atomicAdd(&a.force[k + 2 * a.stride], (unsigned long long)f.fz);
+  atomicAdd(&a.dEdB[k], (unsigned long long)f.db);
+  if (ADJ) atomicAdd(&a.dEdq[k], (unsigned long long)f.dq);
+}
+
+__device__ __forceinline__ void rotate(PAtom& J, PAcc& aj, int src, bool adj) {
+  J.x = __shfl_sync(0xffffffffu, J.x, src);
+  J.y = __shfl_sync(0xffffffffu, J.y, src);
+  J.z = __shfl_sync(0xffffffffu, J.z, src);
+  J.q = __shfl_sync(0xffffffffu, J.q, src);
+  J.B = __shfl_sync(0xffffffffu, J.B, src);
+  J.invB = __shfl_sync(0xffffffffu, J.invB, src);
+  aj.fx = __shfl_sync(0xffffffffu, aj.fx, src);
+  aj.fy = __shfl_sync(0xffffffffu, aj.fy, src);
+  aj.fz = __shfl_sync(0xffffffffu, aj.fz, src);
+  aj.db = __shfl_sync(0xffffffffu, aj.db, src);
+  if (adj) aj.dq = __shfl_sync(0xffffffffu, aj.dq, src);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+constexpr float kLog2e = 1.4426950408889634f;
+
+template <bool CUTOFF, bool ADJ>
+__global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
+  const int unit = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (unit >= a.nblocks * a.chunks) return;
+  const int b = unit / a.chunks, ch = unit % a.chunks;
+  const int jt0 = 2 * b + 2 + ch * kSymChunk;
+  const int jt1 = min(a.ntiles, jt0 + kSymChunk);
+  double E = 0.0;
+  if (jt0 < jt1) {
+    const PAtom I0 = load_patom(a, kSymI * b + lane), I1 = load_patom(a, kSymI * b + kWarp + lane);
+    const float pq0 = a.pref * I0.q, pq1 = a.pref * I1.q;
+    const float kD0 = -0.25f * kLog2e * I0.invB, kD1 = -0.25f * kLog2e * I1.invB;
+    const float kB0 = 0.25f * I0.invB, kB1 = 0.25f * I1.invB;
+    const int src = (lane + 1) % kWarp;
+    PFixed s0, s1;
+    for (int jt = jt0; jt < jt1; ++jt) {
+      PAtom J = load_patom(a, kWarp * jt + lane);
+      PAcc a0{0.f, 0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f, 0.f}, aj{0.f, 0.f, 0.f, 0.f, 0.f};
+      float et = 0.0f;
+#pragma unroll 2
+      for (int t = 0; t < kWarp; ++t) {
+        const float kBj = 0.25f * J.invB;
+        gb_pair<true, CUTOFF, ADJ>(I0, pq0, kD0, kB0, J, kBj, a.pref, a.cutoff2, a0, aj, et);
+        gb_pair<true, CUTOFF, ADJ>(I1, pq1, kD1, kB1, J, kBj, a.pref, a.cutoff2, a1, aj, et);
+        rotate(J, aj, src, ADJ);  // after 32 steps every j is back in its own lane
+      }
+      PFixed sj;
+      sj.add(aj);
+      push_atom<ADJ>(a, kWarp * jt + lane, sj);
+      s0.add(a0);
+      s1.add(a1);
+      E += (double)et;
+    }
+    push_atom<ADJ>(a, kSymI * b + lane, s0);
+    push_atom<ADJ>(a, kSymI * b + kWarp + lane, s1);
+  }
+  E = warp_sum(E);
+  if (lane == 0) a.energy_part[unit] = E;
+}
+
+// Pairs inside each 64-atom i-block (i side only, each ordered pair once)
+// and the self terms 1/2 pref q_i^2 / B_i.
+template <bool CUTOFF, bool ADJ>
+__global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
+  const int b = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (b >= a.nblocks) return;
+  const int i0 = kSymI * b + lane, i1 = i0 + kWarp;
+  const PAtom I0 = load_patom(a, i0), I1 = load_patom(a, i1);
+  const float pq0 = a.pref * I0.q, pq1 = a.pref * I1.q;
+  const float kD0 = -0.25f * kLog2e * I0.invB, kD1 = -0.25f * kLog2e * I1.invB;
+  const float kB0 = 0.25f * I0.invB, kB1 = 0.25f * I1.invB;
+  PAcc a0{0.f, 0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f, 0.f}, dummy{0.f, 0.f, 0.f, 0.f, 0.f};
+  float e0 = 0.0f, e1 = 0.0f;
+  for (int h = 0; h < 2; ++h)
+    for (int t = 0; t < kWarp; ++t) {
+      const PAtom& S = h ? I1 : I0;
+      const PAtom J{__shfl_sync(0xffffffffu, S.x, t), __shfl_sync(0xffffffffu, S.y, t),
+                    __shfl_sync(0xffffffffu, S.z, t), __shfl_sync(0xffffffffu, S.q, t),
+                    __shfl_sync(0xffffffffu, S.B, t), __shfl_sync(0xffffffffu, S.invB, t)};
+      const int j = kSymI * b + h * kWarp + t;
+      if (j != i0) gb_pair<false, CUTOFF, ADJ>(I0, pq0, kD0, kB0, J, 0.f, a.pref, a.cutoff2, a0, dummy, e0);
+      if (j != i1) gb_pair<false, CUTOFF, ADJ>(I1, pq1, kD1, kB1, J, 0.f, a.pref, a.cutoff2, a1, dummy, e1);
+    }
+  PFixed s0, s1;
+  s0.add(a0);
+  s1.add(a1);
+  // self term: 1/2 pref q^2 / B, dE/dB = -1/2 pref q^2 / B^2, dE/dq = pref q / B
+  s0.db += float_to_fixed(-0.5f * pq0 * I0.q * I0.invB * I0.invB);
+  s1.db += float_to_fixed(-0.5f * pq1 * I1.q * I1.invB * I1.invB);
+  if (ADJ) {
+    s0.dq += float_to_fixed(pq0 * I0.invB);
+    s1.dq += float_to_fixed(pq1 * I1.invB);
+  }
+  push_atom<ADJ>(a, i0, s0);
+  push_atom<ADJ>(a, i1, s1);
+  double E = 0.5 * ((double)e0 + (double)e1);  // each pair visited from both ends
+  E += 0.5 * ((double)pq0 * I0.q * I0.invB + (double)pq1 * I1.q * I1.invB);
+  E = warp_sum(E);
+  if (lane == 0) a.energy_part[a.nblocks * a.chunks + b] = E;
+}
+
+SymArgs sym_args(int n) {
+  SymArgs a{};
+  a.n = n;
+  a.nblocks = (n + kSymI - 1) / kSymI;
+  a.ntiles = (n + kWarp - 1) / kWarp;
+  a.chunks = (a.ntiles + kSymChunk - 1) / kSymChunk;
+  return a;
+}
+
 }  // namespace
+
+int pair_sym_parts(int n) {
+  const SymArgs a = sym_args(n);
+  return a.nblocks * a.chunks + a.nblocks;
+}
 
 int pair_energy_parts(int n, int segments) { return ((n + kPairThreads - 1) / kPairThreads) * segments; }
 
@@ -169,26 +386,36 @@ cudaError_t launch_pair_raw(const float4* pos, const float* charge, const float2
 }
 
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint) {
-  PairArgs a;
+  SymArgs a = sym_args(ctx->n);
   a.pos = pos;
   a.charge = ctx->d_charge;
   a.born = reinterpret_cast<const float2*>(ctx->d_bornf);
-  a.n = ctx->n;
-  a.segments = pair_segments(ctx->n);
   a.pref = (float)ctx->cfg.prefactor;
   a.cutoff2 = ctx->cfg.cutoff > 0 ? (float)(ctx->cfg.cutoff * ctx->cfg.cutoff) : 0.0f;
   a.force = force;
   a.stride = stride;
   a.dEdB = ctx->d_dEdB_fx;
-  a.energy_part = ctx->d_energy_part;
   a.dEdq = ctx->d_dEdq_fx;
-  dim3 grid((ctx->n + kPairThreads - 1) / kPairThreads, a.segments);
+  a.energy_part = ctx->d_energy_part;
+  const int wpb = kSymThreads / kWarp;
+  const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
+  cudaStream_t st = ctx->stream;
   if (a.cutoff2 > 0) {
-    if (adjoint) pair_kernel<true, true><<<grid, kPairThreads, 0, ctx->stream>>>(a);
-    else pair_kernel<true, false><<<grid, kPairThreads, 0, ctx->stream>>>(a);
+    if (adjoint) {
+      pair_sym_kernel<true, true><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<true, true><<<gb, kSymThreads, 0, st>>>(a);
+    } else {
+      pair_sym_kernel<true, false><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<true, false><<<gb, kSymThreads, 0, st>>>(a);
+    }
   } else {
-    if (adjoint) pair_kernel<false, true><<<grid, kPairThreads, 0, ctx->stream>>>(a);
-    else pair_kernel<false, false><<<grid, kPairThreads, 0, ctx->stream>>>(a);
+    if (adjoint) {
+      pair_sym_kernel<false, true><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<false, true><<<gb, kSymThreads, 0, st>>>(a);
+    } else {
+      pair_sym_kernel<false, false><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<false, false><<<gb, kSymThreads, 0, st>>>(a);
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
