@@ -272,6 +272,7 @@ def main():
     barrier(world)
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
+    launches0 = ctx.launches()
     with torch.cuda.stream(stream):
         for k in range(args.steps):
             flush.fill_(float(k))
@@ -281,6 +282,7 @@ def main():
     torch.cuda.synchronize()
     barrier(world)
     wall = time.perf_counter() - wall0
+    launches = ctx.launches() - launches0
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = allmax(world, float(np.mean(step_ms)))
@@ -374,7 +376,7 @@ def main():
                 "config": {"workload": args.workload, "desc": w["desc"], "atoms": n,
                            "quadrature_points": model.n_quad, "l2": "flushed (256 MiB write) between steps",
                            "parallelism": "replicas" if world > 1 else "single"},
-                "gpu_launches": 14, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "err_vs_fp64": err, "clocks": clk, "wall_s": wall}
         print(json.dumps(line))
 

@@ -179,6 +179,10 @@ GBX_API gbx_status gbx_get_work(gbx_context* ctx, double* volume_evals, double* 
  * roofline accounting; no counterpart in the reference. */
 GBX_API gbx_status gbx_get_chain_work(gbx_context* ctx, double* list_evals, double* derivative_evals);
 
+/* Kernels this context has launched so far (all entry points).  No
+ * counterpart in the reference. */
+GBX_API gbx_status gbx_get_launches(gbx_context* ctx, long long* launches);
+
 /* GBSW forces: the integral pass writes one 16-byte record (q, V, mask of
  * the shaping list entries) per quadrature point that an atom other than its
  * own shapes, so that the chain rule visits only those entries instead of

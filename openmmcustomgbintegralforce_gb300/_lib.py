@@ -27,7 +27,7 @@ EXPORTED = (
     "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
     "gbx_adjoint_host", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
-    "gbx_get_chain_records", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
+    "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
@@ -133,6 +133,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_get_chain_work.argtypes = [vp, vp, vp]
     L.gbx_set_chain_records.argtypes = [vp, ci]
     L.gbx_get_chain_records.argtypes = [vp, vp, vp, vp, vp]
+    L.gbx_get_launches.argtypes = [vp, vp]
     L.gbx_set_timing.argtypes = [vp, ci]
     L.gbx_get_stage_times.argtypes = [vp, vp, ci, vp]
     L.gbx_pair_noalloc.argtypes = [vp, vp, vp, ci, cd, cd, vp, ci, vp, vp, vp]
@@ -253,6 +254,11 @@ class Context:
         self._check(self.lib.gbx_get_chain_records(self.h, ctypes.byref(w), ctypes.byref(mx), ctypes.byref(R),
                                                    ctypes.byref(over)))
         return {"written": w.value, "max_need": mx.value, "per_warp": R.value, "overflowed": over.value}
+
+    def launches(self) -> int:
+        v = ctypes.c_longlong()
+        self._check(self.lib.gbx_get_launches(self.h, ctypes.byref(v)))
+        return v.value
 
     def set_timing(self, enable: bool = True):
         self._check(self.lib.gbx_set_timing(self.h, 1 if enable else 0))

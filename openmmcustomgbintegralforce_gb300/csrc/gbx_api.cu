@@ -158,8 +158,9 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_integrals, 2 * (size_t)n));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdB_fx, n));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdJ, n));
-  ctx->energy_parts = gbx::pair_sym_parts(n);
-  GBX_TRY(dalloc(ctx, &ctx->d_energy_part, ctx->energy_parts));
+  ctx->energy_parts = 0;  // the pair kernels add the energy to d_energy_fx
+  GBX_TRY(dalloc(ctx, &ctx->d_energy_part, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_energy_fx, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_force_fx, 3 * (size_t)n));
   GBX_TRY(dalloc(ctx, &ctx->d_energy, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdR_fx, n));
@@ -569,7 +570,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax};
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)
@@ -876,6 +877,13 @@ gbx_status gbx_get_chain_records(gbx_context* handle, long long* written, int* m
   if (max_need) *max_need = mx;
   if (per_warp) *per_warp = ctx->srec_R;
   if (overflowed) *overflowed = over;
+  return GBX_OK;
+}
+
+gbx_status gbx_get_launches(gbx_context* handle, long long* launches) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !launches) return GBX_ERR_INVALID_ARGUMENT;
+  *launches = ctx->launches;
   return GBX_OK;
 }
 

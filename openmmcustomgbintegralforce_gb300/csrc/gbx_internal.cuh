@@ -118,8 +118,9 @@ struct Context {
   double* d_integrals = nullptr; // [2n]  I4, I7
   unsigned long long* d_dEdB_fx = nullptr;  // [n] fixed point
   float2* d_dEdJ = nullptr;      // [n]
-  double* d_energy_part = nullptr;  // [max warps]
+  double* d_energy_part = nullptr;  // [energy_parts] per-CTA energy partials
   int energy_parts = 0;
+  unsigned long long* d_energy_fx = nullptr;  // pair energy, fixed point (2^-32)
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]
@@ -142,6 +143,8 @@ struct Context {
   cudaEvent_t srec_ev = nullptr;
   bool srec_pending = false;     // srec_ev recorded and not yet read
   bool have_result = false;
+
+  long long launches = 0;  // kernels this context has launched
 
   // optional per-stage timing (CUDA events on the execute stream)
   bool timing = false;
@@ -188,7 +191,6 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
 int pair_energy_parts(int n, int segments);
-int pair_sym_parts(int n);
 int pair_segments(int n);
 ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);

@@ -92,6 +92,7 @@ constexpr int kRedThreads = 1024;
 
 // One block; fixed reduction shape, so the result is bit-reproducible.
 __global__ void __launch_bounds__(kRedThreads) energy_reduce_kernel(const double* __restrict__ parts, int nparts,
+                                                                    const unsigned long long* __restrict__ energy_fx,
                                                                     double* __restrict__ energy,
                                                                     const double* __restrict__ alpha_terms, int n,
                                                                     double* __restrict__ alpha_grad) {
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kRedThreads) energy_reduce_kernel(const double
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    if (energy) *energy += s[0][0];
+    if (energy) *energy += s[0][0] + (energy_fx ? fixed_to_double(*energy_fx) : 0.0);
     if (alpha_grad) {
       alpha_grad[0] = s[1][0];
       alpha_grad[1] = s[2][0];
@@ -134,6 +135,7 @@ __global__ void __launch_bounds__(kRedThreads) energy_reduce_kernel(const double
 gbx_status launch_stage_positions(Context* ctx, const float4* posq) {
   const int n = ctx->n;
   stage_positions_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(posq, n, ctx->d_wpar, ctx->d_pos);
+  ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("stage launch: ") + cudaGetErrorString(e);
@@ -148,6 +150,7 @@ gbx_status launch_born(Context* ctx) {
       n, ctx->n_chunks, ctx->d_J, ctx->S4, ctx->S7, ctx->C4, ctx->C7, ctx->alpha0, ctx->alpha1, ctx->d_born,
       reinterpret_cast<float2*>(ctx->d_bornf), ctx->d_dBdJ, ctx->d_dBdJ + 2 * (size_t)n, ctx->d_integrals,
       ctx->d_status);
+  ++ctx->launches;
   cudaMemsetAsync(ctx->d_dEdB_fx, 0, sizeof(unsigned long long) * n, ctx->stream);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -162,6 +165,7 @@ gbx_status launch_chain_prep(Context* ctx, bool adjoint) {
   chain_prep_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
       n, ctx->d_dEdB_fx, ctx->d_dBdJ, ctx->d_dBdJ + 2 * (size_t)n, ctx->d_dEdJ,
       adjoint ? ctx->d_dBdJ + 4 * (size_t)n : nullptr);
+  ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("chain prep launch: ") + cudaGetErrorString(e);
@@ -171,9 +175,11 @@ gbx_status launch_chain_prep(Context* ctx, bool adjoint) {
 }
 
 gbx_status launch_energy_reduce(Context* ctx, double* energy, bool adjoint) {
-  energy_reduce_kernel<<<1, kRedThreads, 0, ctx->stream>>>(ctx->d_energy_part, ctx->energy_parts, energy,
+  energy_reduce_kernel<<<1, kRedThreads, 0, ctx->stream>>>(ctx->d_energy_part, ctx->energy_parts, ctx->d_energy_fx,
+                                                           energy,
                                                            adjoint ? ctx->d_dBdJ + 4 * (size_t)ctx->n : nullptr,
                                                            ctx->n, adjoint ? ctx->d_alpha_grad : nullptr);
+  ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("energy reduce launch: ") + cudaGetErrorString(e);

@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
 // per tile and added as integers.
 // ---------------------------------------------------------------------------
 constexpr int kSymI = 64;       // atoms per i-block
-constexpr int kSymChunk = 32;   // j-tiles per warp unit
+constexpr int kSymChunk = 16;   // j-tiles per warp unit
 constexpr int kSymThreads = 128;
 
 struct SymArgs {
@@ -155,7 +155,7 @@ struct SymArgs {
   int stride;
   unsigned long long* dEdB;
   unsigned long long* dEdq;
-  double* energy_part;  // [nblocks * chunks] units, then [nblocks] blocks
+  unsigned long long* energy;  // fixed point (2^-32), summed as integers
   int nblocks, ntiles, chunks;
 };
 
@@ -177,6 +177,21 @@ __device__ __forceinline__ PAtom load_patom(const SymArgs& a, int k) {
   return t;
 }
 
+// Hardware 2^x and 1/sqrt(x) (PTX ex2.approx / rsqrt.approx, relative error
+// below 2^-22; subnormal results and inputs flush to zero, which e^-D and
+// 1/f never need).
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // One pair.  kDi = -log2(e) / (4 B_i), kBi = 1 / (4 B_i), pqi = pref q_i.
 // Adds dG/dx_i to ai (force on i: g d, d = x_j - x_i) and dG/dB_i / (-1/2)
 // to ai.db; with SYM also the j side to aj.
@@ -186,8 +201,8 @@ __device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, fl
   const float dx = J.x - I.x, dy = J.y - I.y, dz = J.z - I.z;
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   if (CUTOFF && r2 > cutoff2) return;
-  const float ex = exp2f(r2 * (kDi * J.invB));  // e^-D, D = r^2 / (4 B_i B_j)
-  const float invf = rsqrtf(fmaf(I.B * J.B, ex, r2));
+  const float ex = ex2_ftz(r2 * (kDi * J.invB));  // e^-D, D = r^2 / (4 B_i B_j)
+  const float invf = rsqrt_ftz(fmaf(I.B * J.B, ex, r2));
   const float e = pqi * J.q * invf;
   esum += e;
   const float c = e * invf * invf;  // pref q_i q_j / f^3
@@ -287,7 +302,7 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
     push_atom<ADJ>(a, kSymI * b + kWarp + lane, s1);
   }
   E = warp_sum(E);
-  if (lane == 0) a.energy_part[unit] = E;
+  if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
 }
 
 // Pairs inside each 64-atom i-block (i side only, each ordered pair once)
@@ -329,7 +344,7 @@ __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
   double E = 0.5 * ((double)e0 + (double)e1);  // each pair visited from both ends
   E += 0.5 * ((double)pq0 * I0.q * I0.invB + (double)pq1 * I1.q * I1.invB);
   E = warp_sum(E);
-  if (lane == 0) a.energy_part[a.nblocks * a.chunks + b] = E;
+  if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
 }
 
 SymArgs sym_args(int n) {
@@ -342,11 +357,6 @@ SymArgs sym_args(int n) {
 }
 
 }  // namespace
-
-int pair_sym_parts(int n) {
-  const SymArgs a = sym_args(n);
-  return a.nblocks * a.chunks + a.nblocks;
-}
 
 int pair_energy_parts(int n, int segments) { return ((n + kPairThreads - 1) / kPairThreads) * segments; }
 
@@ -396,25 +406,34 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
   a.stride = stride;
   a.dEdB = ctx->d_dEdB_fx;
   a.dEdq = ctx->d_dEdq_fx;
-  a.energy_part = ctx->d_energy_part;
+  a.energy = ctx->d_energy_fx;
   const int wpb = kSymThreads / kWarp;
   const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
   cudaStream_t st = ctx->stream;
+  cudaMemsetAsync(ctx->d_energy_fx, 0, sizeof(unsigned long long), st);
   if (a.cutoff2 > 0) {
     if (adjoint) {
       pair_sym_kernel<true, true><<<gu, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
       pair_block_kernel<true, true><<<gb, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
     } else {
       pair_sym_kernel<true, false><<<gu, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
       pair_block_kernel<true, false><<<gb, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
     }
   } else {
     if (adjoint) {
       pair_sym_kernel<false, true><<<gu, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
       pair_block_kernel<false, true><<<gb, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
     } else {
       pair_sym_kernel<false, false><<<gu, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
       pair_block_kernel<false, false><<<gb, kSymThreads, 0, st>>>(a);
+      ++ctx->launches;
     }
   }
   cudaError_t e = cudaGetLastError();

@@ -373,6 +373,7 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
   table_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->d_radius, ctx->n, c.table_mode, c.grid_length,
                                                 c.table_buffer, c.switch_width, c.box[0], c.box[1], c.box[2],
                                                 ctx->d_geom, ctx->cell_cap, ctx->d_status);
+  ++ctx->launches;
   const long long cells = ctx->cell_cap;
   if (cells == 0) {
     // sizing call: geometry only; the caller reads it back and allocates
@@ -388,9 +389,11 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
   const int threads = 256;
   const int blocks = grid_for((long long)ctx->n * kWarp, threads);
   for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1)
+    if (pass == 1) {
       launch_scan(ctx->d_cell_count, ctx->d_geom, ctx->d_block_sums, ctx->d_cell_start, ctx->d_cell_cursor, cells,
                   ctx->entry_cap, ctx->d_status, st);
+      ctx->launches += 3;  // the scan's three kernels
+    }
     const bool fill = pass == 1;
     switch (c.table_mode) {
       case GBX_TABLE_STANDALONE:
@@ -418,12 +421,15 @@ gbx_status launch_table_build(Context* ctx, const float4* pos) {
                                                                            c.table_buffer, em, cells, ctx->d_status);
         break;
     }
+    ++ctx->launches;
   }
   sort_cells_kernel<<<grid_for(cells, kSortWarps), kSortWarps * kWarp, 0, st>>>(
       ctx->d_cell_count, ctx->d_cell_start, ctx->d_entries, ctx->d_cell2, ctx->d_geom, c.table_cap, cells, ctx->entry_cap,
       ctx->d_status);
+  ++ctx->launches;
   denormalize_kernel<<<grid_for(ctx->entry_cap, 256), 256, 0, st>>>(ctx->d_entries, ctx->d_geom, pos, ctx->d_par,
                                                                     ctx->d_entry4, ctx->d_entry_par, ctx->entry_cap);
+  ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("table build launch: ") + cudaGetErrorString(e);

@@ -193,49 +193,57 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
   if (g.ncell > cell_cap || g.total > entry_cap) return;
   const long long ncell = g.ncell;
   const long long sx = (long long)g.dims[1] * g.dims[2];
-  for (long long c = (long long)blockIdx.x * kSortWarps + wib; c < ncell; c += (long long)gridDim.x * kSortWarps) {
-    const int cnt = count[c];
-    const int s = start[c];
-    if (cnt == 0) {
-      if (lane == 0) cell[c] = make_int2(0, s);
-      continue;
+  const float cmin[3] = {(float)g.min[0], (float)g.min[1], (float)g.min[2]};
+  const float step = (float)g.step[0];
+  // lanes classify 32 consecutive cells (coalesced); the warp then sorts the
+  // listed, unburied ones one at a time
+  for (long long c0 = ((long long)blockIdx.x * kSortWarps + wib) * kWarp; c0 < ncell;
+       c0 += (long long)gridDim.x * kSortWarps * kWarp) {
+    const long long c = c0 + lane;
+    int cnt = 0, s = 0, bur = 0;
+    if (c < ncell) {
+      cnt = count[c];
+      s = start[c];
+      bur = cnt > 0 ? buried[c] : 0;
+      cell[c] = make_int2(bur ? -1 : cnt, s);
+      if (bur) count[c] = -1;
     }
-    if (buried[c]) {
-      if (lane == 0) {
-        count[c] = -1;
-        cell[c] = make_int2(-1, s);
+    unsigned todo = __ballot_sync(0xffffffffu, cnt > 0 && !bur);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const long long cc = c0 + src;
+      const int ccnt = __shfl_sync(0xffffffffu, cnt, src), cs = __shfl_sync(0xffffffffu, s, src);
+      if (ccnt > kSortBuf) {
+        if (lane == 0) atomicOr(status, kStatusSegmentTooLong);
+        continue;
       }
-      continue;
-    }
-    if (lane == 0) cell[c] = make_int2(cnt, s);
-    if (cnt > kSortBuf) {
-      if (lane == 0) atomicOr(status, kStatusSegmentTooLong);
-      continue;
-    }
-    const int cx = (int)(c / sx), cy = (int)((c / g.dims[2]) % g.dims[1]), cz = (int)(c % g.dims[2]);
-    const double ctr[3] = {g.min[0] + (cx + 0.5) * g.step[0], g.min[1] + (cy + 0.5) * g.step[1],
-                           g.min[2] + (cz + 0.5) * g.step[2]};
-    for (int q = lane; q < cnt; q += kWarp) {
-      const float4 e = entry[s + q];
-      s_e[wib][q] = e;
-      s_i[wib][q] = index[s + q];
-      const float dx = (float)((double)e.x - ctr[0]), dy = (float)((double)e.y - ctr[1]),
-                  dz = (float)((double)e.z - ctr[2]);
-      s_k[wib][q] = sqrtf(dx * dx + dy * dy + dz * dz) - (e.w - w);
-    }
-    __syncwarp();
-    for (int q = lane; q < cnt; q += kWarp) {
-      const float kq = s_k[wib][q];
-      const int iq = s_i[wib][q];
-      int r = 0;
-      for (int o = 0; o < cnt; ++o) {
-        const float ko = s_k[wib][o];
-        r += (ko < kq) || (ko == kq && s_i[wib][o] < iq);
+      // key: distance to the cell centre less R' - w (atoms likely to bury
+      // the cell's points first); FP32, any fixed order is exact
+      const int cx = (int)(cc / sx), cy = (int)((cc / g.dims[2]) % g.dims[1]), cz = (int)(cc % g.dims[2]);
+      const float ctr[3] = {cmin[0] + ((float)cx + 0.5f) * step, cmin[1] + ((float)cy + 0.5f) * step,
+                            cmin[2] + ((float)cz + 0.5f) * step};
+      for (int q = lane; q < ccnt; q += kWarp) {
+        const float4 e = entry[cs + q];
+        s_e[wib][q] = e;
+        s_i[wib][q] = index[cs + q];
+        const float dx = e.x - ctr[0], dy = e.y - ctr[1], dz = e.z - ctr[2];
+        s_k[wib][q] = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - (e.w - w);
       }
-      entry[s + r] = s_e[wib][q];
-      index[s + r] = iq;
+      __syncwarp();
+      for (int q = lane; q < ccnt; q += kWarp) {
+        const float kq = s_k[wib][q];
+        const int iq = s_i[wib][q];
+        int r = 0;
+        for (int o = 0; o < ccnt; ++o) {
+          const float ko = s_k[wib][o];
+          r += (ko < kq) || (ko == kq && s_i[wib][o] < iq);
+        }
+        entry[cs + r] = s_e[wib][q];
+        index[cs + r] = iq;
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -246,6 +254,7 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
   const double h = ctx->tight_h;
   tight_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->n, h, ctx->cfg.switch_width, ctx->d_tgeom, ctx->tcell_cap,
                                                 ctx->d_status);
+  ++ctx->launches;
   const long long cells = ctx->tcell_cap;
   if (cells > 0) {
     cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * cells, st);
@@ -258,15 +267,19 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
     long long blocks = ((long long)ctx->n * kWarp + threads - 1) / threads;
     if (blocks > 65535) blocks = 65535;
     tight_members_kernel<false><<<(int)blocks, threads, 0, st>>>(a);
+    ++ctx->launches;
     launch_scan(ctx->d_tcount, ctx->d_tgeom, ctx->d_tblock_sums, ctx->d_tstart, ctx->d_tcursor, cells,
                 ctx->tentry_cap, ctx->d_status, st);
+    ctx->launches += 3;  // the scan's three kernels
     tight_members_kernel<true><<<(int)blocks, threads, 0, st>>>(a);
-    long long sb = (cells + kSortWarps - 1) / kSortWarps;
-    if (sb > 1048576) sb = 1048576;
+    ++ctx->launches;
+    long long sb = (cells + kSortWarps * kWarp - 1) / (kSortWarps * kWarp);
+    if (sb > 152 * 64) sb = 152 * 64;
     tight_sort_kernel<<<(int)sb, kSortWarps * kWarp, 0, st>>>(ctx->d_tcount, ctx->d_tstart, ctx->d_tburied,
                                                                ctx->d_tentry, ctx->d_tindex, ctx->d_tcell, ctx->d_tgeom,
                                                                (float)ctx->cfg.switch_width, cells, ctx->tentry_cap,
                                                                ctx->d_status);
+    ++ctx->launches;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

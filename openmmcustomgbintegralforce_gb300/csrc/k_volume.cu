@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
     }
     __syncwarp();
     int head = 0, q = 0, s = 0, cnt = 0, l = 0;
+    float4 an = make_float4(0.f, 0.f, 0.f, 0.f);  // the next list entry, loaded one step ahead
     bool has = false;
     unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -431,13 +432,15 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
           has = true;
           v = quad.qv[q];
           w = quad.qw[q];
+          an = __ldg(tab.e + s);
         }
       }
       head += __popc(need);
       if (__ballot_sync(0xffffffffu, has) == 0u) break;
       bool fin = false;
       if (has) {
-        const float4 a = __ldg(tab.e + s + l);
+        const float4 a = an;
+        if (l + 1 < cnt) an = __ldg(tab.e + s + l + 1);
         const float3 d = delta(a, xi, v);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         const float lo = a.w - m.sw, hi = a.w + m.sw;
@@ -752,6 +755,7 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   else
     integral_kernel<MODEL, Q, false><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, nullptr);
+  ++ctx->launches;
 }
 
 template <int MODEL, class Q, bool ADJ>
@@ -764,6 +768,7 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R};
   chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
                                                                                 ctx->n_chunks, ctx->d_dEdJ, o, rr);
+  ++ctx->launches;
 }
 
 gbx_status launch_status(Context* ctx, const char* what) {
