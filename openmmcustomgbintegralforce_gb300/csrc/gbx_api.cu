@@ -161,6 +161,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   ctx->energy_parts = 0;  // the pair kernels add the energy to d_energy_fx
   GBX_TRY(dalloc(ctx, &ctx->d_energy_part, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_energy_fx, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_tile_box, 2 * (((size_t)n + 31) / 32)));
   GBX_TRY(dalloc(ctx, &ctx->d_force_fx, 3 * (size_t)n));
   GBX_TRY(dalloc(ctx, &ctx->d_energy, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_dEdR_fx, n));
@@ -570,7 +571,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx};
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)

@@ -121,6 +121,7 @@ struct Context {
   double* d_energy_part = nullptr;  // [energy_parts] per-CTA energy partials
   int energy_parts = 0;
   unsigned long long* d_energy_fx = nullptr;  // pair energy, fixed point (2^-32)
+  float4* d_tile_box = nullptr;               // cutoff: bounding box of each 32-atom tile
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]

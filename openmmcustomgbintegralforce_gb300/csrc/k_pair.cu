@@ -156,6 +156,7 @@ struct SymArgs {
   unsigned long long* dEdB;
   unsigned long long* dEdq;
   unsigned long long* energy;  // fixed point (2^-32), summed as integers
+  const float4* tile_box;      // cutoff: [2 * ntiles] (lower, upper) corner of each 32-atom tile
   int nblocks, ntiles, chunks;
 };
 
@@ -264,6 +265,44 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 constexpr float kLog2e = 1.4426950408889634f;
 
+// Bounding box of each 32-atom tile (cutoff path), one warp per tile.
+__global__ void __launch_bounds__(kSymThreads) tile_box_kernel(const float4* __restrict__ pos, int n, int ntiles,
+                                                               float4* __restrict__ box) {
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (t >= ntiles) return;
+  const int k = kWarp * t + lane;
+  float lo[3], hi[3];
+  if (k < n) {
+    const float4 p = pos[k];
+    lo[0] = hi[0] = p.x;
+    lo[1] = hi[1] = p.y;
+    lo[2] = hi[2] = p.z;
+  } else {  // padding: the tile's first atom
+    const float4 p = pos[kWarp * t];
+    lo[0] = hi[0] = p.x;
+    lo[1] = hi[1] = p.y;
+    lo[2] = hi[2] = p.z;
+  }
+  for (int off = 16; off > 0; off >>= 1)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+    }
+  if (lane == 0) {
+    box[2 * t] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    box[2 * t + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+  }
+}
+
+// Squared distance between two boxes (0 if they overlap).
+__device__ __forceinline__ float box_gap2(const float4 alo, const float4 ahi, const float4 blo, const float4 bhi) {
+  const float gx = fmaxf(0.f, fmaxf(blo.x - ahi.x, alo.x - bhi.x));
+  const float gy = fmaxf(0.f, fmaxf(blo.y - ahi.y, alo.y - bhi.y));
+  const float gz = fmaxf(0.f, fmaxf(blo.z - ahi.z, alo.z - bhi.z));
+  return fmaf(gx, gx, fmaf(gy, gy, gz * gz));
+}
+
 template <bool CUTOFF, bool ADJ>
 __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
   const int unit = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
@@ -279,8 +318,18 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
     const float kD0 = -0.25f * kLog2e * I0.invB, kD1 = -0.25f * kLog2e * I1.invB;
     const float kB0 = 0.25f * I0.invB, kB1 = 0.25f * I1.invB;
     const int src = (lane + 1) % kWarp;
+    float4 ilo = make_float4(0.f, 0.f, 0.f, 0.f), ihi = ilo;
+    if (CUTOFF) {  // the i-block's box: its two tiles
+      const int t1 = min(2 * b + 1, a.ntiles - 1);
+      const float4 l0 = a.tile_box[4 * b], h0 = a.tile_box[4 * b + 1];
+      const float4 l1 = a.tile_box[2 * t1], h1 = a.tile_box[2 * t1 + 1];
+      ilo = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f);
+      ihi = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f);
+    }
     PFixed s0, s1;
     for (int jt = jt0; jt < jt1; ++jt) {
+      // a tile whose box is beyond the cutoff from the i-block's holds no pair
+      if (CUTOFF && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
       PAtom J = load_patom(a, kWarp * jt + lane);
       PAcc a0{0.f, 0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f, 0.f}, aj{0.f, 0.f, 0.f, 0.f, 0.f};
       float et = 0.0f;
@@ -407,11 +456,14 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
   a.dEdB = ctx->d_dEdB_fx;
   a.dEdq = ctx->d_dEdq_fx;
   a.energy = ctx->d_energy_fx;
+  a.tile_box = ctx->d_tile_box;
   const int wpb = kSymThreads / kWarp;
   const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
   cudaStream_t st = ctx->stream;
   cudaMemsetAsync(ctx->d_energy_fx, 0, sizeof(unsigned long long), st);
   if (a.cutoff2 > 0) {
+    tile_box_kernel<<<(a.ntiles + wpb - 1) / wpb, kSymThreads, 0, st>>>(pos, a.n, a.ntiles, ctx->d_tile_box);
+    ++ctx->launches;
     if (adjoint) {
       pair_sym_kernel<true, true><<<gu, kSymThreads, 0, st>>>(a);
       ++ctx->launches;
