@@ -166,6 +166,14 @@ GBX_API gbx_status gbx_get_lookup_table(gbx_context* ctx, int dims[3], double mi
 GBX_API gbx_status gbx_adjoint_host(gbx_context* ctx, const double* positions, double* energy, double* forces,
                                     double* dEdq, double* dEdR, double* dEdalpha);
 
+/* Device form of gbx_adjoint_host for differentiable callers (a
+ * torch.autograd.Function): posq = device float4 [n] (x, y, z, unused) in nm;
+ * outputs are device FP64 arrays, any of them may be NULL: energy [1],
+ * forces [n][3] (-dE/dx), dEdq [n], dEdR [n], dEdalpha [2].  Runs on `stream`
+ * (NULL: the context's own); flags may hold GBX_EXEC_CHECK. */
+GBX_API gbx_status gbx_adjoint(gbx_context* ctx, const void* posq, double* energy, double* forces, double* dEdq,
+                               double* dEdR, double* dEdalpha, int flags, void* stream);
+
 /* Work counters of the last execute run with GBX_EXEC_COUNT_WORK: (point,
  * listed atom) evaluations, of which inside a GBSW switching shell, and
  * ordered pairs.  Diagnostics for roofline accounting; no counterpart in the

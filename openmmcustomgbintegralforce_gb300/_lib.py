@@ -26,7 +26,7 @@ EXPORTED = (
     "gbx_status_string", "gbx_version", "gbx_config_preset", "gbx_create", "gbx_destroy", "gbx_last_error",
     "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
-    "gbx_adjoint_host", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
+    "gbx_adjoint_host", "gbx_adjoint", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
@@ -130,6 +130,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_get_lookup_table.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.gbx_adjoint_host.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.gbx_get_work.argtypes = [vp, vp, vp, vp]
+    L.gbx_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, ci, vp]
     L.gbx_get_chain_work.argtypes = [vp, vp, vp]
     L.gbx_set_chain_records.argtypes = [vp, ci]
     L.gbx_get_chain_records.argtypes = [vp, vp, vp, vp, vp]
@@ -221,6 +222,14 @@ class Context:
         da = np.zeros(2)
         self._check(self.lib.gbx_adjoint_host(self.h, _p(x), _p(E), _p(F), _p(dq), _p(dR), _p(da)))
         return {"energy": float(E[0]), "forces": F, "dEdq": dq, "dEdR": dR, "dEdalpha": da}
+
+    def adjoint_device(self, posq_ptr: int, energy_ptr: int, forces_ptr: int, dEdq_ptr: int, dEdR_ptr: int,
+                       dEdalpha_ptr: int, flags: int = 0, stream: int = 0):
+        """Device adjoint: every pointer a device address (0 = not wanted)."""
+        self._check(self.lib.gbx_adjoint(self.h, ctypes.c_void_p(posq_ptr), ctypes.c_void_p(energy_ptr or None),
+                                         ctypes.c_void_p(forces_ptr or None), ctypes.c_void_p(dEdq_ptr or None),
+                                         ctypes.c_void_p(dEdR_ptr or None), ctypes.c_void_p(dEdalpha_ptr or None),
+                                         int(flags), ctypes.c_void_p(stream or None)))
 
     def born_radii(self):
         out = np.zeros(self.n)

@@ -732,6 +732,20 @@ gbx_status gbx_adjoint_host(gbx_context* handle, const double* positions, double
   return GBX_OK;
 }
 
+gbx_status gbx_adjoint(gbx_context* handle, const void* posq, double* energy, double* forces, double* dEdq,
+                       double* dEdR, double* dEdalpha, int flags, void* stream) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  const int n = ctx->n;
+  GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));
+  GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
+  const bool check = (flags & GBX_EXEC_CHECK) || (ctx->use_tight ? ctx->tcell_cap == 0 : ctx->cell_cap == 0);
+  GBX_TRY(run_pipeline(ctx, reinterpret_cast<const float4*>(posq), ctx->d_force_fx, n, ctx->d_energy, check, true,
+                       false));
+  return gbx::launch_adjoint_out(ctx, energy, forces, dEdq, dEdR, dEdalpha);
+}
+
 gbx_status gbx_get_born_radii(gbx_context* handle, double* born) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !born) return GBX_ERR_INVALID_ARGUMENT;

@@ -197,5 +197,7 @@ ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
 gbx_status launch_energy_reduce(Context* ctx, double* energy, bool adjoint);
+gbx_status launch_adjoint_out(Context* ctx, double* energy, double* forces, double* dEdq, double* dEdR,
+                              double* dEdalpha);
 
 }  // namespace gbx

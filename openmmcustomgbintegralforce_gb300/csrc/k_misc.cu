@@ -174,6 +174,43 @@ gbx_status launch_chain_prep(Context* ctx, bool adjoint) {
   return GBX_OK;
 }
 
+// Device adjoint outputs: fixed-point sums to FP64, forces as [n][3].
+__global__ void adjoint_out_kernel(int n, int stride, const unsigned long long* __restrict__ force_fx,
+                                   const unsigned long long* __restrict__ dq_fx,
+                                   const unsigned long long* __restrict__ dR_fx, const double* __restrict__ e_in,
+                                   const double* __restrict__ a_in, double* __restrict__ forces,
+                                   double* __restrict__ dEdq, double* __restrict__ dEdR, double* __restrict__ energy,
+                                   double* __restrict__ dEdalpha) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    if (energy) *energy = *e_in;
+    if (dEdalpha) {
+      dEdalpha[0] = a_in[0];
+      dEdalpha[1] = a_in[1];
+    }
+  }
+  if (i >= n) return;
+  if (forces)
+    for (int k = 0; k < 3; ++k) forces[3 * (size_t)i + k] = fixed_to_double(force_fx[(size_t)k * stride + i]);
+  if (dEdq) dEdq[i] = fixed_to_double(dq_fx[i]);
+  if (dEdR) dEdR[i] = fixed_to_double(dR_fx[i]);
+}
+
+gbx_status launch_adjoint_out(Context* ctx, double* energy, double* forces, double* dEdq, double* dEdR,
+                              double* dEdalpha) {
+  const int n = ctx->n;
+  adjoint_out_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, n, ctx->d_force_fx, ctx->d_dEdq_fx, ctx->d_dEdR_fx,
+                                                               ctx->d_energy, ctx->d_alpha_grad, forces, dEdq, dEdR,
+                                                               energy, dEdalpha);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ctx->last_error = std::string("adjoint output launch: ") + cudaGetErrorString(e);
+    return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
 gbx_status launch_energy_reduce(Context* ctx, double* energy, bool adjoint) {
   energy_reduce_kernel<<<1, kRedThreads, 0, ctx->stream>>>(ctx->d_energy_part, ctx->energy_parts, ctx->d_energy_fx,
                                                            energy,
