@@ -174,6 +174,39 @@ GBX_API gbx_status gbx_adjoint_host(gbx_context* ctx, const double* positions, d
 GBX_API gbx_status gbx_adjoint(gbx_context* ctx, const void* posq, double* energy, double* forces, double* dEdq,
                                double* dEdR, double* dEdalpha, int flags, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched evaluation: many independent molecules (uneven sizes, any mix of
+ * presets) per call.  One context per molecule; positions, forces and
+ * energies live in batch-owned device buffers:
+ *   posq     float4 [total atoms], molecule m from atom_offset(m) on (nm)
+ *   forces   u64 fixed point (2^-32) [3 * total], molecule m's block at
+ *            3 * atom_offset(m), layout [3][n_m]
+ *   energies double [molecules] (kJ/mol)
+ * The first call (or one with GBX_EXEC_CHECK) sizes every buffer; later
+ * calls replay one CUDA graph of the whole batch and re-run checked when a
+ * device status word reports that a table outgrew its capacity.  No
+ * counterpart in the reference (which loops one Context per molecule).
+ * ------------------------------------------------------------------------ */
+typedef struct gbx_batch gbx_batch;
+GBX_API gbx_status gbx_batch_create(const gbx_config* configs, const int* n_atoms, int n_molecules, gbx_batch** out);
+GBX_API gbx_status gbx_batch_destroy(gbx_batch* batch);
+/* Molecule m's context (for gbx_set_particle_parameters / _global_ / _box)
+ * and its first atom in the batch buffers. */
+GBX_API gbx_status gbx_batch_molecule(gbx_batch* batch, int m, gbx_context** ctx, long long* atom_offset);
+GBX_API gbx_status gbx_batch_buffers(gbx_batch* batch, void** posq, unsigned long long** forces, double** energies,
+                                     long long* total_atoms);
+/* Device-resident call on `stream` (NULL: the batch's own); returns after
+ * the replay's status check (one 4-byte read-back). */
+GBX_API gbx_status gbx_batch_execute(gbx_batch* batch, int flags, void* stream);
+/* Host arrays: positions / forces [total][3] (nm, kJ/mol/nm), energies [molecules]. */
+GBX_API gbx_status gbx_batch_execute_host(gbx_batch* batch, const double* positions, double* forces,
+                                          double* energies);
+/* Autotuner: times the captured batch over stream counts {4, 8, 16, 32} and
+ * quadrature chunkings (default chunks per atom / {1, 2, 4}) and keeps the
+ * fastest.  Outputs may be NULL. */
+GBX_API gbx_status gbx_batch_tune(gbx_batch* batch, int* streams, int* chunk_divisor, double* ms_per_call);
+GBX_API gbx_status gbx_batch_last_error(gbx_batch* batch, char* buf, size_t len);
+
 /* Work counters of the last execute run with GBX_EXEC_COUNT_WORK: (point,
  * listed atom) evaluations, of which inside a GBSW switching shell, and
  * ordered pairs.  Diagnostics for roofline accounting; no counterpart in the

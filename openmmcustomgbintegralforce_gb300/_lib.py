@@ -28,6 +28,8 @@ EXPORTED = (
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
     "gbx_adjoint_host", "gbx_adjoint", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
+    "gbx_batch_create", "gbx_batch_destroy", "gbx_batch_molecule", "gbx_batch_buffers", "gbx_batch_execute",
+    "gbx_batch_execute_host", "gbx_batch_tune", "gbx_batch_last_error",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
@@ -135,6 +137,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_set_chain_records.argtypes = [vp, ci]
     L.gbx_get_chain_records.argtypes = [vp, vp, vp, vp, vp]
     L.gbx_get_launches.argtypes = [vp, vp]
+    L.gbx_batch_create.argtypes = [vp, vp, ci, ctypes.POINTER(vp)]
+    L.gbx_batch_destroy.argtypes = [vp]
+    L.gbx_batch_molecule.argtypes = [vp, ci, ctypes.POINTER(vp), vp]
+    L.gbx_batch_buffers.argtypes = [vp, vp, vp, vp, vp]
+    L.gbx_batch_execute.argtypes = [vp, ci, vp]
+    L.gbx_batch_execute_host.argtypes = [vp, vp, vp, vp]
+    L.gbx_batch_tune.argtypes = [vp, vp, vp, vp]
+    L.gbx_batch_last_error.argtypes = [vp, ctypes.c_char_p, sz]
     L.gbx_set_timing.argtypes = [vp, ci]
     L.gbx_get_stage_times.argtypes = [vp, vp, ci, vp]
     L.gbx_pair_noalloc.argtypes = [vp, vp, vp, ci, cd, cd, vp, ci, vp, vp, vp]
@@ -170,9 +180,17 @@ class Context:
                 msg = buf.value.decode()
             raise GBXError(status, msg)
 
+    @classmethod
+    def _borrowed(cls, lib, handle, model: GBModel, num_atoms: int) -> "Context":
+        """A view of a context owned by something else (a batch molecule)."""
+        c = cls.__new__(cls)
+        c.lib, c.model, c.n, c.cfg, c.h, c._owner = lib, model, int(num_atoms), GbxConfig.from_model(model), handle, False
+        return c
+
     def close(self):
         if getattr(self, "h", None):
-            self.lib.gbx_destroy(self.h)
+            if getattr(self, "_owner", True):
+                self.lib.gbx_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -291,3 +309,72 @@ class Context:
         self._check(self.lib.gbx_get_lookup_table(self.h, _p(dims), _p(mn), _p(step), ctypes.byref(ncell),
                                                   _p(counts), ctypes.byref(total), _p(atoms)))
         return {"dims": dims, "min": mn, "step": step, "counts": counts, "atoms": atoms[: total.value]}
+
+
+class Batch:
+    """gbx_batch: many molecules per call (one CUDA graph after the first)."""
+
+    def __init__(self, models, sizes):
+        self.lib = load()
+        self.models = list(models)
+        self.sizes = [int(n) for n in sizes]
+        if len(self.models) != len(self.sizes) or not self.sizes:
+            raise GBXError(1, "one model per molecule")
+        cfgs = (GbxConfig * len(self.sizes))(*[GbxConfig.from_model(m) for m in self.models])
+        ns = (ctypes.c_int * len(self.sizes))(*self.sizes)
+        h = ctypes.c_void_p()
+        st = self.lib.gbx_batch_create(cfgs, ns, len(self.sizes), ctypes.byref(h))
+        if st != GBX_OK:
+            raise GBXError(st, "gbx_batch_create")
+        self.h = h
+        self.offsets = []
+        self.molecules = []
+        for m, (model, n) in enumerate(zip(self.models, self.sizes)):
+            ch, off = ctypes.c_void_p(), ctypes.c_longlong()
+            self._check(self.lib.gbx_batch_molecule(self.h, m, ctypes.byref(ch), ctypes.byref(off)))
+            self.offsets.append(off.value)
+            self.molecules.append(Context._borrowed(self.lib, ch, model, n))
+        self.total = sum(self.sizes)
+
+    def _check(self, status: int):
+        if status != GBX_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.gbx_batch_last_error(self.h, buf, 512)
+            raise GBXError(status, buf.value.decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            for c in self.molecules:
+                c.h = None
+            self.lib.gbx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def buffers(self):
+        """Device addresses: (posq float4 [total], forces u64 [3 total], energies f64 [molecules])."""
+        p, f, e, t = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_longlong()
+        self._check(self.lib.gbx_batch_buffers(self.h, ctypes.byref(p), ctypes.byref(f), ctypes.byref(e),
+                                               ctypes.byref(t)))
+        return p.value, f.value, e.value
+
+    def execute_device(self, flags: int = 0, stream: int = 0):
+        self._check(self.lib.gbx_batch_execute(self.h, int(flags), ctypes.c_void_p(stream or None)))
+
+    def execute_host(self, positions):
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        if x.shape != (self.total, 3):
+            raise GBXError(1, "positions must be [total atoms, 3]")
+        F = np.zeros((self.total, 3))
+        E = np.zeros(len(self.sizes))
+        self._check(self.lib.gbx_batch_execute_host(self.h, _p(x), _p(F), _p(E)))
+        return E, F
+
+    def tune(self):
+        s, d, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(self.lib.gbx_batch_tune(self.h, ctypes.byref(s), ctypes.byref(d), ctypes.byref(ms)))
+        return {"streams": s.value, "chunk_divisor": d.value, "ms_per_call": ms.value}

@@ -443,6 +443,40 @@ void set_model_params(Context* ctx, std::vector<float>& wpar, std::vector<float2
 
 }  // namespace
 
+namespace gbx {
+gbx_status pipeline(Context* ctx, const float4* posq, unsigned long long* force, int stride, double* energy, bool check,
+                    bool adjoint, bool count_work, bool forces) {
+  return run_pipeline(ctx, posq, force, stride, energy, check, adjoint, count_work, forces);
+}
+
+gbx_status set_chunks(Context* ctx, int chunks) {
+  const int Q = ctx->cfg.n_radial * ctx->cfg.lebedev_order;
+  chunks = std::max(1, std::min(chunks, std::max(1, Q / 32)));
+  if (chunks == ctx->n_chunks) return GBX_OK;
+  GBX_CUDA(cudaDeviceSynchronize());
+  ctx->n_chunks = chunks;
+  GBX_TRY(dalloc(ctx, &ctx->d_J, 2 * (size_t)chunks * ctx->n));
+  ctx->srec_pending = false;
+  ctx->srec_auto = true;  // record regions are per warp: sized again by the next call
+  return alloc_records(ctx, 0);
+}
+
+gbx_status fix_chain_records(Context* ctx) {
+  // freeze the record regions at the largest need seen so far (no further
+  // event queries: the call sequence can be captured in a CUDA graph)
+  if (ctx->srec_pending) {
+    GBX_CUDA(cudaEventSynchronize(ctx->srec_ev));
+    ctx->srec_pending = false;
+  }
+  const long long seen = ctx->h_rmax ? *ctx->h_rmax : 0;
+  ctx->srec_auto = false;
+  if (ctx->cfg.model != GBX_MODEL_GBSW) return alloc_records(ctx, 0);
+  const int want = (int)((seen + seen / 4 + 64 + 31) / 32 * 32);
+  if (ctx->srec_R >= want && ctx->srec_R > 0) return GBX_OK;
+  return alloc_records(ctx, want);
+}
+}  // namespace gbx
+
 extern "C" {
 
 const char* gbx_status_string(gbx_status s) {

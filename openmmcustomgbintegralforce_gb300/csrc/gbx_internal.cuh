@@ -185,6 +185,12 @@ __host__ __device__ __forceinline__ double fixed_to_double(unsigned long long v)
 // Launchers (implemented in the k_*.cu files); all enqueue on ctx->stream.
 // --------------------------------------------------------------------------
 
+// Whole evaluation on ctx->stream (gbx_api.cu); used by the batch.
+gbx_status pipeline(Context* ctx, const float4* posq, unsigned long long* force, int stride, double* energy, bool check,
+                    bool adjoint, bool count_work, bool forces);
+gbx_status set_chunks(Context* ctx, int chunks);
+gbx_status fix_chain_records(Context* ctx);
+
 gbx_status launch_stage_positions(Context* ctx, const float4* posq);
 gbx_status launch_table_build(Context* ctx, const float4* pos);
 gbx_status launch_tight_build(Context* ctx, const float4* pos);

@@ -124,3 +124,28 @@ def make_globule(n: int, seed: int = 0, density_A3: float = 0.1, step_A: float =
 def jitter(positions: np.ndarray, sigma_nm: float, rng: np.random.Generator) -> np.ndarray:
     """MD-like perturbation (N(0, sigma) per coordinate), rounded to float32."""
     return (positions + rng.normal(0.0, sigma_nm, size=positions.shape)).astype(np.float32).astype(np.float64)
+
+
+def _globule_job(args):
+    n, seed = args
+    return make_globule(n, seed=seed)
+
+
+def batch_sizes(count: int = 256, lo: int = 500, hi: int = 8000, seed: int = 4242):
+    """Atom counts drawn log-uniformly from [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [int(round(np.exp(x))) for x in rng.uniform(np.log(lo), np.log(hi), count)]
+
+
+def make_batch(sizes, seed: int = 4242, workers: int = 0):
+    """One globule per size (seed + index), generated in a spawn-started
+    process pool so that it is safe before or after CUDA initialisation."""
+    import multiprocessing as mp
+    import os
+
+    jobs = [(int(n), seed + k) for k, n in enumerate(sizes)]
+    workers = workers or min(len(jobs), os.cpu_count() or 1)
+    if workers <= 1:
+        return [_globule_job(j) for j in jobs]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_globule_job, jobs, chunksize=1)

@@ -1,0 +1,99 @@
+"""Batched evaluation (gbx_batch): uneven GBSW and GBMV molecules in one call,
+first checked, then replayed from a CUDA graph.  Every molecule must match
+its own single-molecule context bit for bit (same kernels, same order of
+every sum), and the oracle within the usual tolerances; a replay whose table
+outgrows its capacity must fall back to a checked run, not return a
+truncated result."""
+import numpy as np
+import pytest
+
+from openmmcustomgbintegralforce_gb300._lib import Batch, Context
+from openmmcustomgbintegralforce_gb300.globule import batch_sizes, make_batch
+from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def batch_models(gs):
+    ms = []
+    for k, g in enumerate(gs):
+        if k % 2 == 0:
+            ms.append(GBModel.charmm_gbsw(n_radial=24, lebedev=50))
+        else:
+            ms.append(GBModel.gbmv2(box=box_for(g.positions, margin=1.5), n_radial=24, lebedev=50))
+    return ms
+
+
+@pytest.fixture(scope="module")
+def setup():
+    gs = make_batch(batch_sizes(10, 150, 1500, seed=77), seed=77, workers=1)
+    ms = batch_models(gs)
+    b = Batch(ms, [g.n for g in gs])
+    for c, g in zip(b.molecules, gs):
+        c.set_particle_parameters(g.charge, g.radius)
+    X = np.concatenate([g.positions for g in gs])
+    return gs, ms, b, X
+
+
+def plain(gs, ms, X=None):
+    out = []
+    for k, (g, m) in enumerate(zip(gs, ms)):
+        c = Context(m, g.n)
+        c.set_particle_parameters(g.charge, g.radius)
+        out.append(c.execute_host(g.positions if X is None else X[k]))
+        c.close()
+    return out
+
+
+def split(b, F):
+    return [F[o:o + n] for o, n in zip(b.offsets, b.sizes)]
+
+
+def test_batch_matches_single_contexts_bitwise(setup):
+    gs, ms, b, X = setup
+    ref = plain(gs, ms)
+    for call in range(3):  # checked, captured, replayed
+        E, F = b.execute_host(X)
+        for k, (Fk, (Er, Fr)) in enumerate(zip(split(b, F), ref)):
+            assert E[k] == Er, (call, k)
+            assert np.array_equal(Fk, Fr), (call, k)
+
+
+def test_batch_against_oracle(setup):
+    gs, ms, b, X = setup
+    E, F = b.execute_host(X)
+    for k in (0, 1, 2, 3):
+        r = O.Oracle(ms[k]).energy_forces(gs[k].positions, gs[k].charge, gs[k].radius)
+        assert abs(E[k] / r["energy"] - 1) < 2e-5
+        assert rel_rms(split(b, F)[k], r["forces"]) < 1e-4
+
+
+def test_replay_that_outgrows_a_table_reruns_checked(setup):
+    gs, ms, b, X = setup
+    b.execute_host(X)
+    X2 = X.copy()
+    o, n = b.offsets[0], b.sizes[0]  # a GBSW molecule: its exact table must grow
+    ctr = X2[o:o + n].mean(axis=0)
+    X2[o:o + n] = ctr + 1.4 * (X2[o:o + n] - ctr)
+    E, F = b.execute_host(X2)
+    Xs = [X2[o:o + n] for o, n in zip(b.offsets, b.sizes)]
+    ref = plain(gs, ms, Xs)
+    for k, (Fk, (Er, Fr)) in enumerate(zip(split(b, F), ref)):
+        assert E[k] == Er, k
+        assert np.array_equal(Fk, Fr), k
+    b.execute_host(X)
+
+
+def test_tune_keeps_results(setup):
+    gs, ms, b, X = setup
+    E0, F0 = b.execute_host(X)
+    t = b.tune()
+    assert t["streams"] >= 1 and t["chunk_divisor"] in (1, 2, 4) and t["ms_per_call"] > 0
+    E1, F1 = b.execute_host(X)
+    assert np.allclose(E1, E0, rtol=1e-6)
+    assert rel_rms(F1, F0) < 1e-5
