@@ -34,7 +34,7 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-from openmmcustomgbintegralforce_gb300.globule import make_globule  # noqa: E402
+from openmmcustomgbintegralforce_gb300.globule import batch_sizes, make_batch, make_globule  # noqa: E402
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for  # noqa: E402
 
 METRIC = "GB energy+force evals/s at 50k atoms; batched confs/s vs plain; err vs FP64"
@@ -220,6 +220,102 @@ def run_reference(args, world, rank):
     print(json.dumps(line))
 
 
+BATCH_MOLECULES = 256
+BATCH_SEED = 4242
+
+
+def batch_models(gs):
+    """128 GBSW + 128 GBMV-II molecules, 24 x 50 quadrature (alternating)."""
+    out = []
+    for k, g in enumerate(gs):
+        if k % 2 == 0:
+            out.append(GBModel.charmm_gbsw(n_radial=24, lebedev=50))
+        else:
+            out.append(GBModel.gbmv2(box=box_for(g.positions, margin=1.5), n_radial=24, lebedev=50))
+    return out
+
+
+def measure_batched(gs, steps: int):
+    """Conformations/s of the batched form (one CUDA graph per call) against
+    looping the plain single-molecule path over the same molecules, both with
+    device-resident inputs and through host arrays, plus the error of a
+    sample against the FP64 oracle."""
+    import torch
+
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_ENERGY, EXEC_FORCES, Batch
+
+    models = batch_models(gs)
+    sizes = [g.n for g in gs]
+    b = Batch(models, sizes)
+    for c, g in zip(b.molecules, gs):
+        c.set_particle_parameters(g.charge, g.radius)
+    X = np.concatenate([g.positions for g in gs])
+    E, F = b.execute_host(X)  # checked: sizes every buffer, uploads the positions
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    p, f, e = b.buffers()
+
+    def plain_loop():  # one gbx_execute per molecule on one stream, inputs resident
+        for m, c in enumerate(b.molecules):
+            c.execute_device(p + 16 * b.offsets[m], f + 24 * b.offsets[m], c.n, e + 8 * m,
+                             EXEC_FORCES | EXEC_ENERGY, sptr)
+
+    def timed(fn, k):
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(k):
+            fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / k
+
+    def host_timed(fn, k):
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        return 1000.0 * (time.perf_counter() - t0) / k
+
+    def plain_host_loop():  # one host-array call per conformation, as a caller of the plain API
+        for c, g in zip(b.molecules, gs):
+            c.execute_host(g.positions)
+
+    for _ in range(2):
+        plain_loop()
+    plain_ms = timed(plain_loop, steps)
+    plain_host_loop()
+    plain_host_ms = host_timed(plain_host_loop, max(2, steps // 3))
+    tune = b.tune()
+    b.execute_host(X)  # restores the positions; the tuned graph is captured on the next call
+    for _ in range(2):
+        b.execute_device(0, sptr)
+    batch_ms = timed(lambda: b.execute_device(0, sptr), steps)
+    batch_host_ms = host_timed(lambda: b.execute_host(X), max(2, steps // 3))
+    E, F = b.execute_host(X)
+    errs = []
+    from oracle import oracle as O
+
+    for k in (0, 1, 2, 3):
+        r = O.Oracle(models[k]).energy_forces(gs[k].positions, gs[k].charge, gs[k].radius)
+        Fk = F[b.offsets[k]:b.offsets[k] + sizes[k]]
+        errs.append((abs(E[k] / r["energy"] - 1.0),
+                     float(np.sqrt(((Fk - r["forces"]) ** 2).sum() / (r["forces"] ** 2).sum()))))
+    b.close()
+    n = len(gs)
+    return {"workload": f"{n} globules, atoms log-uniform in [500, 8000] (total {sum(sizes)}), "
+                        f"{(n + 1) // 2} GBSW + {n // 2} GBMV-II, 24x50 quadrature, full N^2",
+            "confs_per_s": n * 1000.0 / batch_ms, "ms_per_batch": batch_ms,
+            "plain_confs_per_s": n * 1000.0 / plain_ms, "plain_ms_per_loop": plain_ms,
+            "speedup_vs_plain": plain_ms / batch_ms, "tune": tune,
+            "plain": "one gbx_execute per molecule on one stream (inputs resident, no per-call sync)",
+            "host": {"confs_per_s": n * 1000.0 / batch_host_ms, "plain_confs_per_s": n * 1000.0 / plain_host_ms,
+                     "speedup_vs_plain": plain_host_ms / batch_host_ms,
+                     "plain": "gbx_execute_host per molecule (host positions in, forces and energy out)",
+                     "batched": "gbx_batch_execute_host (all positions in, all forces and energies out)"},
+            "err_vs_fp64_sample": {"molecules": [0, 1, 2, 3], "energy_rel_max": max(a for a, _ in errs),
+                                   "force_rel_rms_max": max(b_ for _, b_ in errs)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -228,7 +324,12 @@ def main():
     ap.add_argument("--workload", default="gbsw50k", choices=sorted(workloads()))
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-molecule measurement")
     args = ap.parse_args()
+    batch_set = None
+    if args.impl == "gb300" and not args.no_batch and int(os.environ.get("RANK", "0")) == 0:
+        # generated before any CUDA work, in a spawn-started pool
+        batch_set = make_batch(batch_sizes(BATCH_MOLECULES, 500, 8000, seed=BATCH_SEED), seed=BATCH_SEED)
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
@@ -378,6 +479,8 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single"},
                 "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "err_vs_fp64": err, "clocks": clk, "wall_s": wall}
+        if batch_set is not None:
+            line["batched"] = measure_batched(batch_set, max(3, min(args.steps, 10)))
         print(json.dumps(line))
 
 

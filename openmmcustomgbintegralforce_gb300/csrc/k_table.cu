@@ -228,7 +228,12 @@ template <bool FILL>
 __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, const double* __restrict__ radius,
                                               int n, const TableGeom* __restrict__ gp, double buffer, Emit em,
                                               long long cell_cap, unsigned* __restrict__ status) {
+  // per warp and axis: the samples, their cell index (-1 outside) and the
+  // squared offset from the atom -- each depends on one axis only, so it is
+  // computed once per axis value, with the same FP64 operations
   __shared__ double s_samp[8][3][kMaxSamples];
+  __shared__ double s_sq[8][3][kMaxSamples];
+  __shared__ int s_id[8][3][kMaxSamples];
   const int wib = threadIdx.x / kWarp;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
@@ -236,14 +241,16 @@ __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, co
   if (g.ncell > cell_cap) return;
   const long long ncell = g.ncell;
   double (*samp)[kMaxSamples] = s_samp[wib];
+  double (*sq)[kMaxSamples] = s_sq[wib];
+  int (*idx)[kMaxSamples] = s_id[wib];
   for (int a = warp; a < n; a += (gridDim.x * blockDim.x) / kWarp) {
     float4 p = pos[a];
     const double c[3] = {(double)p.x, (double)p.y, (double)p.z};
     const double L = g.L;
     const double pad = dadd(dadd(radius[a], dmul(half_sqrt3(), L)), buffer);
     const double pad2 = dmul(pad, pad);
-    int cnt[3] = {0, 0, 0};
-    // lanes 0..2 walk one axis each
+    int cnt0 = 0;
+    // lanes 0..2 walk one axis each (samples by repeated addition, as the reference)
     if (lane < 3) {
       const int k = lane;
       double x = dsub(dsub(c[k], pad), L);
@@ -255,31 +262,36 @@ __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, co
         x = dadd(x, g.step[k]);
       }
       if (m > kMaxSamples) atomicOr(status, kStatusTableEntries);
-      cnt[0] = m;  // reused below via shuffle
+      cnt0 = m;
     }
-    __syncwarp();
+    int cnt[3];
     for (int k = 0; k < 3; ++k) {
-      int v = __shfl_sync(0xffffffffu, cnt[0], k);
+      const int v = __shfl_sync(0xffffffffu, cnt0, k);
       cnt[k] = v < kMaxSamples ? v : kMaxSamples;
     }
+    __syncwarp();
+    for (int t = lane; t < cnt[0] + cnt[1] + cnt[2]; t += kWarp) {
+      const int k = t < cnt[0] ? 0 : (t < cnt[0] + cnt[1] ? 1 : 2);
+      const int m = t - (k == 0 ? 0 : (k == 1 ? cnt[0] : cnt[0] + cnt[1]));
+      const double xk = samp[k][m];
+      const double d = g.box[k];
+      const double x0 = dsub(xk, dmul(d, floor(ddiv(dsub(xk, g.min[k]), d))));
+      const int id = (int)floor(ddiv(dsub(x0, g.min[k]), g.step[k]));
+      idx[k][m] = (id < 0 || id >= g.dims[k]) ? -1 : id;
+      const double e = dsub(xk, c[k]);
+      sq[k][m] = dmul(e, e);
+    }
+    __syncwarp();
     const int total = cnt[0] * cnt[1] * cnt[2];
     const long long sy = g.dims[2], sx = (long long)g.dims[1] * g.dims[2];
     for (int t = lane; t < total; t += kWarp) {
       const int kx = t / (cnt[1] * cnt[2]);
       const int ky = (t / cnt[2]) % cnt[1];
       const int kz = t % cnt[2];
-      const double xyz[3] = {samp[0][kx], samp[1][ky], samp[2][kz]};
-      int id[3];
-      bool inside = true;
-      for (int k = 0; k < 3; ++k) {
-        const double d = g.box[k];
-        const double x0 = dsub(xyz[k], dmul(d, floor(ddiv(dsub(xyz[k], g.min[k]), d))));
-        id[k] = (int)floor(ddiv(dsub(x0, g.min[k]), g.step[k]));
-        if (id[k] < 0 || id[k] >= g.dims[k]) inside = false;
-      }
-      const double e0 = dsub(xyz[0], c[0]), e1 = dsub(xyz[1], c[1]), e2 = dsub(xyz[2], c[2]);
-      const double s = dadd(dadd(dmul(e0, e0), dmul(e1, e1)), dmul(e2, e2));
-      if (s < pad2 && inside) em.put<FILL>((long long)id[0] * sx + (long long)id[1] * sy + id[2], a, ncell);
+      const int i0 = idx[0][kx], i1 = idx[1][ky], i2 = idx[2][kz];
+      const double s = dadd(dadd(sq[0][kx], sq[1][ky]), sq[2][kz]);
+      if (s < pad2 && i0 >= 0 && i1 >= 0 && i2 >= 0)
+        em.put<FILL>((long long)i0 * sx + (long long)i1 * sy + i2, a, ncell);
     }
     __syncwarp();
   }

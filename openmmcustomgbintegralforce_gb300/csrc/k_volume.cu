@@ -512,10 +512,14 @@ struct ChainRecords {
   int R;
 };
 
+// A component whose fixed-point value is 0 (|g| < 2^-33, common for distant
+// GBMV atoms) changes nothing: its reduction is skipped, the result is the
+// same bits.
 __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, float gy, float gz) {
-  red_add_fixed(&o.force[k], -gx);
-  red_add_fixed(&o.force[k + o.stride], -gy);
-  red_add_fixed(&o.force[k + 2 * o.stride], -gz);
+  const long long fx = float_to_fixed(-gx), fy = float_to_fixed(-gy), fz = float_to_fixed(-gz);
+  if (fx) atomicAdd(&o.force[k], (unsigned long long)fx);
+  if (fy) atomicAdd(&o.force[k + o.stride], (unsigned long long)fy);
+  if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
 }
 
 template <int MODEL, class Q, bool ADJ>
