@@ -60,6 +60,11 @@ FLOPS_CHAIN_SHELL = 22.0
 FLOPS_PAIR = 39.0
 
 
+# DRAM bytes (read + write) per launch of each stage's main kernel, from one ncu
+# capture of the same command (profiles/kernels_gbsw50k.md).
+TRAFFIC = {"gbsw50k": {"integrals": 854.3e6 + 573.5e6, "pair": 3.0e6, "chain_rule": 957.5e6 + 3.8e6}}
+
+
 def workloads():
     return {
         "gbsw50k": dict(n=50000, seed=2026, model=GBModel.charmm_gbsw(n_radial=32, lebedev=110),
@@ -433,7 +438,9 @@ def main():
     dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
     achieved = cand.get(dominant)
     roofline = {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                "frac": (achieved / fp32_peak) if achieved else None,
+                "traffic": TRAFFIC.get(args.workload, {}).get(dominant),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, profiles/kernels_gbsw50k.md",
                 "peak_source": "nominal FP32 (152 SM x 128 lanes x 2 flop x max SM clock); "
                                f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
                 "per_stage_tflops": cand, "stage_ms": stage_ms,
