@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
 
 // ---------------------------------------------------------------------------
 // Symmetric scheme (the context path): every unordered pair once.  A warp
-// owns an i-block of 64 atoms (two per lane: 64 b + lane and 64 b + 32 + lane)
+// owns an i-block of 128 atoms (four per lane: 128 b + 32 u + lane)
 // and a run of 32-atom j-tiles above the block.  A j-tile's atoms and their
 // force / dE/dB accumulators rotate one lane per step through shuffles, so
 // after 32 steps every (i, j) pair of the tile was evaluated once and each
@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
 // runs in a fixed order; i- and j-side sums are rounded to fixed point once
 // per tile and added as integers.
 // ---------------------------------------------------------------------------
-constexpr int kSymI = 64;       // atoms per i-block
+constexpr int kNI = 4;          // i-atoms per lane
+constexpr int kSymI = kWarp * kNI;  // atoms per i-block (one warp)
 constexpr int kSymChunk = 16;   // j-tiles per warp unit
 constexpr int kSymThreads = 128;
 
@@ -309,89 +310,101 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
   const int lane = threadIdx.x % kWarp;
   if (unit >= a.nblocks * a.chunks) return;
   const int b = unit / a.chunks, ch = unit % a.chunks;
-  const int jt0 = 2 * b + 2 + ch * kSymChunk;
+  const int jt0 = kNI * b + kNI + ch * kSymChunk;
   const int jt1 = min(a.ntiles, jt0 + kSymChunk);
   double E = 0.0;
   if (jt0 < jt1) {
-    const PAtom I0 = load_patom(a, kSymI * b + lane), I1 = load_patom(a, kSymI * b + kWarp + lane);
-    const float pq0 = a.pref * I0.q, pq1 = a.pref * I1.q;
-    const float kD0 = -0.25f * kLog2e * I0.invB, kD1 = -0.25f * kLog2e * I1.invB;
-    const float kB0 = 0.25f * I0.invB, kB1 = 0.25f * I1.invB;
+    PAtom I[kNI];
+    float pq[kNI], kD[kNI], kB[kNI];
+#pragma unroll
+    for (int u = 0; u < kNI; ++u) {
+      I[u] = load_patom(a, kSymI * b + kWarp * u + lane);
+      pq[u] = a.pref * I[u].q;
+      kD[u] = -0.25f * kLog2e * I[u].invB;
+      kB[u] = 0.25f * I[u].invB;
+    }
     const int src = (lane + 1) % kWarp;
     float4 ilo = make_float4(0.f, 0.f, 0.f, 0.f), ihi = ilo;
-    if (CUTOFF) {  // the i-block's box: its two tiles
-      const int t1 = min(2 * b + 1, a.ntiles - 1);
-      const float4 l0 = a.tile_box[4 * b], h0 = a.tile_box[4 * b + 1];
-      const float4 l1 = a.tile_box[2 * t1], h1 = a.tile_box[2 * t1 + 1];
-      ilo = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f);
-      ihi = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f);
+    if (CUTOFF) {  // the i-block's box: the union of its tiles
+      ilo = make_float4(3e38f, 3e38f, 3e38f, 0.f);
+      ihi = make_float4(-3e38f, -3e38f, -3e38f, 0.f);
+      for (int u = 0; u < kNI; ++u) {
+        const int t = min(kNI * b + u, a.ntiles - 1);
+        const float4 l = a.tile_box[2 * t], h = a.tile_box[2 * t + 1];
+        ilo = make_float4(fminf(ilo.x, l.x), fminf(ilo.y, l.y), fminf(ilo.z, l.z), 0.f);
+        ihi = make_float4(fmaxf(ihi.x, h.x), fmaxf(ihi.y, h.y), fmaxf(ihi.z, h.z), 0.f);
+      }
     }
-    PFixed s0, s1;
+    PFixed si[kNI];
     for (int jt = jt0; jt < jt1; ++jt) {
-      // a tile whose box is beyond the cutoff from the i-block's holds no pair
       if (CUTOFF && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
       PAtom J = load_patom(a, kWarp * jt + lane);
-      PAcc a0{0.f, 0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f, 0.f}, aj{0.f, 0.f, 0.f, 0.f, 0.f};
+      PAcc ai[kNI], aj{0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int u = 0; u < kNI; ++u) ai[u] = PAcc{0.f, 0.f, 0.f, 0.f, 0.f};
       float et = 0.0f;
 #pragma unroll 2
       for (int t = 0; t < kWarp; ++t) {
         const float kBj = 0.25f * J.invB;
-        gb_pair<true, CUTOFF, ADJ>(I0, pq0, kD0, kB0, J, kBj, a.pref, a.cutoff2, a0, aj, et);
-        gb_pair<true, CUTOFF, ADJ>(I1, pq1, kD1, kB1, J, kBj, a.pref, a.cutoff2, a1, aj, et);
-        rotate(J, aj, src, ADJ);  // after 32 steps every j is back in its own lane
+#pragma unroll
+        for (int u = 0; u < kNI; ++u)
+          gb_pair<true, CUTOFF, ADJ>(I[u], pq[u], kD[u], kB[u], J, kBj, a.pref, a.cutoff2, ai[u], aj, et);
+        rotate(J, aj, src, ADJ);
       }
       PFixed sj;
       sj.add(aj);
       push_atom<ADJ>(a, kWarp * jt + lane, sj);
-      s0.add(a0);
-      s1.add(a1);
+#pragma unroll
+      for (int u = 0; u < kNI; ++u) si[u].add(ai[u]);
       E += (double)et;
     }
-    push_atom<ADJ>(a, kSymI * b + lane, s0);
-    push_atom<ADJ>(a, kSymI * b + kWarp + lane, s1);
+#pragma unroll
+    for (int u = 0; u < kNI; ++u) push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, si[u]);
   }
   E = warp_sum(E);
   if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
 }
 
-// Pairs inside each 64-atom i-block (i side only, each ordered pair once)
-// and the self terms 1/2 pref q_i^2 / B_i.
+// Pairs inside each i-block (i side only, each ordered pair once: lane t of
+// slot h broadcasts its atom to the warp) and the self terms 1/2 pref q^2 / B.
 template <bool CUTOFF, bool ADJ>
 __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
   const int b = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (b >= a.nblocks) return;
-  const int i0 = kSymI * b + lane, i1 = i0 + kWarp;
-  const PAtom I0 = load_patom(a, i0), I1 = load_patom(a, i1);
-  const float pq0 = a.pref * I0.q, pq1 = a.pref * I1.q;
-  const float kD0 = -0.25f * kLog2e * I0.invB, kD1 = -0.25f * kLog2e * I1.invB;
-  const float kB0 = 0.25f * I0.invB, kB1 = 0.25f * I1.invB;
-  PAcc a0{0.f, 0.f, 0.f, 0.f, 0.f}, a1{0.f, 0.f, 0.f, 0.f, 0.f}, dummy{0.f, 0.f, 0.f, 0.f, 0.f};
-  float e0 = 0.0f, e1 = 0.0f;
-  for (int h = 0; h < 2; ++h)
-    for (int t = 0; t < kWarp; ++t) {
-      const PAtom& S = h ? I1 : I0;
-      const PAtom J{__shfl_sync(0xffffffffu, S.x, t), __shfl_sync(0xffffffffu, S.y, t),
-                    __shfl_sync(0xffffffffu, S.z, t), __shfl_sync(0xffffffffu, S.q, t),
-                    __shfl_sync(0xffffffffu, S.B, t), __shfl_sync(0xffffffffu, S.invB, t)};
-      const int j = kSymI * b + h * kWarp + t;
-      if (j != i0) gb_pair<false, CUTOFF, ADJ>(I0, pq0, kD0, kB0, J, 0.f, a.pref, a.cutoff2, a0, dummy, e0);
-      if (j != i1) gb_pair<false, CUTOFF, ADJ>(I1, pq1, kD1, kB1, J, 0.f, a.pref, a.cutoff2, a1, dummy, e1);
-    }
-  PFixed s0, s1;
-  s0.add(a0);
-  s1.add(a1);
-  // self term: 1/2 pref q^2 / B, dE/dB = -1/2 pref q^2 / B^2, dE/dq = pref q / B
-  s0.db += float_to_fixed(-0.5f * pq0 * I0.q * I0.invB * I0.invB);
-  s1.db += float_to_fixed(-0.5f * pq1 * I1.q * I1.invB * I1.invB);
-  if (ADJ) {
-    s0.dq += float_to_fixed(pq0 * I0.invB);
-    s1.dq += float_to_fixed(pq1 * I1.invB);
+  PAtom I[kNI];
+  float pq[kNI], kD[kNI], kB[kNI], e[kNI];
+  PAcc ai[kNI], dummy{0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int u = 0; u < kNI; ++u) {
+    I[u] = load_patom(a, kSymI * b + kWarp * u + lane);
+    pq[u] = a.pref * I[u].q;
+    kD[u] = -0.25f * kLog2e * I[u].invB;
+    kB[u] = 0.25f * I[u].invB;
+    ai[u] = PAcc{0.f, 0.f, 0.f, 0.f, 0.f};
+    e[u] = 0.0f;
   }
-  push_atom<ADJ>(a, i0, s0);
-  push_atom<ADJ>(a, i1, s1);
-  double E = 0.5 * ((double)e0 + (double)e1);  // each pair visited from both ends
-  E += 0.5 * ((double)pq0 * I0.q * I0.invB + (double)pq1 * I1.q * I1.invB);
+#pragma unroll
+  for (int h = 0; h < kNI; ++h)
+    for (int t = 0; t < kWarp; ++t) {
+      const PAtom J{__shfl_sync(0xffffffffu, I[h].x, t), __shfl_sync(0xffffffffu, I[h].y, t),
+                    __shfl_sync(0xffffffffu, I[h].z, t), __shfl_sync(0xffffffffu, I[h].q, t),
+                    __shfl_sync(0xffffffffu, I[h].B, t), __shfl_sync(0xffffffffu, I[h].invB, t)};
+#pragma unroll
+      for (int u = 0; u < kNI; ++u)
+        if (h != u || t != lane)
+          gb_pair<false, CUTOFF, ADJ>(I[u], pq[u], kD[u], kB[u], J, 0.f, a.pref, a.cutoff2, ai[u], dummy, e[u]);
+    }
+  double E = 0.0;
+#pragma unroll
+  for (int u = 0; u < kNI; ++u) {
+    PFixed su;
+    su.add(ai[u]);
+    su.db += float_to_fixed(-0.5f * pq[u] * I[u].q * I[u].invB * I[u].invB);
+    if (ADJ) su.dq += float_to_fixed(pq[u] * I[u].invB);
+    push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, su);
+    E += 0.5 * (double)e[u] + 0.5 * (double)pq[u] * I[u].q * I[u].invB;
+  }
   E = warp_sum(E);
   if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
 }

@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
     }
     __syncwarp();
     int head = 0, q = 0, s = 0, cnt = 0, l = 0;
-    float4 an = make_float4(0.f, 0.f, 0.f, 0.f);  // the next list entry, loaded one step ahead
+    float4 an = make_float4(0.f, 0.f, 0.f, 0.f), an2 = an;  // the next two list entries
     bool has = false;
     unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -433,30 +433,38 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
           v = quad.qv[q];
           w = quad.qw[q];
           an = __ldg(tab.e + s);
+          if (cnt > 1) an2 = __ldg(tab.e + s + 1);
         }
       }
       head += __popc(need);
       if (__ballot_sync(0xffffffffu, has) == 0u) break;
       bool fin = false;
       if (has) {
-        const float4 a = an;
-        if (l + 1 < cnt) an = __ldg(tab.e + s + l + 1);
-        const float3 d = delta(a, xi, v);
-        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-        const float lo = a.w - m.sw, hi = a.w + m.sw;
-        if (r2 <= lo * lo) {
-          V = 0.0f;
-          fin = true;
-        } else {
-          if (r2 < hi * hi) {
-            const float dr = r2 * rsqrtf(r2) - a.w;
-            V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-            if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
-              if (l < 64) shaped |= 1ull << l;
-              else s_long[wib] = 1;
+        // two list entries per step (entries l and l + 1 were loaded one step ahead)
+        const float4 ea = an, eb = an2;
+        if (l + 2 < cnt) an = __ldg(tab.e + s + l + 2);
+        if (l + 3 < cnt) an2 = __ldg(tab.e + s + l + 3);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (fin) break;
+          const float4 a = u == 0 ? ea : eb;
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float lo = a.w - m.sw, hi = a.w + m.sw;
+          if (r2 <= lo * lo) {
+            V = 0.0f;
+            fin = true;
+          } else {
+            if (r2 < hi * hi) {
+              const float dr = r2 * rsqrtf(r2) - a.w;
+              V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+              if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
+                if (l < 64) shaped |= 1ull << l;
+                else s_long[wib] = 1;
+              }
             }
+            fin = ++l == cnt;
           }
-          fin = ++l == cnt;
         }
       }
       if (fin) {
