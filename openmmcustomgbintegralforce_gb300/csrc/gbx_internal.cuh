@@ -14,6 +14,7 @@ namespace gbx {
 constexpr int kWarp = 32;
 constexpr double kFixedScale = 4294967296.0;  // 2^32, OpenMM's force fixed-point scale
 constexpr int kMaxSortSegment = 2048;         // longest cell list the sort handles
+constexpr int kMaxSortCells = 1 << 17;        // cells of the cutoff pair term's spatial order
 
 // Device status bits (context->d_status).
 enum : unsigned {
@@ -122,6 +123,13 @@ struct Context {
   int energy_parts = 0;
   unsigned long long* d_energy_fx = nullptr;  // pair energy, fixed point (2^-32)
   float4* d_tile_box = nullptr;               // cutoff: bounding box of each 32-atom tile
+  int* d_perm = nullptr;                      // cutoff: atoms in spatial order [n]
+  int* d_perm_tmp = nullptr;                  // cutoff: the same before the per-cell sort [n]
+  int* d_cell_of = nullptr;                   // cutoff: spatial cell of each atom [n]
+  int* d_scount = nullptr;                    // cutoff: atoms per spatial cell [kMaxSortCells]
+  int* d_sstart = nullptr;
+  int* d_scursor = nullptr;
+  int4* d_sgeom = nullptr;                    // cutoff: spatial grid geometry
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]

@@ -158,6 +158,7 @@ struct SymArgs {
   unsigned long long* dEdq;
   unsigned long long* energy;  // fixed point (2^-32), summed as integers
   const float4* tile_box;      // cutoff: [2 * ntiles] (lower, upper) corner of each 32-atom tile
+  const int* perm;             // cutoff: slot k holds atom perm[k] (spatial order); nullptr: identity
   int nblocks, ntiles, chunks;
 };
 
@@ -172,6 +173,7 @@ struct PAcc {
 __device__ __forceinline__ PAtom load_patom(const SymArgs& a, int k) {
   PAtom t{0.f, 0.f, 0.f, 0.f, 1.f, 1.f};  // padding atom: no charge
   if (k < a.n) {
+    if (a.perm) k = a.perm[k];
     const float4 p = a.pos[k];
     const float2 b = a.born[k];
     t = PAtom{p.x, p.y, p.z, a.charge[k], b.x, b.y};
@@ -238,6 +240,7 @@ struct PFixed {
 template <bool ADJ>
 __device__ __forceinline__ void push_atom(const SymArgs& a, int k, const PFixed& f) {
   if (k >= a.n) return;
+  if (a.perm) k = a.perm[k];
   atomicAdd(&a.force[k], (unsigned long long)f.fx);
   atomicAdd(&a.force[k + a.stride], (unsigned long long)f.fy);
   atomicAdd(&a.force[k + 2 * a.stride], (unsigned long long)f.fz);
@@ -267,20 +270,20 @@ __device__ __forceinline__ double warp_sum(double v) {
 constexpr float kLog2e = 1.4426950408889634f;
 
 // Bounding box of each 32-atom tile (cutoff path), one warp per tile.
-__global__ void __launch_bounds__(kSymThreads) tile_box_kernel(const float4* __restrict__ pos, int n, int ntiles,
-                                                               float4* __restrict__ box) {
+__global__ void __launch_bounds__(kSymThreads) tile_box_kernel(const float4* __restrict__ pos, const int* __restrict__ perm,
+                                                               int n, int ntiles, float4* __restrict__ box) {
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (t >= ntiles) return;
   const int k = kWarp * t + lane;
   float lo[3], hi[3];
   if (k < n) {
-    const float4 p = pos[k];
+    const float4 p = pos[perm[k]];
     lo[0] = hi[0] = p.x;
     lo[1] = hi[1] = p.y;
     lo[2] = hi[2] = p.z;
   } else {  // padding: the tile's first atom
-    const float4 p = pos[kWarp * t];
+    const float4 p = pos[perm[kWarp * t]];
     lo[0] = hi[0] = p.x;
     lo[1] = hi[1] = p.y;
     lo[2] = hi[2] = p.z;
@@ -409,6 +412,167 @@ __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
   if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
 }
 
+// ---------------------------------------------------------------------------
+// Spatial order for the cutoff pair term: atoms are binned into cubic cells
+// (1 nm, grown so that the grid holds at most kMaxSortCells cells) and, within
+// a cell, kept in ascending atom order, so the permutation depends on the
+// input alone.  32 consecutive slots then form a compact tile whose bounding
+// box is far from most others, and the cutoff culls those tile pairs.
+// ---------------------------------------------------------------------------
+struct SortGeom {
+  float lo[3];
+  float inv_cell;
+  int dims[3];
+  int ncell;
+};
+
+constexpr int kBoxThreads = 1024;
+constexpr int kSortSeg = 512;  // atoms per cell ranked in shared memory
+
+__global__ void __launch_bounds__(kBoxThreads) sort_geom_kernel(const float4* __restrict__ pos, int n,
+                                                                SortGeom* __restrict__ g) {
+  __shared__ float s_lo[3][kBoxThreads / kWarp], s_hi[3][kBoxThreads / kWarp];
+  float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const float4 p = pos[k];
+    lo[0] = fminf(lo[0], p.x), hi[0] = fmaxf(hi[0], p.x);
+    lo[1] = fminf(lo[1], p.y), hi[1] = fmaxf(hi[1], p.y);
+    lo[2] = fminf(lo[2], p.z), hi[2] = fmaxf(hi[2], p.z);
+  }
+  for (int off = 16; off > 0; off >>= 1)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+    }
+  if (threadIdx.x % kWarp == 0)
+    for (int d = 0; d < 3; ++d) {
+      s_lo[d][threadIdx.x / kWarp] = lo[d];
+      s_hi[d][threadIdx.x / kWarp] = hi[d];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x / kWarp); ++w)
+      for (int d = 0; d < 3; ++d) {
+        s_lo[d][0] = fminf(s_lo[d][0], s_lo[d][w]);
+        s_hi[d][0] = fmaxf(s_hi[d][0], s_hi[d][w]);
+      }
+    float cell = 1.0f;
+    for (;;) {
+      long long tot = 1;
+      int dims[3];
+      for (int d = 0; d < 3; ++d) {
+        const float span = (s_hi[d][0] - s_lo[d][0]) / cell;
+        // non-finite or huge spans (invalid positions) collapse to one cell row
+        dims[d] = (span >= 0.0f && span < (float)kMaxSortCells) ? (int)span + 1 : 1;
+        tot *= dims[d];
+      }
+      if (tot <= kMaxSortCells || cell > 1e6f) {
+        for (int d = 0; d < 3; ++d) {
+          g->lo[d] = s_lo[d][0];
+          g->dims[d] = dims[d];
+        }
+        g->inv_cell = 1.0f / cell;
+        g->ncell = (int)tot;
+        break;
+      }
+      cell *= 1.25f;
+    }
+  }
+}
+
+__device__ __forceinline__ int sort_cell(const SortGeom& g, const float4 p) {
+  int c[3];
+  const float x[3] = {p.x, p.y, p.z};
+  for (int d = 0; d < 3; ++d) c[d] = min(g.dims[d] - 1, max(0, (int)((x[d] - g.lo[d]) * g.inv_cell)));
+  return (c[0] * g.dims[1] + c[1]) * g.dims[2] + c[2];
+}
+
+__global__ void sort_count_kernel(const float4* __restrict__ pos, int n, const SortGeom* __restrict__ g,
+                                  int* __restrict__ cell_of, int* __restrict__ count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int c = sort_cell(*g, pos[k]);
+  cell_of[k] = c;
+  atomicAdd(&count[c], 1);
+}
+
+// Exclusive scan of the cell counts, one block (at most kMaxSortCells cells).
+__global__ void __launch_bounds__(kBoxThreads) sort_scan_kernel(const int* __restrict__ count,
+                                                                const SortGeom* __restrict__ g,
+                                                                int* __restrict__ start, int* __restrict__ cursor) {
+  __shared__ int s_warp[kBoxThreads / kWarp];
+  __shared__ int s_carry;
+  const int ncell = g->ncell;
+  const int lane = threadIdx.x % kWarp, wib = threadIdx.x / kWarp;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int base = 0; base < ncell; base += blockDim.x) {
+    const int c = base + threadIdx.x;
+    const int v = c < ncell ? count[c] : 0;
+    int incl = v;
+    for (int off = 1; off < kWarp; off <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += u;
+    }
+    if (lane == kWarp - 1) s_warp[wib] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int w = 0; w < (int)(blockDim.x / kWarp); ++w) {
+        const int t = s_warp[w];
+        s_warp[w] = acc;
+        acc += t;
+      }
+    }
+    __syncthreads();
+    const int excl = s_carry + s_warp[wib] + incl - v;
+    if (c < ncell) {
+      start[c] = excl;
+      cursor[c] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry = excl + v;
+    __syncthreads();
+  }
+}
+
+__global__ void sort_scatter_kernel(const int* __restrict__ cell_of, int n, const int* __restrict__ start,
+                                    int* __restrict__ cursor, int* __restrict__ perm) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int c = cell_of[k];
+  perm[start[c] + atomicAdd(&cursor[c], 1)] = k;
+}
+
+// Each cell's atoms in ascending atom order: ranks from the scatter's output
+// (arbitrary order within a cell) into perm, out of place.
+__global__ void __launch_bounds__(kSymThreads) sort_cells_by_atom_kernel(const int* __restrict__ count,
+                                                                         const int* __restrict__ start,
+                                                                         const SortGeom* __restrict__ g,
+                                                                         const int* __restrict__ unsorted,
+                                                                         int* __restrict__ perm) {
+  __shared__ int s_buf[kSymThreads / kWarp][kSortSeg];
+  const int lane = threadIdx.x % kWarp, wib = threadIdx.x / kWarp;
+  const int ncell = g->ncell;
+  int* buf = s_buf[wib];
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp; c < ncell; c += gridDim.x * blockDim.x / kWarp) {
+    const int cnt = count[c], s = start[c];
+    const int* src = unsorted + s;
+    if (cnt <= kSortSeg) {
+      for (int p = lane; p < cnt; p += kWarp) buf[p] = src[p];
+      __syncwarp();
+      src = buf;
+    }
+    for (int p = lane; p < cnt; p += kWarp) {
+      const int v = src[p];
+      int r = 0;
+      for (int q = 0; q < cnt; ++q) r += src[q] < v;  // atom indices are distinct
+      perm[s + r] = v;
+    }
+    __syncwarp();
+  }
+}
+
 SymArgs sym_args(int n) {
   SymArgs a{};
   a.n = n;
@@ -470,12 +634,26 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
   a.dEdq = ctx->d_dEdq_fx;
   a.energy = ctx->d_energy_fx;
   a.tile_box = ctx->d_tile_box;
+  a.perm = nullptr;
   const int wpb = kSymThreads / kWarp;
   const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
   cudaStream_t st = ctx->stream;
   cudaMemsetAsync(ctx->d_energy_fx, 0, sizeof(unsigned long long), st);
   if (a.cutoff2 > 0) {
-    tile_box_kernel<<<(a.ntiles + wpb - 1) / wpb, kSymThreads, 0, st>>>(pos, a.n, a.ntiles, ctx->d_tile_box);
+    // spatial order, then tile boxes over it
+    const int n = a.n, nb = (n + 255) / 256;
+    SortGeom* sg = reinterpret_cast<SortGeom*>(ctx->d_sgeom);
+    sort_geom_kernel<<<1, kBoxThreads, 0, st>>>(pos, n, sg);
+    cudaMemsetAsync(ctx->d_scount, 0, sizeof(int) * kMaxSortCells, st);
+    sort_count_kernel<<<nb, 256, 0, st>>>(pos, n, sg, ctx->d_cell_of, ctx->d_scount);
+    sort_scan_kernel<<<1, kBoxThreads, 0, st>>>(ctx->d_scount, sg, ctx->d_sstart, ctx->d_scursor);
+    sort_scatter_kernel<<<nb, 256, 0, st>>>(ctx->d_cell_of, n, ctx->d_sstart, ctx->d_scursor, ctx->d_perm_tmp);
+    sort_cells_by_atom_kernel<<<152 * 8, kSymThreads, 0, st>>>(ctx->d_scount, ctx->d_sstart, sg, ctx->d_perm_tmp,
+                                                               ctx->d_perm);
+    ctx->launches += 5;
+    a.perm = ctx->d_perm;
+    tile_box_kernel<<<(a.ntiles + wpb - 1) / wpb, kSymThreads, 0, st>>>(pos, ctx->d_perm, a.n, a.ntiles,
+                                                                        ctx->d_tile_box);
     ++ctx->launches;
     if (adjoint) {
       pair_sym_kernel<true, true><<<gu, kSymThreads, 0, st>>>(a);
