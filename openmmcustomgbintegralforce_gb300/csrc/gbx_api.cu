@@ -162,6 +162,8 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_energy_part, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_energy_fx, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_tile_box, 2 * (((size_t)n + 31) / 32)));
+  if (ctx->cfg.model != GBX_MODEL_GBSW)
+    GBX_TRY(dalloc(ctx, &ctx->d_pstate, (size_t)n * Q * (ctx->cfg.model == GBX_MODEL_GBMV1 ? 1 : 5)));
   if (ctx->cfg.cutoff > 0) {
     GBX_TRY(dalloc(ctx, &ctx->d_perm, n));
     GBX_TRY(dalloc(ctx, &ctx->d_perm_tmp, n));
@@ -615,7 +617,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
                   ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
-                  ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom};
+                  ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)

@@ -130,6 +130,7 @@ struct Context {
   int* d_sstart = nullptr;
   int* d_scursor = nullptr;
   int4* d_sgeom = nullptr;                    // cutoff: spatial grid geometry
+  float* d_pstate = nullptr;                  // GBMV: per-point sums kept for the chain rule
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]

@@ -10,6 +10,8 @@
 // arithmetic of a symmetric tile scheme, but no j-side accumulators, no
 // shuffles and no per-tile atomics, and every per-atom sum runs in a fixed
 // sequential order.  Per-tile FP32 partial sums are folded into FP64.
+#include <algorithm>
+
 #include "gbx_internal.cuh"
 
 namespace gbx {
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
 // ---------------------------------------------------------------------------
 constexpr int kNI = 4;          // i-atoms per lane
 constexpr int kSymI = kWarp * kNI;  // atoms per i-block (one warp)
-constexpr int kSymChunk = 16;   // j-tiles per warp unit
+constexpr int kSymChunkMax = 16;  // j-tiles per warp unit, at most
 constexpr int kSymThreads = 128;
 
 struct SymArgs {
@@ -160,6 +162,7 @@ struct SymArgs {
   const float4* tile_box;      // cutoff: [2 * ntiles] (lower, upper) corner of each 32-atom tile
   const int* perm;             // cutoff: slot k holds atom perm[k] (spatial order); nullptr: identity
   int nblocks, ntiles, chunks;
+  int chunk;  // j-tiles per warp unit
 };
 
 struct PAtom {
@@ -313,8 +316,8 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
   const int lane = threadIdx.x % kWarp;
   if (unit >= a.nblocks * a.chunks) return;
   const int b = unit / a.chunks, ch = unit % a.chunks;
-  const int jt0 = kNI * b + kNI + ch * kSymChunk;
-  const int jt1 = min(a.ntiles, jt0 + kSymChunk);
+  const int jt0 = kNI * b + kNI + ch * a.chunk;
+  const int jt1 = min(a.ntiles, jt0 + a.chunk);
   double E = 0.0;
   if (jt0 < jt1) {
     PAtom I[kNI];
@@ -578,7 +581,11 @@ SymArgs sym_args(int n) {
   a.n = n;
   a.nblocks = (n + kSymI - 1) / kSymI;
   a.ntiles = (n + kWarp - 1) / kWarp;
-  a.chunks = (a.ntiles + kSymChunk - 1) / kSymChunk;
+  // j-tiles per unit: long runs amortise the i-block setup, but small
+  // systems need short ones to give ~8k working warps
+  const long long visits = (long long)a.nblocks * a.ntiles / 2;
+  a.chunk = (int)std::max(2LL, std::min((long long)kSymChunkMax, visits / 8192));
+  a.chunks = (a.ntiles + a.chunk - 1) / a.chunk;
   return a;
 }
 

@@ -275,11 +275,41 @@ __device__ __forceinline__ float solvent_fraction(const ModelConst& m, const Ent
 // ---------------------------------------------------------------------------
 // Integral kernel: J4 = sum w/r^2 s, J7 = sum w/r^5 s per (atom, chunk).
 // ---------------------------------------------------------------------------
+// GBMV point state kept for the chain rule (saves it re-summing every list):
+// GBMV-I S at state[i Q + q]; GBMV-II s1, s2, vx, vy, vz in five planes of N Q.
+template <int MODEL, class W>
+__device__ __forceinline__ float gbmv_fraction_keep(const ModelConst& m, const Entries& t, long long cell,
+                                                    const float4 xi, const float4 v, W& wk, float* state,
+                                                    size_t idx, size_t plane) {
+  int cnt = 0, s = 0;
+  if (cell >= 0) {
+    const int2 cs = __ldg(t.cell + cell);
+    cnt = cs.x;
+    s = cs.y;
+  }
+  float p;
+  if constexpr (MODEL == GBX_MODEL_GBMV1) {
+    const float S = gbmv1_sum(t.e + s, cnt, xi, v, wk);
+    state[idx] = S;
+    return logistic_solvent(m.beta, m.lambda, S, p);
+  } else {
+    if (cnt == 0) return 1.0f;  // empty list: V = 0 (GBMVIntegralTypeII.cpp:140)
+    const Gbmv2State st = gbmv2_sums(t.e + s, t.par + s, cnt, xi, v, wk);
+    state[idx] = st.s1;
+    state[idx + plane] = st.s2;
+    state[idx + 2 * plane] = st.vx;
+    state[idx + 3 * plane] = st.vy;
+    state[idx + 4 * plane] = st.vz;
+    return logistic_solvent(m.beta, m.lambda, gbmv2_S(m, st), p);
+  }
+}
+
 template <int MODEL, class Q, bool COUNT>
 __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                             Quad quad, ModelConst m, int chunk, int n_chunks,
                                                             float* __restrict__ Jpart,
-                                                            unsigned long long* __restrict__ work) {
+                                                            unsigned long long* __restrict__ work,
+                                                            float* __restrict__ state) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (warp >= n * n_chunks) return;
@@ -294,7 +324,12 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
     const float4 v = quad.qv[q];
     const float2 w = quad.qw[q];
     const long long cell = query.cell(xi, v, q);
-    const float s = solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
+    float s;
+    if constexpr (MODEL != GBX_MODEL_GBSW)
+      s = state ? gbmv_fraction_keep<MODEL>(m, tab, cell, xi, v, wk, state, (size_t)i * m.nq + q, (size_t)n * m.nq)
+                : solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
+    else
+      s = solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
     if constexpr (COUNT) count_chain_work<MODEL>(m, tab, cell, xi, v, wk);
     J4 = fmaf(w.x, s, J4);
     J7 = fmaf(w.y, s, J7);
@@ -369,19 +404,16 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
                                                                  Quad quad, ModelConst m, int chunk, int n_chunks,
                                                                  float* __restrict__ Jpart, ShellSink sink) {
   __shared__ int3 s_queue[kThreads / kWarp][kStage];  // (q, list start, list length)
-  __shared__ int s_fill[kThreads / kWarp];
   __shared__ int s_long[kThreads / kWarp];  // a shaping entry beyond list position 63
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
   const unsigned lt = (1u << lane) - 1u;
-  if (lane == 0) {
-    s_fill[wib] = 0;
-    s_long[wib] = 0;
-  }
+  if (lane == 0) s_long[wib] = 0;
   __syncwarp();
   if (warp >= n * n_chunks) return;
   int3* queue = s_queue[wib];
+  int fill = 0;  // warp-uniform: points recorded so far (may exceed R)
   const int i = warp % n, c = warp / n;
   int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
   const float4 xi = pos[i];
@@ -471,11 +503,17 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
         J4 = fmaf(w.x, V, J4);
         J7 = fmaf(w.y, V, J7);
         has = false;
-        if (EMIT && shaped != 0ull && V != 0.0f) {
-          const int slot = atomicAdd(&s_fill[wib], 1);  // any order: the chain rule's sums do not depend on it
+      }
+      if (EMIT) {
+        // slots in finishing order (the chain rule's sums do not depend on it)
+        const bool emit = fin && shaped != 0ull && V != 0.0f;
+        const unsigned em = __ballot_sync(0xffffffffu, emit);
+        if (emit) {
+          const int slot = fill + __popc(em & lt);
           if (slot < sink.R)
             __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
         }
+        fill += __popc(em);
       }
     }
     __syncwarp();  // the next stage rewrites the queue
@@ -485,7 +523,6 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
     J7 += __shfl_xor_sync(0xffffffffu, J7, off);
   }
   __syncwarp();
-  const int fill = s_fill[wib];
   if (lane == 0) {
     Jpart[(size_t)c * n + i] = J4;
     Jpart[((size_t)n_chunks + c) * n + i] = J7;
@@ -518,6 +555,7 @@ struct ChainRecords {
   const int4* rec;  // (q, V, mask low, mask high) per recorded point
   const int* count;
   int R;
+  const float* state;  // GBMV point state of the integral pass (nullptr: re-sum the lists)
 };
 
 // A component whose fixed-point value is 0 (|g| < 2^-33, common for distant
@@ -664,7 +702,8 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
       } else if (MODEL == GBX_MODEL_GBMV1) {
         Work<false> wk;
         float p;
-        logistic_solvent(m.beta, m.lambda, gbmv1_sum(E, cnt, xi, v, wk), p);
+        const float Ssum = rr.state ? rr.state[(size_t)i * m.nq + q] : gbmv1_sum(E, cnt, xi, v, wk);
+        logistic_solvent(m.beta, m.lambda, Ssum, p);
         const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
         if (cS == 0.0f) continue;
         for (int l = 0; l < cnt; ++l) {
@@ -685,7 +724,14 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         }
       } else {
         Work<false> wk;
-        const Gbmv2State st = gbmv2_sums(E, tab.par + s, cnt, xi, v, wk);
+        Gbmv2State st;
+        if (rr.state) {
+          const size_t idx = (size_t)i * m.nq + q, plane = (size_t)n * m.nq;
+          st = Gbmv2State{rr.state[idx], rr.state[idx + plane], rr.state[idx + 2 * plane], rr.state[idx + 3 * plane],
+                          rr.state[idx + 4 * plane]};
+        } else {
+          st = gbmv2_sums(E, tab.par + s, cnt, xi, v, wk);
+        }
         const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
         float p;
         logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
@@ -763,10 +809,10 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
   else if (count_work)
     integral_kernel<MODEL, Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
-        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work);
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work, ctx->d_pstate);
   else
     integral_kernel<MODEL, Q, false><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
-        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, nullptr);
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, nullptr, ctx->d_pstate);
   ++ctx->launches;
 }
 
@@ -777,7 +823,8 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
   ChainOut o{force, stride, ctx->d_dEdR_fx, m.cutoff_chain_quirk && m.cutoff2 > 0.0f, m.cutoff2};
   const bool records = MODEL == GBX_MODEL_GBSW && !ADJ && ctx->records;
-  const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R};
+  const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R,
+                        MODEL == GBX_MODEL_GBSW ? nullptr : ctx->d_pstate};
   chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
                                                                                 ctx->n_chunks, ctx->d_dEdJ, o, rr);
   ++ctx->launches;
