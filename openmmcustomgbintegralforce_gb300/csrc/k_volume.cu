@@ -706,6 +706,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         logistic_solvent(m.beta, m.lambda, Ssum, p);
         const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
         if (cS == 0.0f) continue;
+        float px = 0.f, py = 0.f, pz = 0.f;
         for (int l = 0; l < cnt; ++l) {
           const float4 a = __ldg(E + l);
           const float3 d = delta(a, xi, v);
@@ -718,10 +719,14 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           const float gs = cS * 4.0f * a.w * e * r2;  // dS/d(delta) = 4 gamma e r^2 delta
           const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
           push_force(out, k, gx, gy, gz);
-          fix += float_to_fixed(gx);
-          fiy += float_to_fixed(gy);
-          fiz += float_to_fixed(gz);
+          px += gx;
+          py += gy;
+          pz += gz;
         }
+        // the point's pull on its own atom: summed in FP32 over the list, then fixed point
+        fix += float_to_fixed(px);
+        fiy += float_to_fixed(py);
+        fiz += float_to_fixed(pz);
       } else {
         Work<false> wk;
         Gbmv2State st;
@@ -741,6 +746,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const float t1 = st.s2 * inv3;                  // d s1 term
         const float t2 = st.s1 * inv3;                  // d s2 term
         const float t3 = -st.s1 * st.s2 * inv3 * inv3;  // d s3^2 term
+        float px = 0.f, py = 0.f, pz = 0.f;
         for (int l = 0; l < cnt; ++l) {
           const float4 a = __ldg(E + l);
           const float2 pk = __ldg(tab.par + s + l);
@@ -765,10 +771,13 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           const float gy = cS * fmaf(sc, d.y, t3 * 2.0f * F * st.vy);
           const float gz = cS * fmaf(sc, d.z, t3 * 2.0f * F * st.vz);
           push_force(out, k, gx, gy, gz);
-          fix += float_to_fixed(gx);
-          fiy += float_to_fixed(gy);
-          fiz += float_to_fixed(gz);
+          px += gx;
+          py += gy;
+          pz += gz;
         }
+        fix += float_to_fixed(px);
+        fiy += float_to_fixed(py);
+        fiz += float_to_fixed(pz);
       }
     }
   }
