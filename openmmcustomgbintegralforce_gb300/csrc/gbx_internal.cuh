@@ -177,6 +177,16 @@ struct Context {
 // FP64 route without touching the (slow) FP64 pipe.
 __device__ __forceinline__ long long float_to_fixed(float v) { return __float2ll_rn(v * 4294967296.0f); }
 
+// The same integer from two 32-bit conversions (|v| < 2^31): v = floor(v) + r
+// exactly, and round(v 2^32) = floor(v) 2^32 + round(r 2^32) because
+// floor(v) 2^32 is even (ties round the same way); r 2^32 < 2^32 - 2^8.
+// Cheaper where conversions dominate (the chain rule's force pushes).
+__device__ __forceinline__ long long float_to_fixed_split(float v) {
+  const float hf = floorf(v);
+  const unsigned lo = __float2uint_rn((v - hf) * 4294967296.0f);
+  return (long long)(((unsigned long long)(long long)__float2int_rz(hf) << 32) + lo);
+}
+
 __device__ __forceinline__ void red_add_fixed(unsigned long long* addr, float v) {
   atomicAdd(addr, (unsigned long long)float_to_fixed(v));
 }

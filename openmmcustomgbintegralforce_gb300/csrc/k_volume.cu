@@ -562,7 +562,7 @@ struct ChainRecords {
 // GBMV atoms) changes nothing: its reduction is skipped, the result is the
 // same bits.
 __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, float gy, float gz) {
-  const long long fx = float_to_fixed(-gx), fy = float_to_fixed(-gy), fz = float_to_fixed(-gz);
+  const long long fx = float_to_fixed_split(-gx), fy = float_to_fixed_split(-gy), fz = float_to_fixed_split(-gz);
   if (fx) atomicAdd(&o.force[k], (unsigned long long)fx);
   if (fy) atomicAdd(&o.force[k + o.stride], (unsigned long long)fy);
   if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
