@@ -793,6 +793,129 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   }
 }
 
+// GBMV chain rule with the warp cooperating on one point at a time: the
+// point's sums come from the integral pass, lanes read consecutive entries of
+// its list (coalesced; GBMV visits whole lists of nearly equal length), push
+// their atom's force and accumulate the point's pull on atom i.  Lanes first
+// take 32 points' cells together, then the warp walks those points in turn.
+template <int MODEL, class Q, bool ADJ>
+__global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
+                                                              Quad quad, ModelConst m, int chunk, int n_chunks,
+                                                              const float2* __restrict__ dEdJ, ChainOut out,
+                                                              const float* __restrict__ state) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (warp >= n * n_chunks) return;
+  const int i = warp % n, c = warp / n;
+  const float4 xi = pos[i];
+  const float2 de = dEdJ[i];
+  Q query;
+  query.init(*tab.geom, xi, quad.qoff);
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  const size_t plane = (size_t)n * m.nq;
+  long long fix = 0, fiy = 0, fiz = 0;
+  for (int base = q0; base < q1; base += kWarp) {
+    const int qm = base + lane;
+    float4 vm = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cntm = 0, sm = 0;
+    float cqm = 0.0f;
+    if (qm < q1) {
+      vm = quad.qv[qm];
+      const float2 w = quad.qw[qm];
+      cqm = fmaf(de.x, w.x, de.y * w.y);
+      const long long cell = query.cell(xi, vm, qm);
+      if (cell >= 0) {
+        const int2 cs = __ldg(tab.cell + cell);
+        cntm = cs.x;
+        sm = cs.y;
+      }
+    }
+    float px = 0.f, py = 0.f, pz = 0.f;  // this lane's share of the points' pull on atom i
+    const int np = min(kWarp, q1 - base);
+    for (int t = 0; t < np; ++t) {
+      const int cnt = __shfl_sync(0xffffffffu, cntm, t), s = __shfl_sync(0xffffffffu, sm, t);
+      const float cq = __shfl_sync(0xffffffffu, cqm, t);
+      if (cnt <= 0 || cq == 0.0f) continue;
+      const float4 v = make_float4(__shfl_sync(0xffffffffu, vm.x, t), __shfl_sync(0xffffffffu, vm.y, t),
+                                   __shfl_sync(0xffffffffu, vm.z, t), 0.f);
+      const size_t idx = (size_t)i * m.nq + base + t;
+      float p;
+      if constexpr (MODEL == GBX_MODEL_GBMV1) {
+        logistic_solvent(m.beta, m.lambda, state[idx], p);
+        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
+        if (cS == 0.0f) continue;
+        for (int l = lane; l < cnt; l += kWarp) {
+          const float4 a = __ldg(tab.e + s + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float r4 = r2 * r2;
+          const float e = __expf(a.w * r4);
+          const int k = __ldg(tab.index + s + l);
+          if (ADJ) red_add_fixed(&out.dEdR[k], cS * e * r4 * (-4.0f * a.w / __ldg(&tab.par[s + l].x)));
+          if (k == i) continue;
+          const float gs = cS * 4.0f * a.w * e * r2;  // dS/d(delta) = 4 gamma e r^2 delta
+          const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
+          push_force(out, k, gx, gy, gz);
+          px += gx;
+          py += gy;
+          pz += gz;
+        }
+      } else {
+        const Gbmv2State st{state[idx], state[idx + plane], state[idx + 2 * plane], state[idx + 3 * plane],
+                            state[idx + 4 * plane]};
+        const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
+        logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
+        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p)) * m.s0;
+        if (cS == 0.0f) continue;
+        const float inv3 = 1.0f / s3sq;
+        const float t1 = st.s2 * inv3;                  // d s1 term
+        const float t2 = st.s1 * inv3;                  // d s2 term
+        const float t3 = -st.s1 * st.s2 * inv3 * inv3;  // d s3^2 term
+        for (int l = lane; l < cnt; l += kWarp) {
+          const float4 a = __ldg(tab.e + s + l);
+          const float2 pk = __ldg(tab.par + s + l);
+          const float3 d = delta(a, xi, v);
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          const float T = fmaf(100.0f, r2, pk.x);
+          const float CT = __fdividef(a.w, T);
+          const float F = CT * CT;
+          const float dFf = -400.0f * F * __fdividef(1.0f, T);  // dF/d(delta) = dFf delta
+          const float vd = st.vx * d.x + st.vy * d.y + st.vz * d.z;
+          const int k = __ldg(tab.index + s + l);
+          if (ADJ) {
+            const float R = pk.y;
+            const float Cp = 10.0f * m.p1, Tp = Cp - 200.0f * R;
+            const float dFdR = 2.0f * CT * __fdividef(Cp * T - a.w * Tp, T * T);
+            red_add_fixed(&out.dEdR[k], cS * (t1 * dFdR + t2 * (r2 * 2.0f * F * dFdR) + t3 * (2.0f * vd * dFdR)));
+          }
+          if (k == i) continue;
+          const float sc = t1 * dFf + t2 * 2.0f * F * fmaf(dFf, r2, F) + t3 * 2.0f * vd * dFf;
+          const float gx = cS * fmaf(sc, d.x, t3 * 2.0f * F * st.vx);
+          const float gy = cS * fmaf(sc, d.y, t3 * 2.0f * F * st.vy);
+          const float gz = cS * fmaf(sc, d.z, t3 * 2.0f * F * st.vz);
+          push_force(out, k, gx, gy, gz);
+          px += gx;
+          py += gy;
+          pz += gz;
+        }
+      }
+    }
+    fix += float_to_fixed(px);
+    fiy += float_to_fixed(py);
+    fiz += float_to_fixed(pz);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    fix += __shfl_xor_sync(0xffffffffu, fix, off);
+    fiy += __shfl_xor_sync(0xffffffffu, fiy, off);
+    fiz += __shfl_xor_sync(0xffffffffu, fiz, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&out.force[i], (unsigned long long)fix);
+    atomicAdd(&out.force[i + out.stride], (unsigned long long)fiy);
+    atomicAdd(&out.force[i + 2 * out.stride], (unsigned long long)fiz);
+  }
+}
+
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
     return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex};
@@ -834,8 +957,16 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const bool records = MODEL == GBX_MODEL_GBSW && !ADJ && ctx->records;
   const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R,
                         MODEL == GBX_MODEL_GBSW ? nullptr : ctx->d_pstate};
-  chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
-                                                                                ctx->n_chunks, ctx->d_dEdJ, o, rr);
+  bool coop = false;
+  if constexpr (MODEL != GBX_MODEL_GBSW) {
+    coop = ctx->d_pstate != nullptr;
+    if (coop)
+      gbmv_chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
+          pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_dEdJ, o, ctx->d_pstate);
+  }
+  if (!coop)
+    chain_kernel<MODEL, Q, ADJ><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk,
+                                                                                  ctx->n_chunks, ctx->d_dEdJ, o, rr);
   ++ctx->launches;
 }
 
