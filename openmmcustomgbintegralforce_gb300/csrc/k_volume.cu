@@ -389,15 +389,19 @@ __device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const i
   return a.x == xi.x && a.y == xi.y && a.z == xi.z && __ldg(index + l) == i;
 }
 
-// GBSW integrals with lanes refilled from a queue.  A warp classifies a
-// stage of kStage points at once (empty cell: V = 1; buried cell: V = 0) and
-// queues the points that have a list; then every lane evaluates one list
-// entry per iteration and takes the next queued point as soon as its own is
-// finished, so a long list keeps one lane busy instead of the whole warp
-// waiting on it.  The walk per point is the sequential one of gbsw_volume
+// GBSW integrals with lanes refilled from a ring queue.  A warp classifies
+// kRefill points at a time (empty cell: V = 1; buried cell: V = 0) and queues
+// the points that have a list whenever fewer than kRefillBelow are pending;
+// every lane evaluates list entries of its own point and takes the next
+// queued point as soon as its own is finished, so a long list keeps one lane
+// busy instead of the whole warp waiting on it, and lanes idle only at the
+// end of the warp's quadrature range.  The walk per point is the sequential one of gbsw_volume
 // (same order, same early exit).  J is summed in an order fixed by the input
 // alone, so runs are bit-reproducible.
-constexpr int kStage = 256;
+constexpr int kStage = 256;        // ring entries per warp (a power of two)
+constexpr int kRefill = 128;       // points classified per refill
+constexpr int kRefillBelow = 64;   // refill when fewer entries are pending
+static_assert(kRefillBelow - 1 + kRefill <= kStage, "ring overwrite");
 
 template <class Q, bool EMIT>
 __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
@@ -421,102 +425,108 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   query.init(*tab.geom, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
-  for (int base = q0; base < q1; base += kStage) {
-    int nq = 0;  // warp-uniform queue length
+  int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
+  int next = q0;           // warp-uniform: first point not yet classified
+  int q = 0, s = 0, cnt = 0, l = 0;
+  float4 an = make_float4(0.f, 0.f, 0.f, 0.f), an2 = an;  // the next two list entries
+  bool has = false;
+  unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 w = make_float2(0.f, 0.f);
+  float V = 1.0f;
+  while (true) {
+    if (tail - head < kRefillBelow && next < q1) {
+      // classify the next kRefill points into the ring (at most
+      // kRefillBelow - 1 + kRefill entries are ever pending: no overwrite)
 #pragma unroll 4
-    for (int k = 0; k < kStage / kWarp; ++k) {
-      const int q = base + k * kWarp + lane;
-      int2 cs = make_int2(-1, 0);
-      if (q < q1) {
-        const float4 v = quad.qv[q];
-        const long long cell = query.cell(xi, v, q);
-        cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
-        if (cs.x == 0) {
-          const float2 w = quad.qw[q];
-          J4 += w.x;
-          J7 += w.y;
-        }
-      }
-      const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
-      if (cs.x > 0) queue[nq + __popc(qm & lt)] = make_int3(q, cs.y, cs.x);
-      nq += __popc(qm);
-    }
-    __syncwarp();
-    int head = 0, q = 0, s = 0, cnt = 0, l = 0;
-    float4 an = make_float4(0.f, 0.f, 0.f, 0.f), an2 = an;  // the next two list entries
-    bool has = false;
-    unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 w = make_float2(0.f, 0.f);
-    float V = 1.0f;
-    while (true) {
-      const unsigned need = __ballot_sync(0xffffffffu, !has);
-      if (!has) {
-        const int idx = head + __popc(need & lt);
-        if (idx < nq) {
-          const int3 e = queue[idx];
-          q = e.x;
-          s = e.y;
-          cnt = e.z;
-          l = 0;
-          shaped = 0;
-          V = 1.0f;
-          has = true;
-          v = quad.qv[q];
-          w = quad.qw[q];
-          an = __ldg(tab.e + s);
-          if (cnt > 1) an2 = __ldg(tab.e + s + 1);
-        }
-      }
-      head += __popc(need);
-      if (__ballot_sync(0xffffffffu, has) == 0u) break;
-      bool fin = false;
-      if (has) {
-        // two list entries per step (entries l and l + 1 were loaded one step ahead)
-        const float4 ea = an, eb = an2;
-        if (l + 2 < cnt) an = __ldg(tab.e + s + l + 2);
-        if (l + 3 < cnt) an2 = __ldg(tab.e + s + l + 3);
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          if (fin) break;
-          const float4 a = u == 0 ? ea : eb;
-          const float3 d = delta(a, xi, v);
-          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-          const float lo = a.w - m.sw, hi = a.w + m.sw;
-          if (r2 <= lo * lo) {
-            V = 0.0f;
-            fin = true;
-          } else {
-            if (r2 < hi * hi) {
-              const float dr = r2 * rsqrtf(r2) - a.w;
-              V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
-              if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
-                if (l < 64) shaped |= 1ull << l;
-                else s_long[wib] = 1;
-              }
-            }
-            fin = ++l == cnt;
+      for (int k = 0; k < kRefill / kWarp; ++k) {
+        const int qc = next + k * kWarp + lane;
+        int2 cs = make_int2(-1, 0);
+        if (qc < q1) {
+          const float4 vc = quad.qv[qc];
+          const long long cell = query.cell(xi, vc, qc);
+          cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
+          if (cs.x == 0) {
+            const float2 wc = quad.qw[qc];
+            J4 += wc.x;
+            J7 += wc.y;
           }
         }
+        const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
+        if (cs.x > 0) queue[(tail + __popc(qm & lt)) & (kStage - 1)] = make_int3(qc, cs.y, cs.x);
+        tail += __popc(qm);
       }
-      if (fin) {
-        J4 = fmaf(w.x, V, J4);
-        J7 = fmaf(w.y, V, J7);
-        has = false;
-      }
-      if (EMIT) {
-        // slots in finishing order (the chain rule's sums do not depend on it)
-        const bool emit = fin && shaped != 0ull && V != 0.0f;
-        const unsigned em = __ballot_sync(0xffffffffu, emit);
-        if (emit) {
-          const int slot = fill + __popc(em & lt);
-          if (slot < sink.R)
-            __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
-        }
-        fill += __popc(em);
+      next += kRefill;
+      __syncwarp();
+    }
+    const unsigned need = __ballot_sync(0xffffffffu, !has);
+    if (!has) {
+      const int idx = head + __popc(need & lt);
+      if (idx < tail) {
+        const int3 e = queue[idx & (kStage - 1)];
+        q = e.x;
+        s = e.y;
+        cnt = e.z;
+        l = 0;
+        shaped = 0;
+        V = 1.0f;
+        has = true;
+        v = quad.qv[q];
+        w = quad.qw[q];
+        an = __ldg(tab.e + s);
+        if (cnt > 1) an2 = __ldg(tab.e + s + 1);
       }
     }
-    __syncwarp();  // the next stage rewrites the queue
+    head = min(head + __popc(need), tail);
+    if (__ballot_sync(0xffffffffu, has) == 0u) {
+      if (next >= q1) break;
+      continue;
+    }
+    bool fin = false;
+    if (has) {
+      // two list entries per step (entries l and l + 1 were loaded one step ahead)
+      const float4 ea = an, eb = an2;
+      if (l + 2 < cnt) an = __ldg(tab.e + s + l + 2);
+      if (l + 3 < cnt) an2 = __ldg(tab.e + s + l + 3);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (fin) break;
+        const float4 a = u == 0 ? ea : eb;
+        const float3 d = delta(a, xi, v);
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        const float lo = a.w - m.sw, hi = a.w + m.sw;
+        if (r2 <= lo * lo) {
+          V = 0.0f;
+          fin = true;
+        } else {
+          if (r2 < hi * hi) {
+            const float dr = r2 * rsqrtf(r2) - a.w;
+            V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
+            if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
+              if (l < 64) shaped |= 1ull << l;
+              else s_long[wib] = 1;
+            }
+          }
+          fin = ++l == cnt;
+        }
+      }
+    }
+    if (fin) {
+      J4 = fmaf(w.x, V, J4);
+      J7 = fmaf(w.y, V, J7);
+      has = false;
+    }
+    if (EMIT) {
+      // slots in finishing order (the chain rule's sums do not depend on it)
+      const bool emit = fin && shaped != 0ull && V != 0.0f;
+      const unsigned em = __ballot_sync(0xffffffffu, emit);
+      if (emit) {
+        const int slot = fill + __popc(em & lt);
+        if (slot < sink.R)
+          __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
+      }
+      fill += __popc(em);
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     J4 += __shfl_xor_sync(0xffffffffu, J4, off);
