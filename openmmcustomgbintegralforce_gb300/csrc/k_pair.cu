@@ -229,6 +229,57 @@ __device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, fl
   }
 }
 
+// Two i atoms (the halves of each float2) against one j atom, in the packed
+// FP32x2 instructions: one issue slot does both halves' arithmetic, each half
+// rounded exactly as the scalar gb_pair rounds it.  The j side is summed as
+// +g d (the force on j, -g d, is its negation: exact) in two halves that are
+// added once per tile.  With a cutoff, a pair beyond it gets 1/f = 0, which
+// turns every one of its terms into a zero that leaves the sums unchanged.
+struct PAtom2 {
+  float2 nx, ny, nz;  // -x, -y, -z
+  float2 B, pq, kD, kB;
+};
+
+struct PAcc2 {
+  float2 fx, fy, fz, db, dq;
+};
+
+struct PJ2 {  // one j atom, broadcast to both halves
+  float2 x, y, z, q, B, invB, kB, pq;
+};
+
+__device__ __forceinline__ float2 bcast2(float v) { return make_float2(v, v); }
+
+template <bool CUTOFF, bool ADJ>
+__device__ __forceinline__ void gb_pair2(const PAtom2& I, const PJ2& J, float cutoff2, PAcc2& ai, PAcc2& aj,
+                                        float2& esum) {
+  const float2 dx = __fadd2_rn(J.x, I.nx), dy = __fadd2_rn(J.y, I.ny), dz = __fadd2_rn(J.z, I.nz);
+  const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+  const float2 arg = __fmul2_rn(r2, __fmul2_rn(I.kD, J.invB));
+  const float2 ex = make_float2(ex2_ftz(arg.x), ex2_ftz(arg.y));
+  const float2 f2 = __ffma2_rn(__fmul2_rn(I.B, J.B), ex, r2);
+  float2 invf = make_float2(rsqrt_ftz(f2.x), rsqrt_ftz(f2.y));
+  if (CUTOFF) {
+    if (r2.x > cutoff2) invf.x = 0.0f;
+    if (r2.y > cutoff2) invf.y = 0.0f;
+  }
+  const float2 e = __fmul2_rn(__fmul2_rn(I.pq, J.q), invf);
+  esum = __fadd2_rn(esum, e);
+  const float2 c = __fmul2_rn(__fmul2_rn(e, invf), invf);
+  const float2 g = __fmul2_rn(c, __ffma2_rn(bcast2(0.25f), ex, bcast2(-1.0f)));
+  ai.fx = __ffma2_rn(g, dx, ai.fx);
+  ai.fy = __ffma2_rn(g, dy, ai.fy);
+  ai.fz = __ffma2_rn(g, dz, ai.fz);
+  const float2 cex = __fmul2_rn(c, ex);
+  ai.db = __ffma2_rn(cex, __ffma2_rn(r2, I.kB, J.B), ai.db);
+  if (ADJ) ai.dq = __ffma2_rn(J.pq, invf, ai.dq);
+  aj.fx = __ffma2_rn(g, dx, aj.fx);
+  aj.fy = __ffma2_rn(g, dy, aj.fy);
+  aj.fz = __ffma2_rn(g, dz, aj.fz);
+  aj.db = __ffma2_rn(cex, __ffma2_rn(r2, J.kB, I.B), aj.db);
+  if (ADJ) aj.dq = __ffma2_rn(I.pq, invf, aj.dq);
+}
+
 struct PFixed {
   long long fx = 0, fy = 0, fz = 0, db = 0, dq = 0;
   __device__ __forceinline__ void add(const PAcc& v) {
@@ -249,20 +300,6 @@ __device__ __forceinline__ void push_atom(const SymArgs& a, int k, const PFixed&
   atomicAdd(&a.force[k + 2 * a.stride], (unsigned long long)f.fz);
   atomicAdd(&a.dEdB[k], (unsigned long long)f.db);
   if (ADJ) atomicAdd(&a.dEdq[k], (unsigned long long)f.dq);
-}
-
-__device__ __forceinline__ void rotate(PAtom& J, PAcc& aj, int src, bool adj) {
-  J.x = __shfl_sync(0xffffffffu, J.x, src);
-  J.y = __shfl_sync(0xffffffffu, J.y, src);
-  J.z = __shfl_sync(0xffffffffu, J.z, src);
-  J.q = __shfl_sync(0xffffffffu, J.q, src);
-  J.B = __shfl_sync(0xffffffffu, J.B, src);
-  J.invB = __shfl_sync(0xffffffffu, J.invB, src);
-  aj.fx = __shfl_sync(0xffffffffu, aj.fx, src);
-  aj.fy = __shfl_sync(0xffffffffu, aj.fy, src);
-  aj.fz = __shfl_sync(0xffffffffu, aj.fz, src);
-  aj.db = __shfl_sync(0xffffffffu, aj.db, src);
-  if (adj) aj.dq = __shfl_sync(0xffffffffu, aj.dq, src);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -310,8 +347,14 @@ __device__ __forceinline__ float box_gap2(const float4 alo, const float4 ahi, co
   return fmaf(gx, gx, fmaf(gy, gy, gz * gz));
 }
 
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
 template <bool CUTOFF, bool ADJ>
 __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
+  static_assert(kNI % 2 == 0, "i atoms are paired into float2 halves");
+  constexpr int kNH = kNI / 2;
   const int unit = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (unit >= a.nblocks * a.chunks) return;
@@ -320,14 +363,18 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
   const int jt1 = min(a.ntiles, jt0 + a.chunk);
   double E = 0.0;
   if (jt0 < jt1) {
-    PAtom I[kNI];
-    float pq[kNI], kD[kNI], kB[kNI];
+    PAtom2 I[kNH];  // half h, slot s: atom 128 b + 32 (2 h + s) + lane
 #pragma unroll
-    for (int u = 0; u < kNI; ++u) {
-      I[u] = load_patom(a, kSymI * b + kWarp * u + lane);
-      pq[u] = a.pref * I[u].q;
-      kD[u] = -0.25f * kLog2e * I[u].invB;
-      kB[u] = 0.25f * I[u].invB;
+    for (int h = 0; h < kNH; ++h) {
+      const PAtom p0 = load_patom(a, kSymI * b + kWarp * (2 * h) + lane);
+      const PAtom p1 = load_patom(a, kSymI * b + kWarp * (2 * h + 1) + lane);
+      I[h].nx = make_float2(-p0.x, -p1.x);
+      I[h].ny = make_float2(-p0.y, -p1.y);
+      I[h].nz = make_float2(-p0.z, -p1.z);
+      I[h].B = make_float2(p0.B, p1.B);
+      I[h].pq = make_float2(a.pref * p0.q, a.pref * p1.q);
+      I[h].kD = make_float2(-0.25f * kLog2e * p0.invB, -0.25f * kLog2e * p1.invB);
+      I[h].kB = make_float2(0.25f * p0.invB, 0.25f * p1.invB);
     }
     const int src = (lane + 1) % kWarp;
     float4 ilo = make_float4(0.f, 0.f, 0.f, 0.f), ihi = ilo;
@@ -345,24 +392,39 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
     for (int jt = jt0; jt < jt1; ++jt) {
       if (CUTOFF && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
       PAtom J = load_patom(a, kWarp * jt + lane);
-      PAcc ai[kNI], aj{0.f, 0.f, 0.f, 0.f, 0.f};
+      const float2 z2 = make_float2(0.f, 0.f);
+      PAcc2 ai[kNH], aj{z2, z2, z2, z2, z2};
 #pragma unroll
-      for (int u = 0; u < kNI; ++u) ai[u] = PAcc{0.f, 0.f, 0.f, 0.f, 0.f};
-      float et = 0.0f;
+      for (int h = 0; h < kNH; ++h) ai[h] = PAcc2{z2, z2, z2, z2, z2};
+      float2 et = z2;
 #pragma unroll 2
       for (int t = 0; t < kWarp; ++t) {
-        const float kBj = 0.25f * J.invB;
+        const PJ2 J2{bcast2(J.x), bcast2(J.y), bcast2(J.z), bcast2(J.q), bcast2(J.B), bcast2(J.invB),
+                     bcast2(0.25f * J.invB), bcast2(a.pref * J.q)};
 #pragma unroll
-        for (int u = 0; u < kNI; ++u)
-          gb_pair<true, CUTOFF, ADJ>(I[u], pq[u], kD[u], kB[u], J, kBj, a.pref, a.cutoff2, ai[u], aj, et);
-        rotate(J, aj, src, ADJ);
+        for (int h = 0; h < kNH; ++h) gb_pair2<CUTOFF, ADJ>(I[h], J2, a.cutoff2, ai[h], aj, et);
+        J.x = __shfl_sync(0xffffffffu, J.x, src);
+        J.y = __shfl_sync(0xffffffffu, J.y, src);
+        J.z = __shfl_sync(0xffffffffu, J.z, src);
+        J.q = __shfl_sync(0xffffffffu, J.q, src);
+        J.B = __shfl_sync(0xffffffffu, J.B, src);
+        J.invB = __shfl_sync(0xffffffffu, J.invB, src);
+        aj.fx = shfl2(aj.fx, src);
+        aj.fy = shfl2(aj.fy, src);
+        aj.fz = shfl2(aj.fz, src);
+        aj.db = shfl2(aj.db, src);
+        if (ADJ) aj.dq = shfl2(aj.dq, src);
       }
       PFixed sj;
-      sj.add(aj);
+      sj.add(PAcc{-(aj.fx.x + aj.fx.y), -(aj.fy.x + aj.fy.y), -(aj.fz.x + aj.fz.y), aj.db.x + aj.db.y,
+                  aj.dq.x + aj.dq.y});
       push_atom<ADJ>(a, kWarp * jt + lane, sj);
 #pragma unroll
-      for (int u = 0; u < kNI; ++u) si[u].add(ai[u]);
-      E += (double)et;
+      for (int h = 0; h < kNH; ++h) {
+        si[2 * h].add(PAcc{ai[h].fx.x, ai[h].fy.x, ai[h].fz.x, ai[h].db.x, ai[h].dq.x});
+        si[2 * h + 1].add(PAcc{ai[h].fx.y, ai[h].fy.y, ai[h].fz.y, ai[h].db.y, ai[h].dq.y});
+      }
+      E += (double)et.x + (double)et.y;
     }
 #pragma unroll
     for (int u = 0; u < kNI; ++u) push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, si[u]);
