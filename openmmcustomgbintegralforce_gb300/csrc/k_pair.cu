@@ -213,11 +213,11 @@ __device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, fl
   const float e = pqi * J.q * invf;
   esum += e;
   const float c = e * invf * invf;  // pref q_i q_j / f^3
-  const float g = c * fmaf(0.25f, ex, -1.0f);
+  const float cex = c * ex;
+  const float g = fmaf(0.25f, cex, -c);  // c (e^-D / 4 - 1)
   ai.fx = fmaf(g, dx, ai.fx);
   ai.fy = fmaf(g, dy, ai.fy);
   ai.fz = fmaf(g, dz, ai.fz);
-  const float cex = c * ex;
   ai.db = fmaf(cex, fmaf(r2, kBi, J.B), ai.db);
   if (ADJ) ai.dq = fmaf(pref * J.q, invf, ai.dq);
   if (SYM) {
@@ -231,8 +231,9 @@ __device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, fl
 
 // Two i atoms (the halves of each float2) against one j atom, in the packed
 // FP32x2 instructions: one issue slot does both halves' arithmetic, each half
-// rounded exactly as the scalar gb_pair rounds it.  The j side is summed as
-// +g d (the force on j, -g d, is its negation: exact) in two halves that are
+// rounded exactly as the scalar gb_pair rounds it.  Both sides are summed as
+// -g d (exact negations of the scalar form's terms): that is the force on j
+// as it stands and the force on i negated; the j side in two halves that are
 // added once per tile.  With a cutoff, a pair beyond it gets 1/f = 0, which
 // turns every one of its terms into a zero that leaves the sums unchanged.
 struct PAtom2 {
@@ -266,16 +267,16 @@ __device__ __forceinline__ void gb_pair2(const PAtom2& I, const PJ2& J, float cu
   const float2 e = __fmul2_rn(__fmul2_rn(I.pq, J.q), invf);
   esum = __fadd2_rn(esum, e);
   const float2 c = __fmul2_rn(__fmul2_rn(e, invf), invf);
-  const float2 g = __fmul2_rn(c, __ffma2_rn(bcast2(0.25f), ex, bcast2(-1.0f)));
-  ai.fx = __ffma2_rn(g, dx, ai.fx);
-  ai.fy = __ffma2_rn(g, dy, ai.fy);
-  ai.fz = __ffma2_rn(g, dz, ai.fz);
   const float2 cex = __fmul2_rn(c, ex);
+  const float2 gn = __ffma2_rn(bcast2(-0.25f), cex, c);  // -g = c (1 - e^-D / 4)
+  ai.fx = __ffma2_rn(gn, dx, ai.fx);
+  ai.fy = __ffma2_rn(gn, dy, ai.fy);
+  ai.fz = __ffma2_rn(gn, dz, ai.fz);
   ai.db = __ffma2_rn(cex, __ffma2_rn(r2, I.kB, J.B), ai.db);
   if (ADJ) ai.dq = __ffma2_rn(J.pq, invf, ai.dq);
-  aj.fx = __ffma2_rn(g, dx, aj.fx);
-  aj.fy = __ffma2_rn(g, dy, aj.fy);
-  aj.fz = __ffma2_rn(g, dz, aj.fz);
+  aj.fx = __ffma2_rn(gn, dx, aj.fx);
+  aj.fy = __ffma2_rn(gn, dy, aj.fy);
+  aj.fz = __ffma2_rn(gn, dz, aj.fz);
   aj.db = __ffma2_rn(cex, __ffma2_rn(r2, J.kB, I.B), aj.db);
   if (ADJ) aj.dq = __ffma2_rn(I.pq, invf, aj.dq);
 }
@@ -352,7 +353,9 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
 }
 
 template <bool CUTOFF, bool ADJ>
-__global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
+// The plain form is capped at 96 registers (five blocks per SM); the cutoff
+// and adjoint forms keep their wider register sets.
+__global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym_kernel(SymArgs a) {
   static_assert(kNI % 2 == 0, "i atoms are paired into float2 halves");
   constexpr int kNH = kNI / 2;
   const int unit = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
@@ -361,8 +364,15 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
   const int b = unit / a.chunks, ch = unit % a.chunks;
   const int jt0 = kNI * b + kNI + ch * a.chunk;
   const int jt1 = min(a.ntiles, jt0 + a.chunk);
+  // the i atoms' fixed-point sums, lane-private in shared memory (touched
+  // once per tile; in registers they would cost a quarter of the occupancy)
+  constexpr int kNF = ADJ ? 5 : 4;
+  __shared__ long long s_si[kSymThreads / kWarp][kNI * kNF][kWarp];
+  long long(*si)[kWarp] = s_si[threadIdx.x / kWarp];
   double E = 0.0;
   if (jt0 < jt1) {
+#pragma unroll
+    for (int f = 0; f < kNI * kNF; ++f) si[f][lane] = 0;
     PAtom2 I[kNH];  // half h, slot s: atom 128 b + 32 (2 h + s) + lane
 #pragma unroll
     for (int h = 0; h < kNH; ++h) {
@@ -388,7 +398,6 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
         ihi = make_float4(fmaxf(ihi.x, h.x), fmaxf(ihi.y, h.y), fmaxf(ihi.z, h.z), 0.f);
       }
     }
-    PFixed si[kNI];
     for (int jt = jt0; jt < jt1; ++jt) {
       if (CUTOFF && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
       PAtom J = load_patom(a, kWarp * jt + lane);
@@ -416,18 +425,30 @@ __global__ void __launch_bounds__(kSymThreads) pair_sym_kernel(SymArgs a) {
         if (ADJ) aj.dq = shfl2(aj.dq, src);
       }
       PFixed sj;
-      sj.add(PAcc{-(aj.fx.x + aj.fx.y), -(aj.fy.x + aj.fy.y), -(aj.fz.x + aj.fz.y), aj.db.x + aj.db.y,
-                  aj.dq.x + aj.dq.y});
+      sj.add(PAcc{aj.fx.x + aj.fx.y, aj.fy.x + aj.fy.y, aj.fz.x + aj.fz.y, aj.db.x + aj.db.y, aj.dq.x + aj.dq.y});
       push_atom<ADJ>(a, kWarp * jt + lane, sj);
 #pragma unroll
       for (int h = 0; h < kNH; ++h) {
-        si[2 * h].add(PAcc{ai[h].fx.x, ai[h].fy.x, ai[h].fz.x, ai[h].db.x, ai[h].dq.x});
-        si[2 * h + 1].add(PAcc{ai[h].fx.y, ai[h].fy.y, ai[h].fz.y, ai[h].db.y, ai[h].dq.y});
+        const float2 v[5] = {ai[h].fx, ai[h].fy, ai[h].fz, ai[h].db, ai[h].dq};
+#pragma unroll
+        for (int f = 0; f < kNF; ++f) {
+          const float sc = f < 3 ? -1.0f : f == 3 ? -0.5f : 1.0f;  // force: negated sums; dE/dB: -1/2 db
+          si[(2 * h) * kNF + f][lane] += float_to_fixed(sc * v[f].x);
+          si[(2 * h + 1) * kNF + f][lane] += float_to_fixed(sc * v[f].y);
+        }
       }
       E += (double)et.x + (double)et.y;
     }
 #pragma unroll
-    for (int u = 0; u < kNI; ++u) push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, si[u]);
+    for (int u = 0; u < kNI; ++u) {
+      PFixed su;
+      su.fx = si[u * kNF][lane];
+      su.fy = si[u * kNF + 1][lane];
+      su.fz = si[u * kNF + 2][lane];
+      su.db = si[u * kNF + 3][lane];
+      if (ADJ) su.dq = si[u * kNF + 4][lane];
+      push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, su);
+    }
   }
   E = warp_sum(E);
   if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
