@@ -825,35 +825,55 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
   const size_t plane = (size_t)n * m.nq;
   long long fix = 0, fiy = 0, fiz = 0;
   for (int base = q0; base < q1; base += kWarp) {
+    // lane t takes point base + t: its cell, its state (coalesced) and the
+    // point's factors of the chain rule, which the warp then broadcasts
     const int qm = base + lane;
     float4 vm = make_float4(0.f, 0.f, 0.f, 0.f);
     int cntm = 0, sm = 0;
-    float cqm = 0.0f;
+    float cSm = 0.0f;                    // c ds/dS (0: nothing to push)
+    float t1m = 0.f, t2m = 0.f, t3m = 0.f;  // GBMV-II: d s1, d s2, d s3^2 factors
+    float vxm = 0.f, vym = 0.f, vzm = 0.f;
     if (qm < q1) {
       vm = quad.qv[qm];
       const float2 w = quad.qw[qm];
-      cqm = fmaf(de.x, w.x, de.y * w.y);
+      const float cq = fmaf(de.x, w.x, de.y * w.y);
       const long long cell = query.cell(xi, vm, qm);
       if (cell >= 0) {
         const int2 cs = __ldg(tab.cell + cell);
         cntm = cs.x;
         sm = cs.y;
       }
+      if (cntm > 0 && cq != 0.0f) {
+        const size_t idx = (size_t)i * m.nq + qm;
+        float p;
+        if constexpr (MODEL == GBX_MODEL_GBMV1) {
+          logistic_solvent(m.beta, m.lambda, state[idx], p);
+          cSm = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));
+        } else {
+          const Gbmv2State st{state[idx], state[idx + plane], state[idx + 2 * plane], state[idx + 3 * plane],
+                              state[idx + 4 * plane]};
+          const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
+          logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
+          cSm = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p)) * m.s0;
+          const float inv3 = 1.0f / s3sq;
+          t1m = st.s2 * inv3;
+          t2m = st.s1 * inv3;
+          t3m = -st.s1 * st.s2 * inv3 * inv3;
+          vxm = st.vx;
+          vym = st.vy;
+          vzm = st.vz;
+        }
+      }
     }
     float px = 0.f, py = 0.f, pz = 0.f;  // this lane's share of the points' pull on atom i
     const int np = min(kWarp, q1 - base);
     for (int t = 0; t < np; ++t) {
       const int cnt = __shfl_sync(0xffffffffu, cntm, t), s = __shfl_sync(0xffffffffu, sm, t);
-      const float cq = __shfl_sync(0xffffffffu, cqm, t);
-      if (cnt <= 0 || cq == 0.0f) continue;
+      const float cS = __shfl_sync(0xffffffffu, cSm, t);
+      if (cnt <= 0 || cS == 0.0f) continue;
       const float4 v = make_float4(__shfl_sync(0xffffffffu, vm.x, t), __shfl_sync(0xffffffffu, vm.y, t),
                                    __shfl_sync(0xffffffffu, vm.z, t), 0.f);
-      const size_t idx = (size_t)i * m.nq + base + t;
-      float p;
       if constexpr (MODEL == GBX_MODEL_GBMV1) {
-        logistic_solvent(m.beta, m.lambda, state[idx], p);
-        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
-        if (cS == 0.0f) continue;
         for (int l = lane; l < cnt; l += kWarp) {
           const float4 a = __ldg(tab.e + s + l);
           const float3 d = delta(a, xi, v);
@@ -871,16 +891,10 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
           pz += gz;
         }
       } else {
-        const Gbmv2State st{state[idx], state[idx + plane], state[idx + 2 * plane], state[idx + 3 * plane],
-                            state[idx + 4 * plane]};
-        const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
-        logistic_solvent(m.beta, m.lambda, m.s0 * st.s1 * st.s2 / s3sq, p);
-        const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p)) * m.s0;
-        if (cS == 0.0f) continue;
-        const float inv3 = 1.0f / s3sq;
-        const float t1 = st.s2 * inv3;                  // d s1 term
-        const float t2 = st.s1 * inv3;                  // d s2 term
-        const float t3 = -st.s1 * st.s2 * inv3 * inv3;  // d s3^2 term
+        const float t1 = __shfl_sync(0xffffffffu, t1m, t), t2 = __shfl_sync(0xffffffffu, t2m, t),
+                    t3 = __shfl_sync(0xffffffffu, t3m, t);
+        const Gbmv2State st{0.f, 0.f, __shfl_sync(0xffffffffu, vxm, t), __shfl_sync(0xffffffffu, vym, t),
+                            __shfl_sync(0xffffffffu, vzm, t)};
         for (int l = lane; l < cnt; l += kWarp) {
           const float4 a = __ldg(tab.e + s + l);
           const float2 pk = __ldg(tab.par + s + l);
