@@ -359,6 +359,105 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
   }
 }
 
+// GBMV integrals with kGroup lanes per point: the group reads consecutive
+// entries of the point's list (kGroup x 16 contiguous bytes per load instead
+// of one line per lane), each lane sums every kGroup-th entry and the group
+// combines its partial sums by shuffles in a fixed order.  The point's sums
+// are kept for the chain rule as in integral_kernel.  Two lanes per point
+// measured fastest (GBMV-II, 10k atoms: 1.27 ms against 1.64 ms for one lane,
+// 1.47 ms for four and 2.0 ms for eight).
+constexpr int kGroup = 2;
+
+template <int MODEL, class Q>
+__global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
+                                                                 Quad quad, ModelConst m, int chunk, int n_chunks,
+                                                                 float* __restrict__ Jpart, float* __restrict__ state) {
+  constexpr int kPer = kWarp / kGroup;  // points per warp step
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  if (warp >= n * n_chunks) return;
+  const int i = warp % n, c = warp / n;
+  const int g = lane / kGroup, r = lane % kGroup;
+  const float4 xi = pos[i];
+  Q query;
+  query.init(*tab.geom, xi, quad.qoff);
+  const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  const size_t plane = (size_t)n * m.nq;
+  float J4 = 0.0f, J7 = 0.0f;
+  for (int base = q0; base < q1; base += kPer) {
+    const int q = base + g;
+    int cnt = 0, s = 0;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (q < q1) {
+      v = quad.qv[q];
+      const long long cell = query.cell(xi, v, q);
+      if (cell >= 0) {
+        const int2 cs = __ldg(tab.cell + cell);
+        cnt = cs.x;
+        s = cs.y;
+      }
+    }
+    float S1 = 0.f, S2 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f;
+    for (int l = r; l < cnt; l += kGroup) {
+      const float4 a = __ldg(tab.e + s + l);
+      const float3 d = delta(a, xi, v);
+      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      if constexpr (MODEL == GBX_MODEL_GBMV1) {
+        S1 += __expf(a.w * (r2 * r2));
+      } else {
+        float F = __fdividef(a.w, fmaf(100.0f, r2, __ldg(&tab.par[s + l].x)));
+        F = F * F;
+        S1 += F;
+        S2 = fmaf(r2, F * F, S2);
+        Vx = fmaf(d.x, F, Vx);
+        Vy = fmaf(d.y, F, Vy);
+        Vz = fmaf(d.z, F, Vz);
+      }
+    }
+#pragma unroll
+    for (int off = 1; off < kGroup; off <<= 1) {
+      S1 += __shfl_xor_sync(0xffffffffu, S1, off);
+      if constexpr (MODEL != GBX_MODEL_GBMV1) {
+        S2 += __shfl_xor_sync(0xffffffffu, S2, off);
+        Vx += __shfl_xor_sync(0xffffffffu, Vx, off);
+        Vy += __shfl_xor_sync(0xffffffffu, Vy, off);
+        Vz += __shfl_xor_sync(0xffffffffu, Vz, off);
+      }
+    }
+    if (r == 0 && q < q1) {
+      const size_t idx = (size_t)i * m.nq + q;
+      float p, sf;
+      if constexpr (MODEL == GBX_MODEL_GBMV1) {
+        if (state) state[idx] = S1;
+        sf = logistic_solvent(m.beta, m.lambda, S1, p);
+      } else if (cnt == 0) {
+        sf = 1.0f;  // empty list: V = 0 (GBMVIntegralTypeII.cpp:140)
+      } else {
+        const Gbmv2State st{S1, S2, Vx, Vy, Vz};
+        if (state) {
+          state[idx] = st.s1;
+          state[idx + plane] = st.s2;
+          state[idx + 2 * plane] = st.vx;
+          state[idx + 3 * plane] = st.vy;
+          state[idx + 4 * plane] = st.vz;
+        }
+        sf = logistic_solvent(m.beta, m.lambda, gbmv2_S(m, st), p);
+      }
+      const float2 w = quad.qw[q];
+      J4 = fmaf(w.x, sf, J4);
+      J7 = fmaf(w.y, sf, J7);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    J4 += __shfl_xor_sync(0xffffffffu, J4, off);
+    J7 += __shfl_xor_sync(0xffffffffu, J7, off);
+  }
+  if (lane == 0) {
+    Jpart[(size_t)c * n + i] = J4;
+    Jpart[((size_t)n_chunks + c) * n + i] = J7;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // GBSW integral pass that also records which points the chain rule needs:
 // (q, V, mask) for every point with V > 0 shaped by an atom other than i,
@@ -966,6 +1065,9 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   else if (count_work)
     integral_kernel<MODEL, Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work, ctx->d_pstate);
+  else if constexpr (MODEL != GBX_MODEL_GBSW)
+    gbmv_integral_kernel<MODEL, Q><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
+        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_pstate);
   else
     integral_kernel<MODEL, Q, false><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, nullptr, ctx->d_pstate);
