@@ -698,13 +698,16 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
     // recorded points, 32 at a time; lanes over their shaping entries
     const int4* region = rr.rec + (size_t)warp * rr.R;
+    int4 prn = make_int4(0, 0, 0, 0);  // the next batch's records, loaded one batch ahead
+    if (lane < npts) prn = __ldcs(region + lane);
     for (int b = 0; b < npts; b += kWarp) {
       unsigned mlo = 0u, mhi = 0u;
       int st = 0;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       float V = 0.0f, cq = 0.0f;
+      const int4 pr = prn;
+      if (b + kWarp + lane < npts) prn = __ldcs(region + b + kWarp + lane);
       if (b + lane < npts) {
-        const int4 pr = __ldcs(region + b + lane);
         V = __int_as_float(pr.y);
         mlo = (unsigned)pr.z;
         mhi = (unsigned)pr.w;
