@@ -55,14 +55,32 @@ FLOPS_POINT = 13.0
 # force on i and on the listed atom 6 -> +22 flops; per point as above.
 FLOPS_CHAIN_EVAL = 10.0
 FLOPS_CHAIN_SHELL = 22.0
+# GBMV-I per listed atom (GBMVIntegralTypeI.cpp:158-170): delta 3, r^2 5, r^4 1,
+# gamma r^4 1, sum 1 -> 11 flops + exp; chain (:196-222): delta 3, r^2 5,
+# r^4 and r^2 terms 2, exp arg 1, factor 4, times delta 3, force on i and on the
+# listed atom 6 -> 24 flops + exp.
+FLOPS_GBMV1_EVAL = 11.0
+FLOPS_GBMV1_CHAIN = 24.0
+# GBMV-II per listed atom (GBMVIntegralTypeII.cpp:163-191): delta 3, r^2 5,
+# T 2, F = (C/T)^2 1, s1 1, r^2 F^2 3, F delta 6 -> 21 flops + div; chain
+# (:221-282): delta 3, r^2 5, T 2, F 1, dF 3, v.delta 5, factor 9, gradient
+# 12, force on i and on the listed atom 6 -> 46 flops + 2 div.
+FLOPS_GBMV2_EVAL = 21.0
+FLOPS_GBMV2_CHAIN = 46.0
+# per point beyond FLOPS_POINT: GBMV-I logistic 4 + exp; GBMV-II S 7 +
+# logistic 4 + exp; chain factor per point 5
+FLOPS_GBMV_POINT = {1: 4.0, 2: 11.0}
+FLOPS_GBMV_CHAIN_POINT = 5.0
 # unique pair (CharmmReferenceGBSW.cpp:248-282): delta+r^2 8, D 3, exp arg 1,
 # f^2 2, 1/f^3 2, energy 3, dG/dr 4 + force 6, dG/dB 2x5 -> 39 flops + exp, rsqrt
 FLOPS_PAIR = 39.0
 
 
 # DRAM bytes (read + write) per launch of each stage's main kernel, from one ncu
-# capture of the same command (profiles/kernels_gbsw50k.md).
-TRAFFIC = {"gbsw50k": {"integrals": 854.3e6 + 573.5e6, "pair": 3.0e6, "chain_rule": 957.5e6 + 3.8e6}}
+# capture of the same workload (the files named in TRAFFIC_SOURCE).
+TRAFFIC = {"gbsw50k": {"integrals": 908.1e6 + 570.7e6, "pair": 3.11e6 + 0.05e6, "chain_rule": 956.8e6 + 0.14e6},
+           "gbmv10k": {"integrals": 129.6e6 + 213.8e6, "chain_rule": 318.0e6 + 6.2e6}}
+TRAFFIC_SOURCE = {"gbsw50k": "profiles/kernels_gbsw50k.md", "gbmv10k": "profiles/gbmv_kernels_gbmv10k.md"}
 
 
 def workloads():
@@ -438,21 +456,26 @@ def main():
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
     points = float(n) * model.n_quad
-    integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
-        FLOPS_POINT * points
-    pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
-    cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
-            "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12}
     if model.model == 0:
+        integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
+            FLOPS_POINT * points
         chain_flops = FLOPS_CHAIN_EVAL * work["chain_list_evals"] + FLOPS_CHAIN_SHELL * work["chain_derivative_evals"] + \
             FLOPS_POINT * points
-        cand["chain_rule"] = chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12
+    else:
+        ev, ch = (FLOPS_GBMV1_EVAL, FLOPS_GBMV1_CHAIN) if model.model == 1 else (FLOPS_GBMV2_EVAL, FLOPS_GBMV2_CHAIN)
+        integral_flops = ev * work["volume_evals"] + (FLOPS_POINT + FLOPS_GBMV_POINT[model.model]) * points
+        chain_flops = ch * work["chain_list_evals"] + (FLOPS_POINT + FLOPS_GBMV_CHAIN_POINT) * points
+    pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
+    cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
+            "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12,
+            "chain_rule": chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12}
     dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
     achieved = cand.get(dominant)
     roofline = {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": (achieved / fp32_peak) if achieved else None,
                 "traffic": TRAFFIC.get(args.workload, {}).get(dominant),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, profiles/kernels_gbsw50k.md",
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                   + TRAFFIC_SOURCE[args.workload]) if args.workload in TRAFFIC_SOURCE else None,
                 "peak_source": "nominal FP32 (152 SM x 128 lanes x 2 flop x max SM clock); "
                                f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
                 "per_stage_tflops": cand, "stage_ms": stage_ms,
