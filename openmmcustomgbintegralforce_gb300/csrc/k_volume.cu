@@ -489,8 +489,9 @@ __device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const i
 }
 
 // GBSW integrals with lanes refilled from a ring queue.  A warp classifies
-// kRefill points at a time (empty cell: V = 1; buried cell: V = 0) and queues
-// the points that have a list whenever fewer than kRefillBelow are pending;
+// kRefill points at a time (empty cell: V = 1; buried cell or buried by the
+// list's first entry: V = 0) and queues the points that have a list whenever
+// fewer than kRefillBelow are pending;
 // every lane evaluates list entries of its own point and takes the next
 // queued point as soon as its own is finished, so a long list keeps one lane
 // busy instead of the whole warp waiting on it, and lanes idle only at the
@@ -549,6 +550,14 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
             const float2 wc = quad.qw[qc];
             J4 += wc.x;
             J7 += wc.y;
+          } else if (cs.x > 0) {
+            // the list's first entry, the likeliest burying atom, buries most
+            // listed points: V = 0 adds nothing, the point is not queued
+            const float4 a0 = __ldg(tab.e + cs.y);
+            const float3 d = delta(a0, xi, vc);
+            const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+            const float lo = a0.w - m.sw;
+            if (r2 <= lo * lo) cs.x = -1;
           }
         }
         const unsigned qm = __ballot_sync(0xffffffffu, cs.x > 0);
