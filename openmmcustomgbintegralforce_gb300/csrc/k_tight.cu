@@ -32,6 +32,8 @@ namespace {
 constexpr int kGeomThreads = 1024;
 constexpr int kSortWarps = 4;
 constexpr int kSortBuf = 256;
+constexpr int kSortLanes = 8;                                   // lanes per short list
+constexpr int kSortSmall = kSortBuf / (kWarp / kSortLanes);     // longest short list (64)
 
 __global__ void __launch_bounds__(kGeomThreads) tight_geom_kernel(const float4* __restrict__ pos, int n, double h,
                                                                   double w, TableGeom* __restrict__ g,
@@ -208,7 +210,50 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
       cell[c] = make_int2(bur ? -1 : cnt, s);
       if (bur) count[c] = -1;
     }
-    unsigned todo = __ballot_sync(0xffffffffu, cnt > 0 && !bur);
+    // lists of up to kSortSmall entries: four cells at a time, eight lanes
+    // per cell, each group in its own quarter of the warp's buffer; longer
+    // lists: the whole warp on one cell
+    unsigned small = __ballot_sync(0xffffffffu, cnt > 0 && !bur && cnt <= kSortSmall);
+    unsigned todo = __ballot_sync(0xffffffffu, cnt > kSortSmall && !bur);
+    const int grp = lane / kSortLanes, gl = lane % kSortLanes;
+    while (small) {
+      unsigned t = small;
+      for (int k = 0; k < grp; ++k) t &= t - 1;  // the grp-th listed cell left
+      const int src = t ? __ffs(t) - 1 : -1;
+      for (int k = 0; k < kWarp / kSortLanes; ++k) small &= small - 1;
+      const int ccnt0 = __shfl_sync(0xffffffffu, cnt, src >= 0 ? src : 0);
+      const int cs = __shfl_sync(0xffffffffu, s, src >= 0 ? src : 0);
+      const int ccnt = src >= 0 ? ccnt0 : 0;
+      float4* ge = s_e[wib] + grp * kSortSmall;
+      int* gi = s_i[wib] + grp * kSortSmall;
+      float* gk = s_k[wib] + grp * kSortSmall;
+      if (ccnt > 0) {
+        const long long cc = c0 + src;
+        const int cx = (int)(cc / sx), cy = (int)((cc / g.dims[2]) % g.dims[1]), cz = (int)(cc % g.dims[2]);
+        const float ctr[3] = {cmin[0] + ((float)cx + 0.5f) * step, cmin[1] + ((float)cy + 0.5f) * step,
+                              cmin[2] + ((float)cz + 0.5f) * step};
+        for (int q = gl; q < ccnt; q += kSortLanes) {
+          const float4 e = entry[cs + q];
+          ge[q] = e;
+          gi[q] = index[cs + q];
+          const float dx = e.x - ctr[0], dy = e.y - ctr[1], dz = e.z - ctr[2];
+          gk[q] = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - (e.w - w);
+        }
+      }
+      __syncwarp();
+      for (int q = gl; q < ccnt; q += kSortLanes) {
+        const float kq = gk[q];
+        const int iq = gi[q];
+        int r = 0;
+        for (int o = 0; o < ccnt; ++o) {
+          const float ko = gk[o];
+          r += (ko < kq) || (ko == kq && gi[o] < iq);
+        }
+        entry[cs + r] = ge[q];
+        index[cs + r] = iq;
+      }
+      __syncwarp();
+    }
     while (todo) {
       const int src = __ffs(todo) - 1;
       todo &= todo - 1;
