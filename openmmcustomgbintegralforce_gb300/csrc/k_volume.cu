@@ -502,6 +502,7 @@ constexpr int kStage = 256;        // ring entries per warp (a power of two)
 constexpr int kRefill = 128;       // points classified per refill
 constexpr int kRefillBelow = 64;   // refill when fewer entries are pending
 static_assert(kRefillBelow - 1 + kRefill <= kStage, "ring overwrite");
+constexpr int kEnt = 2;            // list entries per lane step, loaded one step ahead (3 and 4 measured slower)
 
 template <class Q, bool EMIT>
 __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
@@ -528,7 +529,9 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
   int next = q0;           // warp-uniform: first point not yet classified
   int q = 0, s = 0, cnt = 0, l = 0;
-  float4 an = make_float4(0.f, 0.f, 0.f, 0.f), an2 = an;  // the next two list entries
+  float4 an[kEnt];  // the next kEnt list entries
+#pragma unroll
+  for (int u = 0; u < kEnt; ++u) an[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   bool has = false;
   unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
   float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -581,8 +584,9 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
         has = true;
         v = quad.qv[q];
         w = quad.qw[q];
-        an = __ldg(tab.e + s);
-        if (cnt > 1) an2 = __ldg(tab.e + s + 1);
+#pragma unroll
+        for (int u = 0; u < kEnt; ++u)
+          if (u < cnt) an[u] = __ldg(tab.e + s + u);
       }
     }
     head = min(head + __popc(need), tail);
@@ -592,14 +596,17 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
     }
     bool fin = false;
     if (has) {
-      // two list entries per step (entries l and l + 1 were loaded one step ahead)
-      const float4 ea = an, eb = an2;
-      if (l + 2 < cnt) an = __ldg(tab.e + s + l + 2);
-      if (l + 3 < cnt) an2 = __ldg(tab.e + s + l + 3);
+      // kEnt list entries per step (entries l .. l + kEnt - 1 were loaded one step ahead)
+      float4 cur[kEnt];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < kEnt; ++u) {
+        cur[u] = an[u];
+        if (l + kEnt + u < cnt) an[u] = __ldg(tab.e + s + l + kEnt + u);
+      }
+#pragma unroll
+      for (int u = 0; u < kEnt; ++u) {
         if (fin) break;
-        const float4 a = u == 0 ? ea : eb;
+        const float4 a = cur[u];
         const float3 d = delta(a, xi, v);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         const float lo = a.w - m.sw, hi = a.w + m.sw;
