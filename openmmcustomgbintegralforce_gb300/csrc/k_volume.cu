@@ -765,9 +765,9 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
         if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2)
           push_force(out, __ldg(tab.index + e), gx, gy, gz);
-        fix += float_to_fixed(gx);
-        fiy += float_to_fixed(gy);
-        fiz += float_to_fixed(gz);
+        fix += float_to_fixed_split(gx);
+        fiy += float_to_fixed_split(gy);
+        fiz += float_to_fixed_split(gz);
       }
     }
   } else {
@@ -823,9 +823,9 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
           const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
           if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2) push_force(out, k, gx, gy, gz);
-          fix += float_to_fixed(gx);
-          fiy += float_to_fixed(gy);
-          fiz += float_to_fixed(gz);
+          fix += float_to_fixed_split(gx);
+          fiy += float_to_fixed_split(gy);
+          fiz += float_to_fixed_split(gz);
         }
       } else if (MODEL == GBX_MODEL_GBMV1) {
         Work<false> wk;
