@@ -693,6 +693,24 @@ __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, f
   if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
 }
 
+// GBSW: the force -g on a shaping atom k (unless the cutoff quirk drops it)
+// and +g on atom i, as one fixed-point integer triple: atom i gets the
+// negation of what k gets, so the pair's momentum balances exactly and one
+// conversion serves both.
+__device__ __forceinline__ void push_shaping(const ChainOut& o, const int* __restrict__ index, bool push, float gx,
+                                             float gy, float gz, long long& fix, long long& fiy, long long& fiz) {
+  const long long fx = float_to_fixed_split(-gx), fy = float_to_fixed_split(-gy), fz = float_to_fixed_split(-gz);
+  if (push) {
+    const int k = __ldg(index);
+    if (fx) atomicAdd(&o.force[k], (unsigned long long)fx);
+    if (fy) atomicAdd(&o.force[k + o.stride], (unsigned long long)fy);
+    if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
+  }
+  fix -= fx;
+  fiy -= fy;
+  fiz -= fz;
+}
+
 template <int MODEL, class Q, bool ADJ>
 __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                          Quad quad, ModelConst m, int chunk, int n_chunks,
@@ -763,11 +781,8 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const float gs = ocq * g * rsqrtf(r2);
         const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
         const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
-        if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2)
-          push_force(out, __ldg(tab.index + e), gx, gy, gz);
-        fix += float_to_fixed_split(gx);
-        fiy += float_to_fixed_split(gy);
-        fiz += float_to_fixed_split(gz);
+        push_shaping(out, tab.index + e, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx, gy, gz,
+                     fix, fiy, fiz);
       }
     }
   } else {
@@ -822,10 +837,8 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           const float gs = cq * g * rsqrtf(r2);
           const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
           const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
-          if (!out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2) push_force(out, k, gx, gy, gz);
-          fix += float_to_fixed_split(gx);
-          fiy += float_to_fixed_split(gy);
-          fiz += float_to_fixed_split(gz);
+          push_shaping(out, tab.index + s + l, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx,
+                       gy, gz, fix, fiy, fiz);
         }
       } else if (MODEL == GBX_MODEL_GBMV1) {
         Work<false> wk;
