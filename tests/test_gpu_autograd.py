@@ -1,8 +1,9 @@
 """The differentiable form (torch.autograd.Function over the device adjoint)
 on a 5,000-atom GBSW globule: its gradients against the host adjoint of the
 same context, against the FP64 oracle's analytic adjoint, and against FP64
-central finite differences of the oracle energy on randomly chosen entries
-(h = 1e-4 A for positions, 1e-5 for charges, radii and coefficients)."""
+central finite differences of the oracle energy on 200 randomly chosen
+entries (h = 1e-4 A for positions, 1e-5 for charges, radii and
+coefficients)."""
 import numpy as np
 import pytest
 
@@ -56,6 +57,8 @@ def test_against_oracle_adjoint(case):
 
 
 def test_against_fp64_finite_differences(case):
+    """200 randomly chosen entries: 120 position components, 39 charges, 39
+    radii and the two coefficients."""
     g, m, _, _, grads = case
     orc = O.Oracle(m)
     rng = np.random.default_rng(9)
@@ -70,29 +73,34 @@ def test_against_fp64_finite_differences(case):
     F = grads["forces"]
     fs = float(np.sqrt((F ** 2).mean()))
     h = 1e-5  # nm (1e-4 A)
-    for _ in range(8):
-        i, d = int(rng.integers(g.n)), int(rng.integers(3))
+    checked = 0
+    for flat in rng.choice(3 * g.n, size=120, replace=False):
+        i, d = int(flat) // 3, int(flat) % 3
         xp, xm = g.positions.copy(), g.positions.copy()
         xp[i, d] += h
         xm[i, d] -= h
         close(-(E(pos=xp) - E(pos=xm)) / (2 * h), F[i, d], fs, f"F[{i},{d}]")
+        checked += 1
     h = 1e-5
     for key, which in (("dEdq", "q"), ("dEdR", "R")):
         an = grads[key]
         sc = float(np.sqrt((an ** 2).mean()))
-        for _ in range(5):
-            i = int(rng.integers(g.n))
+        for i in rng.choice(g.n, size=39, replace=False):
+            i = int(i)
             p = (g.charge if which == "q" else g.radius).astype(np.float64).copy()
             p[i] += h
             ep = E(q=p) if which == "q" else E(R=p)
             p[i] -= 2 * h
             em = E(q=p) if which == "q" else E(R=p)
             close((ep - em) / (2 * h), an[i], sc, f"{key}[{i}]")
+            checked += 1
     for k, name in enumerate(("alpha0", "alpha1")):
         base = getattr(m, name)
         ep = E(model=m.replace(**{name: base + h}))
         em = E(model=m.replace(**{name: base - h}))
         close((ep - em) / (2 * h), grads["dEdalpha"][k], abs(grads["dEdalpha"][k]), name)
+        checked += 1
+    assert checked == 200
 
 
 def test_fitting_step_moves_charges(case):
