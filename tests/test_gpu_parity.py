@@ -268,3 +268,23 @@ def test_device_buffers_match_host_path(glob1000):
     Fd = np.stack([fx[:g.n], fx[stride:stride + g.n], fx[2 * stride:2 * stride + g.n]], axis=1)
     assert float(energy.cpu()[0]) == E
     assert np.array_equal(Fd, F)
+
+
+@pytest.mark.parametrize("policy", ["exact_table", "reference_table"])
+def test_isolated_atom_known_answer(policy):
+    """Analytic pin on the device: isolated atoms' integrals and Born radii
+    equal the 1-D Gauss-Legendre sums of the switching polynomial
+    (tests/kat_isolated.py), whichever table the context integrates on."""
+    from tests.kat_isolated import expected_born, expected_integrals, isolated_system
+
+    m = GBModel.charmm_gbsw(reference_table=(policy == "reference_table"))
+    pos, radius = isolated_system([0.12, 0.17, 0.18])
+    ctx = Context(m, len(radius))
+    ctx.set_particle_parameters(np.full(len(radius), 0.1), radius)
+    ctx.execute_host(pos)
+    I4, I7 = expected_integrals(m, radius)
+    got = ctx.integrals()
+    assert np.abs(got[0] / I4 - 1).max() < 1e-6
+    assert np.abs(got[1] / I7 - 1).max() < 1e-6
+    assert np.abs(ctx.born_radii() / expected_born(m, I4, I7) - 1).max() < 1e-6
+    ctx.close()

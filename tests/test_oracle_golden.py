@@ -61,3 +61,22 @@ def test_integral_classes(n, tag):
     assert np.abs(I - g[f"{tag}_integrals"]).max() <= 1e-12 * np.abs(g[f"{tag}_integrals"]).max()
     F, _ = orc.integral_chain(g["positions"], g["radius"], g["dEdI"])
     assert rel_rms(F, g[f"{tag}_chain"]) < 1e-12
+
+
+def test_isolated_atom_known_answer():
+    """Analytic pin: isolated atoms, where the integrals are 1-D sums of the
+    switching polynomial over the radial nodes (tests/kat_isolated.py)."""
+    from tests.kat_isolated import continuous_integrals, expected_born, expected_integrals, isolated_system
+
+    m = GBModel.charmm_gbsw()
+    pos, radius = isolated_system([0.12, 0.17, 0.18])
+    out = O.Oracle(m).energy_forces(pos, np.zeros(len(radius)), radius)
+    I4, I7 = expected_integrals(m, radius)
+    assert np.abs(out["integrals"][0] / I4 - 1).max() < 1e-13
+    assert np.abs(out["integrals"][1] / I7 - 1).max() < 1e-13
+    assert np.abs(out["born"] / expected_born(m, I4, I7) - 1).max() < 1e-13
+    # the 24-node radial rule against the integral it approximates (the
+    # switching shell's kinks limit Gauss-Legendre to a few parts in 1e3)
+    for k, R in enumerate(radius):
+        c4, c7 = continuous_integrals(m, R)
+        assert abs(I4[k] / c4 - 1) < 2e-2 and abs(I7[k] / c7 - 1) < 2e-2
