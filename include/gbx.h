@@ -142,7 +142,10 @@ GBX_API gbx_status gbx_execute(gbx_context* ctx, const void* posq, unsigned long
                                int force_stride, double* energy, int flags, void* stream);
 
 /* Same computation on host arrays (Reference-platform style): positions
- * double[3n]; forces double[3n] ADDED to; *energy set.  Copies inside. */
+ * double[3n]; forces double[3n] ADDED to; *energy set.  Copies inside.  Once
+ * the lookup table's buffers are sized the call synchronises once, at the
+ * end; a table that outgrew them is detected there and the call runs again
+ * checked (the outputs are written once). */
 GBX_API gbx_status gbx_execute_host(gbx_context* ctx, const double* positions, double* forces, double* energy,
                                     int flags);
 

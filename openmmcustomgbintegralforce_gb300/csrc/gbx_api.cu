@@ -189,6 +189,8 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_force_fx, sizeof(unsigned long long) * 3 * n));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_rmax, sizeof(unsigned)));
   *ctx->h_rmax = 0;
+  GBX_CUDA(cudaMallocHost((void**)&ctx->h_status, sizeof(unsigned)));
+  GBX_CUDA(cudaMallocHost((void**)&ctx->h_energy, sizeof(double)));
   GBX_CUDA(cudaEventCreateWithFlags(&ctx->srec_ev, cudaEventDisableTiming));
   return GBX_OK;
 }
@@ -625,6 +627,8 @@ gbx_status gbx_destroy(gbx_context* handle) {
   if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
   if (ctx->h_force_fx) cudaFreeHost(ctx->h_force_fx);
   if (ctx->h_rmax) cudaFreeHost(ctx->h_rmax);
+  if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->h_energy) cudaFreeHost(ctx->h_energy);
   if (ctx->srec_ev) cudaEventDestroy(ctx->srec_ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -705,7 +709,7 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
 
 namespace {
 
-gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work) {
+gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work, bool check = true) {
   const int n = ctx->n;
   ctx->stream = ctx->own_stream;
   for (int i = 0; i < n; ++i)
@@ -714,18 +718,41 @@ gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool co
   GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));
   GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
   // d_pos holds the raw copy; staging rewrites it in place with the model parameter
-  return run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, true, adjoint, count_work);
+  return run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, check, adjoint, count_work);
 }
 
-gbx_status host_results(Context* ctx, double* forces, double* energy) {
+// The lookup table's buffers are sized: a host call can run unchecked and
+// read the status word with its results (one synchronisation instead of one
+// after the table build and one at the end).
+bool tables_sized(const Context* ctx) {
+  return ctx->use_tight ? ctx->tight_valid && ctx->tcell_cap > 0 && ctx->tentry_cap > 0
+                        : ctx->cell_cap > 0 && ctx->entry_cap > 0;
+}
+
+// Reads the call's results back.  With `optimistic` (an unchecked run) a table
+// that outgrew its buffers sets *rerun and leaves the outputs untouched: the
+// caller runs again checked, which grows the buffers.
+gbx_status host_results(Context* ctx, double* forces, double* energy, bool optimistic = false,
+                        bool* rerun = nullptr) {
   const int n = ctx->n;
+  if (rerun) *rerun = false;
   if (forces) {
     GBX_CUDA(cudaMemcpyAsync(ctx->h_force_fx, ctx->d_force_fx, sizeof(unsigned long long) * 3 * n,
                              cudaMemcpyDeviceToHost, ctx->stream));
   }
-  double e = 0;
-  GBX_CUDA(cudaMemcpyAsync(&e, ctx->d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(ctx->h_energy, ctx->d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  const unsigned st = *ctx->h_status;
+  if (optimistic && (st & (gbx::kStatusTableCells | gbx::kStatusTableEntries | gbx::kStatusSegmentTooLong))) {
+    if (rerun) *rerun = true;
+    return GBX_OK;
+  }
+  const double e = *ctx->h_energy;
+  if (st & gbx::kStatusNonFinite) {
+    ctx->last_error = "non-finite Born radius";
+    return GBX_ERR_NONFINITE;
+  }
   if (forces)
     for (int i = 0; i < n; ++i)
       for (int k = 0; k < 3; ++k) forces[3 * i + k] += gbx::fixed_to_double(ctx->h_force_fx[(size_t)k * n + i]);
@@ -749,8 +776,15 @@ gbx_status gbx_execute_host(gbx_context* handle, const double* positions, double
       ctx->last_error = "non-finite position";
       return GBX_ERR_INVALID_ARGUMENT;
     }
-  GBX_TRY(host_run(ctx, positions, false, (flags & GBX_EXEC_COUNT_WORK) != 0));
-  return host_results(ctx, (flags & GBX_EXEC_FORCES) ? forces : nullptr, energy);
+  const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0;
+  double* f = (flags & GBX_EXEC_FORCES) ? forces : nullptr;
+  const bool optimistic = !count && !(flags & GBX_EXEC_CHECK) && tables_sized(ctx);
+  GBX_TRY(host_run(ctx, positions, false, count, !optimistic));
+  bool rerun = false;
+  GBX_TRY(host_results(ctx, f, energy, optimistic, &rerun));
+  if (!rerun) return GBX_OK;
+  GBX_TRY(host_run(ctx, positions, false, count, true));
+  return host_results(ctx, f, energy);
 }
 
 gbx_status gbx_adjoint_host(gbx_context* handle, const double* positions, double* energy, double* forces,

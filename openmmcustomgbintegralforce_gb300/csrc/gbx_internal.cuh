@@ -150,6 +150,8 @@ struct Context {
   int* d_rcount = nullptr;       // [warps] records written, or -1 - needed
   unsigned* d_rmax = nullptr;    // largest per-warp need of the call
   unsigned* h_rmax = nullptr;    // pinned copy of the last d_rmax
+  unsigned* h_status = nullptr;  // pinned: status word of the last host-path call
+  double* h_energy = nullptr;    // pinned: energy of the last host-path call
   cudaEvent_t srec_ev = nullptr;
   bool srec_pending = false;     // srec_ev recorded and not yet read
   bool have_result = false;
