@@ -213,13 +213,18 @@ class Context:
         b = np.ascontiguousarray(box, dtype=np.float64)
         self._check(self.lib.gbx_set_box(self.h, _p(b)))
 
-    def execute_host(self, positions, forces: bool = True, energy: bool = True, count_work: bool = False):
+    def execute_host(self, positions, forces: bool = True, energy: bool = True, count_work: bool = False,
+                     check: bool = False):
+        """Energy and forces from host positions [n, 3] (nm).  The first call
+        sizes the lookup table (checked); later ones synchronise once and
+        re-run checked only if the table outgrew its buffers.  check=True
+        forces a checked run."""
         x = np.ascontiguousarray(positions, dtype=np.float64)
         if x.shape != (self.n, 3):
             raise GBXError(1, "positions must be [n, 3]")
         F = np.zeros((self.n, 3))
         E = np.zeros(1)
-        flags = (EXEC_FORCES if forces else 0) | (EXEC_ENERGY if energy else 0) | EXEC_CHECK
+        flags = (EXEC_FORCES if forces else 0) | (EXEC_ENERGY if energy else 0) | (EXEC_CHECK if check else 0)
         if count_work:
             flags |= EXEC_COUNT_WORK
         self._check(self.lib.gbx_execute_host(self.h, _p(x), _p(F), _p(E), flags))

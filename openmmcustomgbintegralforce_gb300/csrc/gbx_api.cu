@@ -712,8 +712,16 @@ namespace {
 gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work, bool check = true) {
   const int n = ctx->n;
   ctx->stream = ctx->own_stream;
-  for (int i = 0; i < n; ++i)
-    ctx->h_pos[i] = make_float4((float)positions[3 * i], (float)positions[3 * i + 1], (float)positions[3 * i + 2], 0.f);
+  bool finite = true;  // checked in the same pass as the conversion
+  for (int i = 0; i < n; ++i) {
+    const double x = positions[3 * i], y = positions[3 * i + 1], z = positions[3 * i + 2];
+    finite &= std::isfinite(x) & std::isfinite(y) & std::isfinite(z);
+    ctx->h_pos[i] = make_float4((float)x, (float)y, (float)z, 0.f);
+  }
+  if (!finite) {
+    ctx->last_error = "non-finite position";
+    return GBX_ERR_INVALID_ARGUMENT;
+  }
   GBX_CUDA(cudaMemcpyAsync(ctx->d_pos, ctx->h_pos, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
   GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));
   GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
@@ -771,11 +779,6 @@ extern "C" {
 gbx_status gbx_execute_host(gbx_context* handle, const double* positions, double* forces, double* energy, int flags) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !positions) return GBX_ERR_INVALID_ARGUMENT;
-  for (int i = 0; i < 3 * ctx->n; ++i)
-    if (!isfinite(positions[i])) {
-      ctx->last_error = "non-finite position";
-      return GBX_ERR_INVALID_ARGUMENT;
-    }
   const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0;
   double* f = (flags & GBX_EXEC_FORCES) ? forces : nullptr;
   const bool optimistic = !count && !(flags & GBX_EXEC_CHECK) && tables_sized(ctx);

@@ -288,3 +288,18 @@ def test_isolated_atom_known_answer(policy):
     assert np.abs(got[1] / I7 - 1).max() < 1e-6
     assert np.abs(ctx.born_radii() / expected_born(m, I4, I7) - 1).max() < 1e-6
     ctx.close()
+
+
+def test_non_finite_position_is_rejected_and_context_recovers():
+    g = make_globule(300, seed=5)
+    m = GBModel.charmm_gbsw()
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    E0, F0 = ctx.execute_host(g.positions)
+    bad = g.positions.copy()
+    bad[17, 1] = np.nan
+    with pytest.raises(GBXError):
+        ctx.execute_host(bad)
+    E1, F1 = ctx.execute_host(g.positions)
+    assert E1 == E0 and np.array_equal(F1, F0)
+    ctx.close()
