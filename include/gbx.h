@@ -137,7 +137,12 @@ GBX_API gbx_status gbx_set_box(gbx_context* ctx, const double box[3]);
  * (charmmKernels.h:81,121; CharmmCudaKernels.cpp:845-993).  posq: float4[num_atoms]
  * on the device.  force_fixed: fixed-point buffer, ADDED to, components at
  * [0, stride), [stride, 2 stride), [2 stride, 3 stride).  energy: one double on
- * the device, ADDED to.  Either may be NULL when not requested by flags. */
+ * the device, ADDED to.  Either may be NULL when not requested by flags.
+ * Without GBX_EXEC_CHECK the call does not synchronise: if the atoms spread
+ * so far that the lookup table outgrows its buffers, that call's results lack
+ * the volume terms (the oversized table is never indexed) until a call with
+ * GBX_EXEC_CHECK resizes it; callers that cannot check every step use
+ * gbx_execute_host or the batch API, which detect this and re-run. */
 GBX_API gbx_status gbx_execute(gbx_context* ctx, const void* posq, unsigned long long* force_fixed,
                                int force_stride, double* energy, int flags, void* stream);
 

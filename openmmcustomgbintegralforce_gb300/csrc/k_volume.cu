@@ -45,6 +45,8 @@ struct Entries {
   const float4* e;     // (x, y, z, main model parameter)
   const float2* par;   // secondary model parameters (reference table only)
   const int* index;    // atom index of each entry
+  long long cell_cap;  // cells allocated: a geometry with more (a table that
+                       // outgrew its buffers, not yet resized) is never indexed
 };
 
 // ---------------------------------------------------------------------------
@@ -74,11 +76,13 @@ struct RefQuery {
   float rel[3];  // (x_i - min) / step, cell units
   float inv[3];
   float eps;     // guard band in cell units
+  bool off;      // the geometry has more cells than are allocated: no cell
   const TableGeom* g;
   const double* qoff;
-  __device__ __forceinline__ void init(const TableGeom& geom, const float4 xi, const double* qo) {
+  __device__ __forceinline__ void init(const TableGeom& geom, const float4 xi, const double* qo, long long cap) {
     g = &geom;
     qoff = qo;
+    off = geom.ncell > cap;
     const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
     const int dmax = max(geom.dims[0], max(geom.dims[1], geom.dims[2]));
     for (int k = 0; k < 3; ++k) {
@@ -88,6 +92,7 @@ struct RefQuery {
     eps = 1e-4f + 64.0f * (float)dmax * 5.96e-8f;
   }
   __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
+    if (off) return -1;
     const TableGeom& G = *g;
     const float t[3] = {fmaf(v.x, inv[0], rel[0]), fmaf(v.y, inv[1], rel[1]), fmaf(v.z, inv[2], rel[2])};
     int id[3];
@@ -116,21 +121,25 @@ struct TightQuery {
   float xr[3];
   float inv_h;
   int dims[3];
-  __device__ __forceinline__ void init(const TableGeom& g, const float4 xi, const double*) {
+  __device__ __forceinline__ void init(const TableGeom& g, const float4 xi, const double*, long long cap) {
     xr[0] = (float)((double)xi.x - g.min[0]);
     xr[1] = (float)((double)xi.y - g.min[1]);
     xr[2] = (float)((double)xi.z - g.min[2]);
     inv_h = (float)(1.0 / g.step[0]);
-    dims[0] = g.dims[0];
-    dims[1] = g.dims[1];
-    dims[2] = g.dims[2];
+    const bool off = g.ncell > cap;  // more cells than allocated: no cell
+    dims[0] = off ? 0 : g.dims[0];
+    dims[1] = off ? 0 : g.dims[1];
+    dims[2] = off ? 0 : g.dims[2];
   }
-  __device__ __forceinline__ long long cell(const float4, const float4 v, int) const {
+  // 32-bit arithmetic: the exact table holds fewer than 2^31 cells (checked
+  // when it is sized); one unsigned compare per axis tests both bounds
+  __device__ __forceinline__ int cell(const float4, const float4 v, int) const {
     const int cx = (int)floorf((xr[0] + v.x) * inv_h);
     const int cy = (int)floorf((xr[1] + v.y) * inv_h);
     const int cz = (int)floorf((xr[2] + v.z) * inv_h);
-    if (cx < 0 || cy < 0 || cz < 0 || cx >= dims[0] || cy >= dims[1] || cz >= dims[2]) return -1;
-    return ((long long)cx * dims[1] + cy) * dims[2] + cz;
+    if ((unsigned)cx >= (unsigned)dims[0] || (unsigned)cy >= (unsigned)dims[1] || (unsigned)cz >= (unsigned)dims[2])
+      return -1;
+    return (cx * dims[1] + cy) * dims[2] + cz;
   }
 };
 
@@ -316,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff);
+  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   Work<COUNT> wk;
@@ -380,7 +389,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* _
   const int g = lane / kGroup, r = lane % kGroup;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff);
+  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   float J4 = 0.0f, J7 = 0.0f;
@@ -523,7 +532,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff);
+  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
@@ -727,7 +736,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   // the record and the list-walk paths give the same bits
   long long fix = 0, fiy = 0, fiz = 0;
   Q query;
-  query.init(*tab.geom, xi, quad.qoff);
+  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
   const int npts = rr.count ? rr.count[warp] : -1;
   if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
     // recorded points, 32 at a time; lanes over their shaping entries
@@ -951,7 +960,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
   const float4 xi = pos[i];
   const float2 de = dEdJ[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff);
+  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   long long fix = 0, fiy = 0, fiz = 0;
@@ -1073,8 +1082,8 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
 
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
-    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex};
-  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries};
+    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap};
+  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap};
 }
 
 int volume_blocks(const Context* ctx) {

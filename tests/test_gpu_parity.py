@@ -303,3 +303,28 @@ def test_non_finite_position_is_rejected_and_context_recovers():
     E1, F1 = ctx.execute_host(g.positions)
     assert E1 == E0 and np.array_equal(F1, F0)
     ctx.close()
+
+
+def test_host_call_after_the_table_outgrows_its_buffers():
+    """A host call sized on one geometry, then given atoms spread 1.6x wider
+    (the exact table needs ~4x the cells): the unchecked run never indexes
+    the oversized table, the call detects the overflow and re-runs checked,
+    and the result equals a fresh context's bit for bit."""
+    g = make_globule(2000, seed=13)
+    m = GBModel.charmm_gbsw()
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    ctx.execute_host(g.positions)
+    ctx.execute_host(g.positions)
+    c = g.positions.mean(axis=0)
+    wide = c + 1.6 * (g.positions - c)
+    E1, F1 = ctx.execute_host(wide)
+    fresh = Context(m, g.n)
+    fresh.set_particle_parameters(g.charge, g.radius)
+    E2, F2 = fresh.execute_host(wide)
+    assert E1 == E2 and np.array_equal(F1, F2)
+    E3, F3 = ctx.execute_host(g.positions)  # and back
+    E4, F4 = fresh.execute_host(g.positions)
+    assert E3 == E4 and np.array_equal(F3, F4)
+    ctx.close()
+    fresh.close()
