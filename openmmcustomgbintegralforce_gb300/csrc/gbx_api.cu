@@ -68,8 +68,23 @@ const double* lebedev_rule(int order) {
   return nullptr;
 }
 
+// The lookup table's buffers are sized: a call can run unchecked (a host
+// call then reads the status word with its results; a device call replays its
+// CUDA graph).
+bool tables_sized(const Context* ctx) {
+  return ctx->use_tight ? ctx->tight_valid && ctx->tcell_cap > 0 && ctx->tentry_cap > 0
+                        : ctx->cell_cap > 0 && ctx->entry_cap > 0;
+}
+
+void drop_graph(Context* ctx) {
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  ctx->graph = nullptr;
+  ctx->graph_kernels = 0;
+}
+
 template <class T>
 gbx_status dalloc(Context* ctx, T** p, size_t count) {
+  drop_graph(ctx);  // a captured graph holds the old pointers
   if (*p) cudaFree(*p);
   *p = nullptr;
   if (count == 0) count = 1;
@@ -611,6 +626,7 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
 gbx_status gbx_destroy(gbx_context* handle) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  drop_graph(ctx);
   void* ptrs[] = {ctx->d_qv, ctx->d_qw, ctx->d_qoff, ctx->d_radius, ctx->d_charge, ctx->d_par, ctx->d_wpar,
                   ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_cell_cursor, ctx->d_entries,
                   ctx->d_block_sums, ctx->d_reduce, ctx->d_pos, ctx->d_J, ctx->d_born, ctx->d_bornf, ctx->d_dBdJ,
@@ -646,6 +662,7 @@ gbx_status gbx_last_error(const gbx_context* handle, char* buf, size_t len) {
 gbx_status gbx_set_particle_parameters(gbx_context* handle, const double* charge, const double* radius) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !charge || !radius) return GBX_ERR_INVALID_ARGUMENT;
+  drop_graph(ctx);
   const int n = ctx->n;
   for (int i = 0; i < n; ++i) {
     if (!isfinite(charge[i]) || !isfinite(radius[i]) || !(radius[i] > 0)) {
@@ -669,6 +686,7 @@ gbx_status gbx_set_particle_parameters(gbx_context* handle, const double* charge
 gbx_status gbx_set_global_parameters(gbx_context* handle, double alpha0, double alpha1) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !isfinite(alpha0) || !isfinite(alpha1)) return GBX_ERR_INVALID_ARGUMENT;
+  drop_graph(ctx);
   ctx->cfg.alpha0 = alpha0;
   ctx->cfg.alpha1 = alpha1;
   ctx->alpha0 = (float)alpha0;
@@ -679,6 +697,7 @@ gbx_status gbx_set_global_parameters(gbx_context* handle, double alpha0, double 
 gbx_status gbx_set_box(gbx_context* handle, const double box[3]) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !box) return GBX_ERR_INVALID_ARGUMENT;
+  drop_graph(ctx);
   for (int k = 0; k < 3; ++k)
     if (!(box[k] > 0) || !isfinite(box[k])) return GBX_ERR_INVALID_ARGUMENT;
   for (int k = 0; k < 3; ++k) ctx->cfg.box[k] = box[k];
@@ -694,15 +713,54 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   unsigned long long* f = force_fixed;
   int stride = force_stride;
-  if (!(flags & GBX_EXEC_FORCES)) {
+  if (!(flags & GBX_EXEC_FORCES)) {  // forces not wanted: computed into (cleared) internal scratch
     f = ctx->d_force_fx;
     stride = ctx->n;
-    GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
   }
   double* e = (flags & GBX_EXEC_ENERGY) ? energy : ctx->d_energy;
-  const bool check = (flags & GBX_EXEC_CHECK) || (ctx->use_tight ? ctx->tcell_cap == 0 : ctx->cell_cap == 0);
-  return run_pipeline(ctx, reinterpret_cast<const float4*>(posq), f, stride, e, check, false,
-                      (flags & GBX_EXEC_COUNT_WORK) != 0, (flags & GBX_EXEC_FORCES) != 0);
+  const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0, forces = (flags & GBX_EXEC_FORCES) != 0;
+  const bool check = (flags & GBX_EXEC_CHECK) || !tables_sized(ctx);
+  const float4* p4 = reinterpret_cast<const float4*>(posq);
+  if (check || count || ctx->timing) {
+    if (!forces) GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
+    return run_pipeline(ctx, p4, f, stride, e, check, false, count, forces);
+  }
+  // unchecked: one CUDA graph of the whole call, captured on first use
+  const Context::GraphKey key{posq, f, stride, e, flags & (GBX_EXEC_FORCES | GBX_EXEC_ENERGY), ctx->stream};
+  if (!ctx->graph || !(key == ctx->graph_key)) {
+    drop_graph(ctx);
+    GBX_TRY(fix_chain_records(ctx));
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      (void)cudaGetLastError();  // a stream that cannot be captured: launch directly
+      if (!forces) GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
+      return run_pipeline(ctx, p4, f, stride, e, false, false, false, forces);
+    }
+    const long long before = ctx->launches;
+    gbx_status s = GBX_OK;
+    if (!forces && cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream) != cudaSuccess)
+      s = GBX_ERR_CUDA;
+    if (s == GBX_OK) s = run_pipeline(ctx, p4, f, stride, e, false, false, false, forces);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->graph_kernels = ctx->launches - before;  // captured, not yet run
+    ctx->launches = before;
+    if (s != GBX_OK || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (s == GBX_OK) {
+        ctx->last_error = std::string("graph capture: ") + cudaGetErrorString(ce);
+        s = GBX_ERR_CUDA;
+      }
+      return s;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    GBX_CUDA(ei);
+    ctx->graph_key = key;
+  }
+  GBX_CUDA(cudaGraphLaunch(ctx->graph, ctx->stream));
+  ctx->launches += ctx->graph_kernels;
+  ctx->have_result = true;
+  return GBX_OK;
 }
 
 }  // extern "C"
@@ -727,14 +785,6 @@ gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool co
   GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
   // d_pos holds the raw copy; staging rewrites it in place with the model parameter
   return run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, check, adjoint, count_work);
-}
-
-// The lookup table's buffers are sized: a host call can run unchecked and
-// read the status word with its results (one synchronisation instead of one
-// after the table build and one at the end).
-bool tables_sized(const Context* ctx) {
-  return ctx->use_tight ? ctx->tight_valid && ctx->tcell_cap > 0 && ctx->tentry_cap > 0
-                        : ctx->cell_cap > 0 && ctx->entry_cap > 0;
 }
 
 // Reads the call's results back.  With `optimistic` (an unchecked run) a table
@@ -942,6 +992,7 @@ gbx_status gbx_get_work(gbx_context* handle, double* volume_evals, double* shell
 gbx_status gbx_set_chain_records(gbx_context* handle, int per_warp) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  drop_graph(ctx);
   GBX_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->srec_pending = false;
   ctx->srec_auto = per_warp < 0;

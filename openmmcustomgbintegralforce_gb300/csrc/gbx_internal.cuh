@@ -158,6 +158,24 @@ struct Context {
 
   long long launches = 0;  // kernels this context has launched
 
+  // CUDA graph of the unchecked device call, replayed while its arguments
+  // (buffers, flags, stream) stay the same; dropped by every setter and
+  // every reallocation
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;  // kernels one replay launches
+  struct GraphKey {
+    const void* posq = nullptr;
+    const void* force = nullptr;
+    int stride = 0;
+    const void* energy = nullptr;
+    int flags = 0;
+    cudaStream_t stream = nullptr;
+    bool operator==(const GraphKey& o) const {
+      return posq == o.posq && force == o.force && stride == o.stride && energy == o.energy && flags == o.flags &&
+             stream == o.stream;
+    }
+  } graph_key;
+
   // optional per-stage timing (CUDA events on the execute stream)
   bool timing = false;
   static constexpr int kStages = 8;

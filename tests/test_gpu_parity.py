@@ -328,3 +328,42 @@ def test_host_call_after_the_table_outgrows_its_buffers():
     assert E3 == E4 and np.array_equal(F3, F4)
     ctx.close()
     fresh.close()
+
+
+def test_device_call_graph_replay_matches_checked_calls():
+    """Unchecked device calls run as one captured CUDA graph: replays into the
+    same buffers, a recapture for new buffers and a recapture after a
+    parameter change all give a checked call's bits."""
+    torch = pytest.importorskip("torch")
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_CHECK, EXEC_ENERGY, EXEC_FORCES
+
+    g = make_globule(1500, seed=21)
+    m = GBModel.charmm_gbsw()
+    ctx = Context(m, g.n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    dev = torch.device("cuda:0")
+    posq = torch.zeros((g.n, 4), dtype=torch.float32, device=dev)
+    posq[:, :3] = torch.from_numpy(g.positions.astype(np.float32)).to(dev)
+
+    def run(flags, force=None, energy=None):
+        force = torch.zeros(3 * g.n, dtype=torch.int64, device=dev) if force is None else force.zero_()
+        energy = torch.zeros(1, dtype=torch.float64, device=dev) if energy is None else energy.zero_()
+        torch.cuda.synchronize()
+        ctx.execute_device(posq.data_ptr(), force.data_ptr(), g.n, energy.data_ptr(), flags, 0)
+        torch.cuda.synchronize()
+        return float(energy.item()), force.cpu().numpy()
+
+    both = EXEC_FORCES | EXEC_ENERGY
+    E0, F0 = run(both | EXEC_CHECK)
+    f = torch.zeros(3 * g.n, dtype=torch.int64, device=dev)
+    e = torch.zeros(1, dtype=torch.float64, device=dev)
+    for _ in range(3):  # capture, then replays
+        E1, F1 = run(both, f, e)
+        assert E1 == E0 and np.array_equal(F1, F0)
+    E2, F2 = run(both)  # new buffers: captured again
+    assert E2 == E0 and np.array_equal(F2, F0)
+    ctx.set_global_parameters(m.alpha0 * 1.01, m.alpha1)
+    E3, F3 = run(both, f, e)
+    Ec, Fc = run(both | EXEC_CHECK)
+    assert E3 == Ec and np.array_equal(F3, Fc) and E3 != E0
+    ctx.close()
