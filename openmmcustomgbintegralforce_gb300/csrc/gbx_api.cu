@@ -348,6 +348,7 @@ gbx_status grow_tight(Context* ctx, long long cells, long long entries) {
     GBX_TRY(dalloc(ctx, &ctx->d_tcursor, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_tburied, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_tcell, cap));
+    GBX_TRY(dalloc(ctx, &ctx->d_tfirst, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_tblock_sums, cap / (1024 * 8) + 2));
     ctx->tcell_cap = cap;
   }
@@ -634,7 +635,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
                   ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -104,6 +104,7 @@ struct Context {
   int* d_tcursor = nullptr;
   int* d_tburied = nullptr;
   int2* d_tcell = nullptr;       // (count or -1 if buried, start)
+  float4* d_tfirst = nullptr;    // per cell: its list's first (sorted) entry
   int* d_tblock_sums = nullptr;
   float4* d_tentry = nullptr;    // (x, y, z, R') per list entry
   int* d_tindex = nullptr;       // atom index per list entry

@@ -184,6 +184,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
                                                                         float4* __restrict__ entry,
                                                                         int* __restrict__ index,
                                                                         int2* __restrict__ cell,
+                                                                        float4* __restrict__ first,
                                                                         const TableGeom* __restrict__ gp, float w,
                                                                         long long cell_cap, long long entry_cap,
                                                                         unsigned* __restrict__ status) {
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
         }
         entry[cs + r] = ge[q];
         index[cs + r] = iq;
+        if (r == 0) first[c0 + src] = ge[q];
       }
       __syncwarp();
     }
@@ -286,6 +288,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
         }
         entry[cs + r] = s_e[wib][q];
         index[cs + r] = iq;
+        if (r == 0) first[cc] = s_e[wib][q];
       }
       __syncwarp();
     }
@@ -321,7 +324,8 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
     long long sb = (cells + kSortWarps * kWarp - 1) / (kSortWarps * kWarp);
     if (sb > 152 * 64) sb = 152 * 64;
     tight_sort_kernel<<<(int)sb, kSortWarps * kWarp, 0, st>>>(ctx->d_tcount, ctx->d_tstart, ctx->d_tburied,
-                                                               ctx->d_tentry, ctx->d_tindex, ctx->d_tcell, ctx->d_tgeom,
+                                                               ctx->d_tentry, ctx->d_tindex, ctx->d_tcell, ctx->d_tfirst,
+                                                               ctx->d_tgeom,
                                                                (float)ctx->cfg.switch_width, cells, ctx->tentry_cap,
                                                                ctx->d_status);
     ++ctx->launches;

@@ -47,6 +47,7 @@ struct Entries {
   const int* index;    // atom index of each entry
   long long cell_cap;  // cells allocated: a geometry with more (a table that
                        // outgrew its buffers, not yet resized) is never indexed
+  const float4* first; // exact table: each cell's first list entry (else nullptr)
 };
 
 // ---------------------------------------------------------------------------
@@ -558,6 +559,10 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
           const float4 vc = quad.qv[qc];
           const long long cell = query.cell(xi, vc, qc);
           cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
+          // the exact table keeps each cell's first entry by cell: loaded
+          // alongside the cell, not after it
+          float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (tab.first && cell >= 0) a0 = __ldg(tab.first + cell);
           if (cs.x == 0) {
             const float2 wc = quad.qw[qc];
             J4 += wc.x;
@@ -565,7 +570,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
           } else if (cs.x > 0) {
             // the list's first entry, the likeliest burying atom, buries most
             // listed points: V = 0 adds nothing, the point is not queued
-            const float4 a0 = __ldg(tab.e + cs.y);
+            if (!tab.first) a0 = __ldg(tab.e + cs.y);
             const float3 d = delta(a0, xi, vc);
             const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
             const float lo = a0.w - m.sw;
@@ -1082,8 +1087,8 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
 
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
-    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap};
-  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap};
+    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap, ctx->d_tfirst};
+  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap, nullptr};
 }
 
 int volume_blocks(const Context* ctx) {
