@@ -80,6 +80,7 @@ void drop_graph(Context* ctx) {
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
   ctx->graph = nullptr;
   ctx->graph_kernels = 0;
+  ++ctx->epoch;
 }
 
 template <class T>

@@ -46,6 +46,7 @@ struct gbx_batch {
   cudaStream_t own = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;     // stream the graph was captured for
+  std::vector<unsigned long long> epochs;  // each molecule's epoch at capture
   bool sized = false;                      // one checked call has run
   std::string last_error;
 };
@@ -142,7 +143,16 @@ gbx_status capture(gbx_batch* b, cudaStream_t main) {
   cudaGraphDestroy(g);
   BCUDA(b, ei);
   b->graph_stream = main;
+  b->epochs.resize(b->mols.size());
+  for (size_t m = 0; m < b->mols.size(); ++m) b->epochs[m] = b->mols[m]->epoch;
   return GBX_OK;
+}
+
+// A molecule's parameters or buffers changed since the capture.
+bool graph_stale(const gbx_batch* b) {
+  for (size_t m = 0; m < b->mols.size(); ++m)
+    if (b->epochs[m] != b->mols[m]->epoch) return true;
+  return false;
 }
 
 // Checked call: sizes every buffer, then freezes the record regions so the
@@ -158,7 +168,7 @@ gbx_status run_checked(gbx_batch* b, cudaStream_t main) {
 
 gbx_status run(gbx_batch* b, cudaStream_t main, bool force_check) {
   if (force_check || !b->sized) return run_checked(b, main);
-  if (!b->graph || b->graph_stream != main) BTRY(capture(b, main));
+  if (!b->graph || b->graph_stream != main || graph_stale(b)) BTRY(capture(b, main));
   BCUDA(b, cudaGraphLaunch(b->graph, main));
   BCUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, main));
   BCUDA(b, cudaStreamSynchronize(main));

@@ -164,6 +164,9 @@ struct Context {
   // every reallocation
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;  // kernels one replay launches
+  unsigned long long epoch = 0; // bumped whenever captured arguments may change
+                                // (setters, reallocation): graphs that hold this
+                                // context's launches (its own, a batch's) are stale
   struct GraphKey {
     const void* posq = nullptr;
     const void* force = nullptr;

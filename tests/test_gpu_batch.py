@@ -97,3 +97,29 @@ def test_tune_keeps_results(setup):
     E1, F1 = b.execute_host(X)
     assert np.allclose(E1, E0, rtol=1e-6)
     assert rel_rms(F1, F0) < 1e-5
+
+
+def test_replay_after_a_molecule_parameter_change(setup):
+    """Changing one molecule's coefficients or charges through its context
+    between calls: the next replay uses them (the graph is captured again)."""
+    gs, ms, b, X = setup
+    b.execute_host(X)
+    b.execute_host(X)  # a replay
+    k = 1
+    c = b.molecules[k]
+    m2 = ms[k].replace(alpha0=ms[k].alpha0 * 1.02)
+    c.set_global_parameters(m2.alpha0, m2.alpha1)
+    q2 = gs[k].charge * 0.9
+    c.set_particle_parameters(q2, gs[k].radius)
+    E, F = b.execute_host(X)
+    ref = Context(m2, gs[k].n)
+    ref.set_particle_parameters(q2, gs[k].radius)
+    Er, Fr = ref.execute_host(gs[k].positions)
+    ref.close()
+    # the earlier tuning may have changed the quadrature chunking (summation
+    # order), so the comparison with a fresh context is to rounding level
+    assert abs(E[k] / Er - 1) < 1e-6 and rel_rms(split(b, F)[k], Fr) < 1e-5
+    c.set_global_parameters(ms[k].alpha0, ms[k].alpha1)  # restore
+    c.set_particle_parameters(gs[k].charge, gs[k].radius)
+    E0, _ = b.execute_host(X)
+    assert abs(E0[k] / E[k] - 1) > 1e-2
