@@ -78,8 +78,8 @@ FLOPS_PAIR = 39.0
 
 # DRAM bytes (read + write) per launch of each stage's main kernel, from one ncu
 # capture of the same workload (the files named in TRAFFIC_SOURCE).
-TRAFFIC = {"gbsw50k": {"integrals": 908.1e6 + 570.7e6, "pair": 3.11e6 + 0.05e6, "chain_rule": 956.8e6 + 0.14e6},
-           "gbmv10k": {"integrals": 129.6e6 + 213.8e6, "chain_rule": 318.0e6 + 6.2e6}}
+TRAFFIC = {"gbsw50k": {"integrals": 1183.1e6 + 570.2e6, "pair": 3.2e6 + 0.05e6, "chain_rule": 984.6e6 + 0.13e6},
+           "gbmv10k": {"integrals": 129.4e6 + 213.7e6, "chain_rule": 317.9e6 + 5.3e6}}
 TRAFFIC_SOURCE = {"gbsw50k": "profiles/kernels_gbsw50k.md", "gbmv10k": "profiles/gbmv_kernels_gbmv10k.md"}
 
 
