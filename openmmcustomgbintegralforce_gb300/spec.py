@@ -43,7 +43,8 @@ class GBModel:
     h: float = 0.15
     buffer: float = 0.20
     cap: int = 0                      # <= 0: uncapped
-    box: tuple = (0.0, 0.0, 0.0)      # periodic-sampled table only
+    box: tuple = (0.0, 0.0, 0.0)      # periodic-sampled table; with periodic, the rectangular box
+    periodic: bool = False            # CutoffPeriodic: minimum-image distances in box
     sw: float = 0.03
     gamma0: float = 0.44
     beta: float = -100.0

@@ -23,6 +23,18 @@ static inline double delta_r(const double* a, const double* b, double d[3]) {
   return sqrt(r2);
 }
 
+/* The same, by minimum image in a rectangular box when the system is periodic
+ * (ReferenceForce::getDeltaRPeriodic: d -= L floor(d / L + 1/2) per axis). */
+static inline double delta_cfg(const orc_config* cfg, const double* a, const double* b, double d[3]) {
+  if (!cfg->periodic) return delta_r(a, b, d);
+  for (int k = 2; k >= 0; --k) {
+    d[k] = b[k] - a[k];
+    d[k] -= cfg->box[k] * floor(d[k] / cfg->box[k] + 0.5);
+  }
+  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  return sqrt(r2);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Lookup tables                                                             */
 /* ------------------------------------------------------------------------- */
@@ -143,6 +155,10 @@ int orc_table_build(const orc_config* cfg, int n, const double* pos, const doubl
   memset(t, 0, sizeof(*t));
   t->mode = cfg->table_mode;
   if (n <= 0) return -1;
+  if (cfg->periodic && cfg->table_mode == ORC_TABLE_STANDALONE) {
+    t->wrap = 1;  /* the table itself is built from the raw coordinates (:440-514) */
+    for (int k = 0; k < 3; ++k) t->box[k] = cfg->box[k];
+  }
   if (cfg->table_mode == ORC_TABLE_STANDALONE || cfg->table_mode == ORC_TABLE_GRID) {
     double mn[3], mx[3];
     for (int k = 0; k < 3; ++k) mn[k] = mx[k] = pos[k];
@@ -242,9 +258,15 @@ int64_t orc_table_query(const orc_table* t, const double p[3]) {
     return (int64_t)id[0] * (ny * nz) + (int64_t)id[1] * nz + id[2];
   }
   int id[3];
+  double pt[3] = {p[0], p[1], p[2]};
+  if (t->wrap)  /* CharmmReferenceGBSW.cpp:522-528: at most one box length per axis */
+    for (int k = 0; k < 3; ++k) {
+      if (pt[k] < t->min[k]) pt[k] += t->box[k];
+      if (pt[k] > t->max[k]) pt[k] -= t->box[k];
+    }
   for (int k = 0; k < 3; ++k) {
-    if (p[k] < t->min[k] || p[k] > t->max[k]) return -1;
-    id[k] = (int)floor((p[k] - t->min[k]) / t->step[k]);
+    if (pt[k] < t->min[k] || pt[k] > t->max[k]) return -1;
+    id[k] = (int)floor((pt[k] - t->min[k]) / t->step[k]);
   }
   return (int64_t)id[0] * (ny * nz) + (int64_t)id[1] * nz + id[2];
 }
@@ -272,7 +294,7 @@ static double vol_gbsw(const orc_config* cfg, const double* pos, const double* r
   for (int l = 0; l < st->n_list; ++l) {
     int j = st->list[l];
     double d[3];
-    double r = delta_r(p, pos + 3 * j, d);
+    double r = delta_cfg(cfg, p, pos + 3 * j, d);
     double Rj = gbsw_radius(radius[j]);
     double dr = r - Rj;
     double dr3 = dr * dr * dr;
@@ -296,7 +318,7 @@ static double presum_gbmv1(const orc_config* cfg, const double* pos, const doubl
   for (int l = 0; l < st->n_list; ++l) {
     int j = st->list[l];
     double d[3];
-    double r = delta_r(p, pos + 3 * j, d);
+    double r = delta_cfg(cfg, p, pos + 3 * j, d);
     double r4 = r * r * r * r;
     double R = radius[j];
     double R4 = R * R * R * R;
@@ -317,7 +339,7 @@ static double presum_gbmv2(const orc_config* cfg, const double* pos, const doubl
   for (int l = 0; l < st->n_list; ++l) {
     int j = st->list[l];
     double d[3];
-    double r = delta_r(p, pos + 3 * j, d);
+    double r = delta_cfg(cfg, p, pos + 3 * j, d);
     double r2 = r * r;
     double R = radius[j];
     double R2 = R * R;
@@ -383,7 +405,7 @@ static int point_grad(const orc_config* cfg, const double* pos, const double* ra
                       const point_state* st, int l, double g[3], double* gR) {
   int j = st->list[l];
   double d[3];
-  double r = delta_r(p, pos + 3 * j, d);
+  double r = delta_cfg(cfg, p, pos + 3 * j, d);
   if (cfg->model == ORC_GBSW) {
     if (st->V == 0) return 0;
     const double sw = cfg->sw, sw3 = sw * sw * sw;
@@ -533,7 +555,7 @@ static int chain_walk(const orc_config* cfg, const orc_table* t, int n, const do
           int keep_j = 1;
           if (cfg->use_cutoff && cfg->cutoff_chain_quirk) {
             double dd[3];
-            if (delta_r(pos + 3 * i, pos + 3 * j, dd) > cfg->cutoff) keep_j = 0;
+            if (delta_cfg(cfg, pos + 3 * i, pos + 3 * j, dd) > cfg->cutoff) keep_j = 0;
           }
           for (int k = 0; k < 3; ++k) {
             if (keep_j) F[3 * j + k] -= c * g[k];
@@ -606,7 +628,7 @@ int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const dou
       if (cfg->atom_stride > 1 && i % cfg->atom_stride) continue;
       for (int j = i; j < n; ++j) {
         double d[3];
-        double r = delta_r(pos + 3 * i, pos + 3 * j, d);
+        double r = delta_cfg(cfg, pos + 3 * i, pos + 3 * j, d);
         if (cfg->use_cutoff && r > cfg->cutoff) continue;
         npairs += 1;
         double qi = charge[i], qj = charge[j], Ri = B[i], Rj = B[j];

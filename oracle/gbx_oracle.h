@@ -62,6 +62,10 @@ typedef struct {
   int atom_stride;    /* timing samples: only atoms i % stride == 0 run their
                          points, chain rule and pair rows (<= 1: all atoms).
                          The results are then partial; the cost scales by stride. */
+  int periodic;       /* CutoffPeriodic (rectangular box[3]): every distance by minimum
+                         image (ReferenceForce::getDeltaRPeriodic, CharmmReferenceGBSW.cpp:
+                         242-243,287-288,620-621,647-648), the standalone table's query
+                         point wrapped once per axis (:522-535) */
 } orc_config;
 
 typedef struct {
@@ -75,6 +79,7 @@ typedef struct {
   int32_t* atoms;   /* ascending insertion order per cell */
   int64_t dropped;  /* insertions refused by the cap */
   int64_t oob;      /* membership hits whose flat index fell outside the table */
+  int wrap;         /* standalone table of a periodic system: queries wrap once per axis */
 } orc_table;
 
 typedef struct {

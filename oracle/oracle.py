@@ -49,6 +49,7 @@ class OrcConfig(ctypes.Structure):
         ("standalone_sums", ctypes.c_int),
         ("nthreads", ctypes.c_int),
         ("atom_stride", ctypes.c_int),
+        ("periodic", ctypes.c_int),
     ]
 
 
@@ -67,6 +68,7 @@ class OrcTable(ctypes.Structure):
         ("atoms", ctypes.POINTER(ctypes.c_int32)),
         ("dropped", ctypes.c_int64),
         ("oob", ctypes.c_int64),
+        ("wrap", ctypes.c_int),
     ]
 
 
@@ -151,6 +153,7 @@ class Oracle:
         c.standalone_sums = 1 if model.standalone_sums else 0
         c.nthreads = nthreads
         c.atom_stride = atom_stride
+        c.periodic = 1 if model.periodic else 0
         self.cfg = c
 
     def table(self, pos, radius):

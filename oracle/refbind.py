@@ -42,6 +42,8 @@ def lib():
         L.ref_gbsw_quadrature.argtypes = [vp, ci]
         L.ref_gbsw_energy_forces.argtypes = [ci, vp, vp, vp, cd, vp, vp]
         L.ref_gbsw_energy_forces.restype = cd
+        L.ref_gbsw_energy_forces_periodic.argtypes = [ci, vp, vp, vp, cd, vp, vp, vp]
+        L.ref_gbsw_energy_forces_periodic.restype = cd
         L.ref_gbsw_table.argtypes = [ci, vp, vp, vp, vp, vp, cl, vp, cl]
         L.ref_gbsw_table.restype = cl
         L.ref_integral_evaluate.argtypes = [ci, ci, vp, vp, ci, vp, vp, vp, vp]
@@ -99,6 +101,18 @@ def gbsw_energy_forces(pos, charge, radius, cutoff=-1.0):
     F = np.zeros(3 * n)
     B = np.zeros(n)
     E = lib().ref_gbsw_energy_forces(n, _p(pos), _p(q), _p(R), cutoff, _p(F), _p(B))
+    return {"energy": E, "forces": F.reshape(n, 3), "born": B}
+
+
+def gbsw_energy_forces_periodic(pos, charge, radius, cutoff, box):
+    pos = np.ascontiguousarray(pos, np.float64)
+    q = np.ascontiguousarray(charge, np.float64)
+    R = np.ascontiguousarray(radius, np.float64)
+    bx = np.ascontiguousarray(box, np.float64)
+    n = len(R)
+    F = np.zeros(3 * n)
+    B = np.zeros(n)
+    E = lib().ref_gbsw_energy_forces_periodic(n, _p(pos), _p(q), _p(R), cutoff, _p(bx), _p(F), _p(B))
     return {"energy": E, "forces": F.reshape(n, 3), "born": B}
 
 

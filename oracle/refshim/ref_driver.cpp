@@ -68,13 +68,18 @@ int ref_gbsw_quadrature(double* out, int cap) {
   return (int)g._quad.size();
 }
 
+namespace {
 // CharmmGBSWForce on the Reference platform: energy, forces (added to zero),
 // Born radii.  A fresh engine per call (the reference does not reset its
-// accumulators between calls).  cutoff < 0 means NoCutoff.
-double ref_gbsw_energy_forces(int n, const double* pos, const double* charge, const double* radius,
-                              double cutoff, double* forces, double* born) {
+// accumulators between calls).  cutoff < 0 means NoCutoff; box (rectangular
+// edge lengths) non-null means CutoffPeriodic.
+double gbsw_run(int n, const double* pos, const double* charge, const double* radius, double cutoff,
+                const double* box, double* forces, double* born) {
   std::vector<Vec3> x = to_vec3(n, pos);
   std::vector<double> q(charge, charge + n), R(radius, radius + n), sf(n, 1.0);
+  Vec3 vectors[3] = {Vec3(0, 0, 0), Vec3(0, 0, 0), Vec3(0, 0, 0)};
+  if (box)
+    for (int k = 0; k < 3; ++k) vectors[k][k] = box[k];
   OpenMM::NeighborList nl;
   OpenMM::CharmmReferenceGBSW g(n);
   g.setAtomicRadii(R);
@@ -84,13 +89,14 @@ double ref_gbsw_energy_forces(int n, const double* pos, const double* charge, co
   g.setNeighborList(nl);
   if (cutoff > 0) {
     g.setUseCutoff(cutoff);
-    // every pair i<j: the engine itself drops r > cutoff
+    // every pair i<j: the engine itself drops r > cutoff (by minimum image when periodic)
     for (int i = 0; i < n; ++i)
       for (int j = i + 1; j < n; ++j) nl.push_back(std::make_pair(i, j));
   } else {
     g.setNoCutoff();
   }
-  g.setNoPeriodic();
+  if (box) g.setPeriodic(vectors);
+  else g.setNoPeriodic();
   std::vector<Vec3> f(n);
   double e = g.computeEnergyForces(x, q, f);
   for (int i = 0; i < n; ++i)
@@ -99,14 +105,31 @@ double ref_gbsw_energy_forces(int n, const double* pos, const double* charge, co
     OpenMM::CharmmReferenceGBSW g2(n);
     g2.setAtomicRadii(R);
     g2.setScaledRadiusFactors(sf);
-    g2.setNoCutoff();
-    g2.setNoPeriodic();
+    if (box) {  // the engine wants a cutoff before a box; Born radii do not use it
+      g2.setUseCutoff(cutoff);
+      g2.setPeriodic(vectors);
+    } else {
+      g2.setNoCutoff();
+      g2.setNoPeriodic();
+    }
     g2.computeLookupTable(x);
     std::vector<double> b(n);
     g2.computeBornRadiiFast(x, q, b);
     for (int i = 0; i < n; ++i) born[i] = b[i];
   }
   return e;
+}
+}  // namespace
+
+double ref_gbsw_energy_forces(int n, const double* pos, const double* charge, const double* radius,
+                              double cutoff, double* forces, double* born) {
+  return gbsw_run(n, pos, charge, radius, cutoff, nullptr, forces, born);
+}
+
+// The same with a rectangular periodic box (CutoffPeriodic).
+double ref_gbsw_energy_forces_periodic(int n, const double* pos, const double* charge, const double* radius,
+                                       double cutoff, const double* box, double* forces, double* born) {
+  return gbsw_run(n, pos, charge, radius, cutoff, box, forces, born);
 }
 
 // Lookup table of CharmmReferenceGBSW: dims[3], min[3], counts[ncell] and the

@@ -54,6 +54,13 @@ def main():
     ref = R.gbsw_energy_forces(g.positions, g.charge, g.radius, cutoff=1.0)
     save("gbsw_200_cutoff1.npz", positions=g.positions, charge=g.charge, radius=g.radius, cutoff=np.array(1.0),
          energy=np.array(ref["energy"]), forces=ref["forces"])
+    # CutoffPeriodic in a rectangular box barely larger than twice the cutoff: far pairs and far
+    # quadrature points take their minimum image, points beyond the table wrap back into it
+    pos = g.positions - g.positions.min(axis=0)
+    box = np.array([2.5, 2.5, 2.6])
+    ref = R.gbsw_energy_forces_periodic(pos, g.charge, g.radius, 1.2, box)
+    save("gbsw_200_periodic.npz", positions=pos, charge=g.charge, radius=g.radius, cutoff=np.array(1.2), box=box,
+         qoff=qoff, qrad=qrad, qw=qw, energy=np.array(ref["energy"]), forces=ref["forces"], born=ref["born"])
 
     # integral classes: GBSWIntegral (grid table), GBMV-I and GBMV-II (box table)
     qoff, qrad, qw = R.integral_quadrature(24, 3)

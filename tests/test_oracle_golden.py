@@ -46,6 +46,24 @@ def test_charmm_gbsw_cutoff_quirk():
     assert rel_rms(out["forces"], g["forces"]) < 1e-12
 
 
+def test_charmm_gbsw_cutoff_periodic():
+    """CutoffPeriodic: minimum-image distances everywhere and the table query
+    wrapped once per axis, against the reference classes in a rectangular box
+    barely larger than twice the cutoff."""
+    g = golden("gbsw_200_periodic.npz")
+    box = tuple(float(b) for b in g["box"])
+    m = GBModel.charmm_gbsw(cutoff=float(g["cutoff"]), periodic=True, box=box)
+    out = O.Oracle(m, quadrature=(g["qoff"], g["qrad"], g["qw"])).energy_forces(g["positions"], g["charge"],
+                                                                              g["radius"])
+    assert abs(out["energy"] / float(g["energy"]) - 1) < 1e-13
+    assert np.abs(out["born"] / g["born"] - 1).max() < 1e-13
+    assert rel_rms(out["forces"], g["forces"]) < 1e-13
+    # the box matters on this input
+    flat = O.Oracle(m.replace(periodic=False), quadrature=(g["qoff"], g["qrad"], g["qw"])).energy_forces(
+        g["positions"], g["charge"], g["radius"])
+    assert abs(flat["energy"] / float(g["energy"]) - 1) > 1e-2
+
+
 @pytest.mark.parametrize("n", [200, 600])
 @pytest.mark.parametrize("tag", ["gbsw", "gbmv1", "gbmv2"])
 def test_integral_classes(n, tag):
