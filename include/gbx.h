@@ -94,7 +94,9 @@ typedef struct {
   int cutoff_chain_quirk; /* drop chain terms beyond the cutoff (CharmmReferenceGBSW.cpp:291-292) */
   int skip_empty;       /* GBSW: an empty list means V = 1 */
   int table_policy;     /* GBX_TABLE_POLICY_* */
-  int reserved_i;
+  int periodic;         /* CutoffPeriodic (GBSW, standalone table): minimum-image distances in the
+                           rectangular box[3] (edges >= 2 cutoff), the table query wrapped once per
+                           axis (CharmmReferenceGBSW.cpp:242-243,287-288,522-535,620-621,647-648) */
   double tight_grid_length; /* cell edge of the exact GBSW table (nm); <= 0: 0.1 */
   int reserved[4];
 } gbx_config;

@@ -67,7 +67,7 @@ class GbxConfig(ctypes.Structure):
         ("cutoff_chain_quirk", ctypes.c_int),
         ("skip_empty", ctypes.c_int),
         ("table_policy", ctypes.c_int),
-        ("reserved_i", ctypes.c_int),
+        ("periodic", ctypes.c_int),
         ("tight_grid_length", ctypes.c_double),
         ("reserved", ctypes.c_int * 4),
     ]
@@ -95,6 +95,7 @@ class GbxConfig(ctypes.Structure):
         c.skip_empty = 1 if m.skip_empty else 0
         c.table_policy = 1 if m.reference_table else 0
         c.tight_grid_length = m.tight_h
+        c.periodic = 1 if m.periodic else 0
         return c
 
 

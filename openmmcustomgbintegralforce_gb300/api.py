@@ -367,8 +367,11 @@ class CalcCharmmGBSWForceKernel:
 
     Name = "CalcCharmmGBSWForce"
 
-    def __init__(self, model: GBModel | None = None):
+    def __init__(self, model: GBModel | None = None, box=None):
+        """``box``: the rectangular periodic box edges (nm) a CutoffPeriodic
+        force needs (the Context's box vectors in OpenMM)."""
         self.model = model or GBModel.charmm_gbsw()
+        self.box = box
         self.ctx = None
 
     def initialize(self, numParticles: int, force: CharmmGBSWForce):
@@ -376,7 +379,10 @@ class CalcCharmmGBSWForceKernel:
             raise OpenMMException("CharmmGBSWForce must have exactly as many particles as the System it belongs to.")
         m = self.model
         if force.getNonbondedMethod() == CutoffPeriodic:
-            raise GBXError(4, "CutoffPeriodic is not implemented on the device path")
+            # CharmmReferenceKernels.cpp:414-430: minimum-image distances in the box
+            if self.box is None:
+                raise OpenMMException("CutoffPeriodic needs the periodic box: pass box= or call setPeriodicBox first")
+            m = m.replace(cutoff=force.getCutoffDistance(), periodic=True, box=tuple(float(b) for b in self.box))
         if force.getNonbondedMethod() == CutoffNonPeriodic:
             m = m.replace(cutoff=force.getCutoffDistance())
         self.model = m
@@ -390,6 +396,12 @@ class CalcCharmmGBSWForceKernel:
             raise OpenMMException("updateParametersInContext: The number of particles has changed")
         q, R, _ = force._arrays()
         self.ctx.set_particle_parameters(q, R)
+
+    def setPeriodicBox(self, box):
+        """The box edges (nm) for the next calls (a barostat step, say)."""
+        self.box = box
+        if self.ctx is not None:
+            self.ctx.set_box(box)
 
     def execute(self, positions, includeForces: bool = True, includeEnergy: bool = True):
         """Returns (energy, forces[n,3]) for positions in nm."""

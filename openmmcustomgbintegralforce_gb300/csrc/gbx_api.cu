@@ -107,6 +107,14 @@ gbx_status validate_config(const gbx_config& c, std::string& why) {
     for (int k = 0; k < 3; ++k)
       if (!(c.box[k] > 0)) return why = "periodic table needs a positive box", GBX_ERR_INVALID_ARGUMENT;
   if (c.table_cap > gbx::kMaxSortSegment) return why = "table_cap too large", GBX_ERR_INVALID_ARGUMENT;
+  if (c.periodic) {  // CutoffPeriodic: CharmmGBSWForce only (CharmmReferenceGBSW.cpp:147-159)
+    if (c.model != GBX_MODEL_GBSW || c.table_mode != GBX_TABLE_STANDALONE)
+      return why = "CutoffPeriodic is supported for the standalone GBSW model", GBX_ERR_UNSUPPORTED;
+    if (!(c.cutoff > 0)) return why = "CutoffPeriodic needs a cutoff", GBX_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 3; ++k)
+      if (!(c.box[k] >= 2.0 * c.cutoff) || !isfinite(c.box[k]))
+        return why = "each box edge must be at least twice the cutoff", GBX_ERR_INVALID_ARGUMENT;
+  }
   return GBX_OK;
 }
 
@@ -601,8 +609,9 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
     delete ctx;
     return GBX_ERR_CUDA;
   }
+  // the exact table assumes plain distances: a periodic system integrates on the reference table
   ctx->use_tight = cfg->model == GBX_MODEL_GBSW && cfg->table_mode == GBX_TABLE_STANDALONE &&
-                   cfg->table_policy == GBX_TABLE_POLICY_AUTO;
+                   cfg->table_policy == GBX_TABLE_POLICY_AUTO && !cfg->periodic;
   ctx->tight_h = cfg->tight_grid_length > 0 ? cfg->tight_grid_length : 0.1;
   s = upload_quadrature(ctx);
   if (s == GBX_OK) s = alloc_atom_buffers(ctx);
@@ -701,7 +710,11 @@ gbx_status gbx_set_box(gbx_context* handle, const double box[3]) {
   if (!ctx || !box) return GBX_ERR_INVALID_ARGUMENT;
   drop_graph(ctx);
   for (int k = 0; k < 3; ++k)
-    if (!(box[k] > 0) || !isfinite(box[k])) return GBX_ERR_INVALID_ARGUMENT;
+    if (!(box[k] > 0) || !isfinite(box[k]) || (ctx->cfg.periodic && !(box[k] >= 2.0 * ctx->cfg.cutoff))) {
+      ctx->last_error = ctx->cfg.periodic ? "each box edge must be positive and at least twice the cutoff"
+                                          : "box edges must be positive";
+      return GBX_ERR_INVALID_ARGUMENT;
+    }
   for (int k = 0; k < 3; ++k) ctx->cfg.box[k] = box[k];
   return GBX_OK;
 }

@@ -161,6 +161,7 @@ struct SymArgs {
   unsigned long long* energy;  // fixed point (2^-32), summed as integers
   const float4* tile_box;      // cutoff: [2 * ntiles] (lower, upper) corner of each 32-atom tile
   const int* perm;             // cutoff: slot k holds atom perm[k] (spatial order); nullptr: identity
+  float3 L, iL;  // periodic: box edges and their inverses (minimum image)
   int nblocks, ntiles, chunks;
   int chunk;  // j-tiles per warp unit
 };
@@ -202,10 +203,20 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
 // One pair.  kDi = -log2(e) / (4 B_i), kBi = 1 / (4 B_i), pqi = pref q_i.
 // Adds dG/dx_i to ai (force on i: g d, d = x_j - x_i) and dG/dB_i / (-1/2)
 // to ai.db; with SYM also the j side to aj.
-template <bool SYM, bool CUTOFF, bool ADJ>
+// Minimum image in a rectangular box: d - L floor(d / L + 1/2)
+// (ReferenceForce::getDeltaRPeriodic).
+__device__ __forceinline__ float min_image(float d, float L, float iL) { return fmaf(-L, floorf(fmaf(d, iL, 0.5f)), d); }
+
+template <bool SYM, bool CUTOFF, bool ADJ, bool PER = false>
 __device__ __forceinline__ void gb_pair(const PAtom& I, float pqi, float kDi, float kBi, const PAtom& J, float kBj,
-                                       float pref, float cutoff2, PAcc& ai, PAcc& aj, float& esum) {
-  const float dx = J.x - I.x, dy = J.y - I.y, dz = J.z - I.z;
+                                       float pref, float cutoff2, PAcc& ai, PAcc& aj, float& esum,
+                                       float3 L = float3{}, float3 iL = float3{}) {
+  float dx = J.x - I.x, dy = J.y - I.y, dz = J.z - I.z;
+  if (PER) {
+    dx = min_image(dx, L.x, iL.x);
+    dy = min_image(dy, L.y, iL.y);
+    dz = min_image(dz, L.z, iL.z);
+  }
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   if (CUTOFF && r2 > cutoff2) return;
   const float ex = ex2_ftz(r2 * (kDi * J.invB));  // e^-D, D = r^2 / (4 B_i B_j)
@@ -251,10 +262,15 @@ struct PJ2 {  // one j atom, broadcast to both halves
 
 __device__ __forceinline__ float2 bcast2(float v) { return make_float2(v, v); }
 
-template <bool CUTOFF, bool ADJ>
+template <bool CUTOFF, bool ADJ, bool PER>
 __device__ __forceinline__ void gb_pair2(const PAtom2& I, const PJ2& J, float cutoff2, PAcc2& ai, PAcc2& aj,
-                                        float2& esum) {
-  const float2 dx = __fadd2_rn(J.x, I.nx), dy = __fadd2_rn(J.y, I.ny), dz = __fadd2_rn(J.z, I.nz);
+                                        float2& esum, float3 L, float3 iL) {
+  float2 dx = __fadd2_rn(J.x, I.nx), dy = __fadd2_rn(J.y, I.ny), dz = __fadd2_rn(J.z, I.nz);
+  if (PER) {
+    dx = make_float2(min_image(dx.x, L.x, iL.x), min_image(dx.y, L.x, iL.x));
+    dy = make_float2(min_image(dy.x, L.y, iL.y), min_image(dy.y, L.y, iL.y));
+    dz = make_float2(min_image(dz.x, L.z, iL.z), min_image(dz.y, L.z, iL.z));
+  }
   const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
   const float2 arg = __fmul2_rn(r2, __fmul2_rn(I.kD, J.invB));
   const float2 ex = make_float2(ex2_ftz(arg.x), ex2_ftz(arg.y));
@@ -352,9 +368,10 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-template <bool CUTOFF, bool ADJ>
 // The plain form is capped at 96 registers (five blocks per SM); the cutoff
-// and adjoint forms keep their wider register sets.
+// and adjoint forms keep their wider register sets.  PER: minimum image in a
+// periodic box, every tile pair evaluated.
+template <bool CUTOFF, bool ADJ, bool PER = false>
 __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym_kernel(SymArgs a) {
   static_assert(kNI % 2 == 0, "i atoms are paired into float2 halves");
   constexpr int kNH = kNI / 2;
@@ -388,7 +405,7 @@ __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym
     }
     const int src = (lane + 1) % kWarp;
     float4 ilo = make_float4(0.f, 0.f, 0.f, 0.f), ihi = ilo;
-    if (CUTOFF) {  // the i-block's box: the union of its tiles
+    if (CUTOFF && !PER) {  // the i-block's box: the union of its tiles
       ilo = make_float4(3e38f, 3e38f, 3e38f, 0.f);
       ihi = make_float4(-3e38f, -3e38f, -3e38f, 0.f);
       for (int u = 0; u < kNI; ++u) {
@@ -399,7 +416,7 @@ __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym
       }
     }
     for (int jt = jt0; jt < jt1; ++jt) {
-      if (CUTOFF && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
+      if (CUTOFF && !PER && box_gap2(ilo, ihi, a.tile_box[2 * jt], a.tile_box[2 * jt + 1]) > a.cutoff2) continue;
       PAtom J = load_patom(a, kWarp * jt + lane);
       const float2 z2 = make_float2(0.f, 0.f);
       PAcc2 ai[kNH], aj{z2, z2, z2, z2, z2};
@@ -411,7 +428,7 @@ __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym
         const PJ2 J2{bcast2(J.x), bcast2(J.y), bcast2(J.z), bcast2(J.q), bcast2(J.B), bcast2(J.invB),
                      bcast2(0.25f * J.invB), bcast2(a.pref * J.q)};
 #pragma unroll
-        for (int h = 0; h < kNH; ++h) gb_pair2<CUTOFF, ADJ>(I[h], J2, a.cutoff2, ai[h], aj, et);
+        for (int h = 0; h < kNH; ++h) gb_pair2<CUTOFF, ADJ, PER>(I[h], J2, a.cutoff2, ai[h], aj, et, a.L, a.iL);
         J.x = __shfl_sync(0xffffffffu, J.x, src);
         J.y = __shfl_sync(0xffffffffu, J.y, src);
         J.z = __shfl_sync(0xffffffffu, J.z, src);
@@ -456,7 +473,7 @@ __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym
 
 // Pairs inside each i-block (i side only, each ordered pair once: lane t of
 // slot h broadcasts its atom to the warp) and the self terms 1/2 pref q^2 / B.
-template <bool CUTOFF, bool ADJ>
+template <bool CUTOFF, bool ADJ, bool PER = false>
 __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
   const int b = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
@@ -482,7 +499,8 @@ __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
 #pragma unroll
       for (int u = 0; u < kNI; ++u)
         if (h != u || t != lane)
-          gb_pair<false, CUTOFF, ADJ>(I[u], pq[u], kD[u], kB[u], J, 0.f, a.pref, a.cutoff2, ai[u], dummy, e[u]);
+          gb_pair<false, CUTOFF, ADJ, PER>(I[u], pq[u], kD[u], kB[u], J, 0.f, a.pref, a.cutoff2, ai[u], dummy, e[u],
+                                           a.L, a.iL);
     }
   double E = 0.0;
 #pragma unroll
@@ -729,7 +747,19 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
   const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
   cudaStream_t st = ctx->stream;
   cudaMemsetAsync(ctx->d_energy_fx, 0, sizeof(unsigned long long), st);
-  if (a.cutoff2 > 0) {
+  if (ctx->cfg.periodic) {
+    // minimum image, every tile pair evaluated (bounding boxes do not wrap)
+    a.L = make_float3((float)ctx->cfg.box[0], (float)ctx->cfg.box[1], (float)ctx->cfg.box[2]);
+    a.iL = make_float3((float)(1.0 / ctx->cfg.box[0]), (float)(1.0 / ctx->cfg.box[1]), (float)(1.0 / ctx->cfg.box[2]));
+    if (adjoint) {
+      pair_sym_kernel<true, true, true><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<true, true, true><<<gb, kSymThreads, 0, st>>>(a);
+    } else {
+      pair_sym_kernel<true, false, true><<<gu, kSymThreads, 0, st>>>(a);
+      pair_block_kernel<true, false, true><<<gb, kSymThreads, 0, st>>>(a);
+    }
+    ctx->launches += 2;
+  } else if (a.cutoff2 > 0) {
     // spatial order, then tile boxes over it
     const int n = a.n, nb = (n + 255) / 256;
     SortGeom* sg = reinterpret_cast<SortGeom*>(ctx->d_sgeom);

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const float4* 
       G.min[k] = lo;
       G.max[k] = dadd(lo, dmul((double)(G.dims[k] - 1), h));
       G.step[k] = h;
-      G.box[k] = 0.0;
+      G.box[k] = k == 0 ? bx : (k == 1 ? by : bz);  // read only by a periodic system's wrapped query
       ncell *= G.dims[k];
     }
   } else {

@@ -114,6 +114,86 @@ struct RefQuery {
     if (!safe) return query_exact(G, xi, qoff, q);
     return (long long)id[0] * ((long long)G.dims[1] * G.dims[2]) + (long long)id[1] * G.dims[2] + id[2];
   }
+  // x_j - p formed as (x_j - x_i) - v: the FP32 difference of nearby atoms is exact
+  __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
+    return make_float3((a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z);
+  }
+};
+
+// Standalone table of a periodic system (CutoffPeriodic): the point is moved
+// by one box length along each axis where it lies below the grid's lower
+// edge, then back where it lies above the upper edge, and misses if it is
+// still off the grid (CharmmReferenceGBSW.cpp:522-535); FP64 as the reference.
+__device__ long long query_exact_wrap(const TableGeom& g, const float4 xi, const double* qoff, int q) {
+  const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
+  int id[3];
+  for (int k = 0; k < 3; ++k) {
+    double p = __dadd_rn(x[k], qoff[3 * q + k]);
+    if (p < g.min[k]) p = __dadd_rn(p, g.box[k]);
+    if (p > g.max[k]) p = __dsub_rn(p, g.box[k]);
+    if (p < g.min[k] || p > g.max[k]) return -1;
+    id[k] = (int)floor(__ddiv_rn(__dsub_rn(p, g.min[k]), g.step[k]));
+  }
+  return (long long)id[0] * ((long long)g.dims[1] * g.dims[2]) + (long long)id[1] * g.dims[2] + id[2];
+}
+
+// The same wrap in FP32 cell units, with the exact query wherever a point
+// lies within the guard band of a grid edge or a cell face; distances by
+// minimum image in the rectangular box (ReferenceForce::getDeltaRPeriodic:
+// d -= L floor(d / L + 1/2)).
+struct PeriodicQuery {
+  float rel[3];   // (x_i - min) / step, cell units
+  float inv[3];
+  float wrap[3];  // box edge in cell units
+  float L[3], iL[3];
+  float eps;
+  bool off;
+  const TableGeom* g;
+  const double* qoff;
+  __device__ __forceinline__ void init(const TableGeom& geom, const float4 xi, const double* qo, long long cap) {
+    g = &geom;
+    qoff = qo;
+    off = geom.ncell > cap;
+    const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
+    const int dmax = max(geom.dims[0], max(geom.dims[1], geom.dims[2]));
+    for (int k = 0; k < 3; ++k) {
+      rel[k] = (float)((x[k] - geom.min[k]) / geom.step[k]);
+      inv[k] = (float)(1.0 / geom.step[k]);
+      wrap[k] = (float)(geom.box[k] / geom.step[k]);
+      L[k] = (float)geom.box[k];
+      iL[k] = (float)(1.0 / geom.box[k]);
+    }
+    eps = 1e-4f + 64.0f * (float)(dmax + wrap[0] + wrap[1] + wrap[2]) * 5.96e-8f;
+  }
+  __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
+    if (off) return -1;
+    const TableGeom& G = *g;
+    const float t0[3] = {fmaf(v.x, inv[0], rel[0]), fmaf(v.y, inv[1], rel[1]), fmaf(v.z, inv[2], rel[2])};
+    int id[3];
+    bool safe = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float hi = (float)(G.dims[k] - 1);
+      float t = t0[k];
+      if (t < -eps) t += wrap[k];
+      else if (t < eps) safe = false;
+      if (t > hi + eps) t -= wrap[k];
+      else if (t > hi - eps) safe = false;
+      if (safe && (t < -eps || t > hi + eps)) return -1;
+      const float f = floorf(t);
+      const float fr = t - f;
+      id[k] = (int)f;
+      if (fr < eps || fr > 1.0f - eps || t < eps || t > hi - eps) safe = false;
+    }
+    if (!safe) return query_exact_wrap(G, xi, qoff, q);
+    return (long long)id[0] * ((long long)G.dims[1] * G.dims[2]) + (long long)id[1] * G.dims[2] + id[2];
+  }
+  __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
+    float d[3] = {(a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = fmaf(-L[k], floorf(fmaf(d[k], iL[k], 0.5f)), d[k]);
+    return make_float3(d[0], d[1], d[2]);
+  }
 };
 
 // Exact GBSW table: FP32 query; the table's membership margin covers a
@@ -142,6 +222,9 @@ struct TightQuery {
       return -1;
     return (cx * dims[1] + cy) * dims[2] + cz;
   }
+  __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
+    return make_float3((a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z);
+  }
 };
 
 // Work counters for roofline accounting: compiled out unless requested.
@@ -169,13 +252,13 @@ __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const f
 
 // GBSW, CharmmReferenceGBSW.cpp:616-639 / GBSWIntegral.cpp:187-224: V is the
 // product of u_j over the switching shells, 0 once an atom buries the point.
-template <class W>
-__device__ __forceinline__ float gbsw_volume(const ModelConst& m, const float4* __restrict__ list, int cnt,
-                                             const float4 xi, const float4 v, W& wk) {
+template <class Q, class W>
+__device__ __forceinline__ float gbsw_volume(const Q& qy, const ModelConst& m, const float4* __restrict__ list,
+                                             int cnt, const float4 xi, const float4 v, W& wk) {
   float V = 1.0f;
   for (int l = 0; l < cnt; ++l) {
     const float4 a = __ldg(list + l);
-    const float3 d = delta(a, xi, v);
+    const float3 d = qy.delta(a, xi, v);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     const float lo = a.w - m.sw, hi = a.w + m.sw;
     wk.eval();
@@ -245,8 +328,8 @@ __device__ __forceinline__ float gbmv2_S(const ModelConst& m, const Gbmv2State& 
 // Chain-pass work of one point, counted only for roofline accounting: the
 // reference chain kernel (reduceIntegralForce.cu:45-65) visits the whole cell
 // list of every point, with the derivative work inside the switching shell.
-template <int MODEL>
-__device__ __forceinline__ void count_chain_work(const ModelConst& m, const Entries& t, long long cell,
+template <int MODEL, class Q>
+__device__ __forceinline__ void count_chain_work(const Q& qy, const ModelConst& m, const Entries& t, long long cell,
                                                  const float4 xi, const float4 v, Work<true>& wk) {
   if (cell < 0) return;
   const int2 cs = __ldg(t.cell + cell);
@@ -257,7 +340,7 @@ __device__ __forceinline__ void count_chain_work(const ModelConst& m, const Entr
   } else {
     for (int l = 0; l < cs.x; ++l) {
       const float4 a = __ldg(t.e + cs.y + l);
-      const float3 d = delta(a, xi, v);
+      const float3 d = qy.delta(a, xi, v);
       const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
       const float lo = a.w - m.sw, hi = a.w + m.sw;
       wk.fs += (r2 > lo * lo && r2 < hi * hi) ? 1 : 0;
@@ -265,8 +348,8 @@ __device__ __forceinline__ void count_chain_work(const ModelConst& m, const Entr
   }
 }
 
-template <int MODEL, class W>
-__device__ __forceinline__ float solvent_fraction(const ModelConst& m, const Entries& t, long long cell,
+template <int MODEL, class Q, class W>
+__device__ __forceinline__ float solvent_fraction(const Q& qy, const ModelConst& m, const Entries& t, long long cell,
                                                   const float4 xi, const float4 v, W& wk) {
   int cnt = 0, s = 0;
   if (cell >= 0) {
@@ -275,7 +358,7 @@ __device__ __forceinline__ float solvent_fraction(const ModelConst& m, const Ent
     if (cnt < 0) return 0.0f;  // buried cell (exact table)
     s = cs.y;
   }
-  if (MODEL == GBX_MODEL_GBSW) return cnt > 0 ? gbsw_volume(m, t.e + s, cnt, xi, v, wk) : 1.0f;
+  if (MODEL == GBX_MODEL_GBSW) return cnt > 0 ? gbsw_volume(qy, m, t.e + s, cnt, xi, v, wk) : 1.0f;
   float p;
   if (MODEL == GBX_MODEL_GBMV1) return logistic_solvent(m.beta, m.lambda, gbmv1_sum(t.e + s, cnt, xi, v, wk), p);
   if (cnt == 0) return 1.0f;  // empty list: V = 0 (GBMVIntegralTypeII.cpp:140)
@@ -337,10 +420,10 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
     float s;
     if constexpr (MODEL != GBX_MODEL_GBSW)
       s = state ? gbmv_fraction_keep<MODEL>(m, tab, cell, xi, v, wk, state, (size_t)i * m.nq + q, (size_t)n * m.nq)
-                : solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
+                : solvent_fraction<MODEL>(query, m, tab, cell, xi, v, wk);
     else
-      s = solvent_fraction<MODEL>(m, tab, cell, xi, v, wk);
-    if constexpr (COUNT) count_chain_work<MODEL>(m, tab, cell, xi, v, wk);
+      s = solvent_fraction<MODEL>(query, m, tab, cell, xi, v, wk);
+    if constexpr (COUNT) count_chain_work<MODEL>(query, m, tab, cell, xi, v, wk);
     J4 = fmaf(w.x, s, J4);
     J7 = fmaf(w.y, s, J7);
   }
@@ -571,7 +654,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
             // the list's first entry, the likeliest burying atom, buries most
             // listed points: V = 0 adds nothing, the point is not queued
             if (!tab.first) a0 = __ldg(tab.e + cs.y);
-            const float3 d = delta(a0, xi, vc);
+            const float3 d = query.delta(a0, xi, vc);
             const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
             const float lo = a0.w - m.sw;
             if (r2 <= lo * lo) cs.x = -1;
@@ -621,7 +704,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
       for (int u = 0; u < kEnt; ++u) {
         if (fin) break;
         const float4 a = cur[u];
-        const float3 d = delta(a, xi, v);
+        const float3 d = query.delta(a, xi, v);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         const float lo = a.w - m.sw, hi = a.w + m.sw;
         if (r2 <= lo * lo) {
@@ -788,13 +871,14 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const int l = nth < nlo ? (int)__fns(olo, 0, nth + 1) : 32 + (int)__fns(ohi, 0, nth - nlo + 1);
         const int e = ost + l;
         const float4 a = __ldg(tab.e + e);
-        const float3 d = delta(a, xi, ov);
+        const float3 d = query.delta(a, xi, ov);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         // the same expressions as the list walk below
         const float g = shell_g(m, oV, r2 * rsqrtf(r2) - a.w);
         const float gs = ocq * g * rsqrtf(r2);
         const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
-        const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+        const float3 dd = query.delta(a, xi, make_float4(0.f, 0.f, 0.f, 0.f));  // x_k - x_i
+        const float ex = dd.x, ey = dd.y, ez = dd.z;
         push_shaping(out, tab.index + e, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx, gy, gz,
                      fix, fiy, fiz);
       }
@@ -819,7 +903,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         int nk = 0, nshell = 0;
         for (int l = 0; l < cnt; ++l) {
           const float4 a = __ldg(E + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float lo = a.w - m.sw, hi = a.w + m.sw;
           if (r2 <= lo * lo) {
@@ -838,7 +922,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         for (int t = 0; t < scan; ++t) {
           const int l = nshell <= kWalkKeep ? keep[t] : t;
           const float4 a = __ldg(E + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float lo = a.w - m.sw, hi = a.w + m.sw;
           if (!(r2 > lo * lo && r2 < hi * hi)) continue;
@@ -850,7 +934,8 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           if (k == i) continue;
           const float gs = cq * g * rsqrtf(r2);
           const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
-          const float ex = a.x - xi.x, ey = a.y - xi.y, ez = a.z - xi.z;
+          const float3 dd = query.delta(a, xi, make_float4(0.f, 0.f, 0.f, 0.f));  // x_k - x_i
+          const float ex = dd.x, ey = dd.y, ez = dd.z;
           push_shaping(out, tab.index + s + l, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx,
                        gy, gz, fix, fiy, fiz);
         }
@@ -1157,6 +1242,8 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
   const ModelConst m = make_model_const(ctx);
   if (ctx->use_tight) {
     launch_integrals_t<GBX_MODEL_GBSW, TightQuery>(ctx, pos, m, count_work);
+  } else if (ctx->cfg.periodic) {
+    launch_integrals_t<GBX_MODEL_GBSW, PeriodicQuery>(ctx, pos, m, count_work);
   } else {
     switch (ctx->cfg.model) {
       case GBX_MODEL_GBSW: launch_integrals_t<GBX_MODEL_GBSW, RefQuery>(ctx, pos, m, count_work); break;
@@ -1172,6 +1259,9 @@ gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* for
   if (ctx->use_tight) {
     if (adjoint) launch_chain_t<GBX_MODEL_GBSW, TightQuery, true>(ctx, pos, m, force, stride);
     else launch_chain_t<GBX_MODEL_GBSW, TightQuery, false>(ctx, pos, m, force, stride);
+  } else if (ctx->cfg.periodic) {
+    if (adjoint) launch_chain_t<GBX_MODEL_GBSW, PeriodicQuery, true>(ctx, pos, m, force, stride);
+    else launch_chain_t<GBX_MODEL_GBSW, PeriodicQuery, false>(ctx, pos, m, force, stride);
   } else {
     switch (ctx->cfg.model * 2 + (adjoint ? 1 : 0)) {
       case 0: launch_chain_t<GBX_MODEL_GBSW, RefQuery, false>(ctx, pos, m, force, stride); break;

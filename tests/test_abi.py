@@ -61,3 +61,20 @@ def test_create_rejects_bad_arguments_before_touching_the_device(lib):
     lib.gbx_config_preset(2, ctypes.byref(cfg))
     cfg.box[0] = 0.0
     assert lib.gbx_create(ctypes.byref(cfg), 10, ctypes.byref(h)) == 1
+
+
+def test_create_checks_cutoff_periodic_settings_before_touching_the_device(lib):
+    """CutoffPeriodic: GBSW standalone only, a cutoff, and box edges of at
+    least twice the cutoff (CharmmReferenceGBSW.cpp:147-159)."""
+    cfg = _lib.GbxConfig()
+    h = ctypes.c_void_p()
+    lib.gbx_config_preset(3, ctypes.byref(cfg))  # GBMV-II
+    cfg.periodic, cfg.cutoff = 1, 1.0
+    assert lib.gbx_create(ctypes.byref(cfg), 10, ctypes.byref(h)) == 4  # unsupported
+    lib.gbx_config_preset(0, ctypes.byref(cfg))
+    cfg.periodic, cfg.cutoff = 1, 0.0
+    cfg.box[0] = cfg.box[1] = cfg.box[2] = 5.0
+    assert lib.gbx_create(ctypes.byref(cfg), 10, ctypes.byref(h)) == 1  # no cutoff
+    cfg.cutoff = 1.2
+    cfg.box[2] = 2.3
+    assert lib.gbx_create(ctypes.byref(cfg), 10, ctypes.byref(h)) == 1  # box < 2 cutoff
