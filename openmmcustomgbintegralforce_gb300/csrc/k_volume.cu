@@ -1,13 +1,14 @@
 // Born-radius integrals and the chain rule through every quadrature point.
 //
 // Work decomposition: one warp = one atom i x one chunk of quadrature
-// points, lanes over points.  The atom is warp-uniform, every per-atom sum
-// is a fixed-shape warp reduction (bit-reproducible), the quadrature data
-// is read coalesced, and in the chain rule the 32 lanes of one instruction
-// push forces to atoms spread around the atom's sphere rather than to the
-// same few neighbours.  Each point walks its cell's list sequentially; lists
-// are stored inline (x, y, z, model parameter) so there is no dependent
-// index -> position gather.
+// points.  GBSW integrals: lanes over points, each lane walking its point's
+// list and refilling from a per-warp queue; the GBSW chain rule: lanes over
+// the shaping entries of recorded points; GBMV integrals: two lanes per
+// point; the GBMV chain rule: the warp on one point at a time, lanes over
+// its list.  The atom is warp-uniform, every per-atom sum is a fixed-shape
+// warp reduction (bit-reproducible), the quadrature data is read coalesced,
+// and lists are stored inline (x, y, z, model parameter) so there is no
+// dependent index -> position gather.
 //
 // Integrals.  The reference accumulates I_n = sum_q w_q/r_q^(n-2) * (1 - V_q)
 // (GBSWIntegral.cpp:142-146) and then forms 1/r0 - I4 and 1/(4 r0^4) - I7,
@@ -22,7 +23,9 @@
 // FP32 and redone in FP64 exactly as the reference does
 // (CharmmReferenceGBSW.cpp:539-549, CustomGBIntegral.cpp:284-324) whenever
 // the FP32 coordinate lies within a guard band of a cell face.  The
-// standalone GBSW model reads the exact table of k_tight.cu instead.
+// standalone GBSW model reads the exact table of k_tight.cu instead, except
+// in a periodic box, where it reads the reference table through a query that
+// wraps the point as the reference does and measures minimum-image distances.
 #include <math.h>
 
 #include "gbx_internal.cuh"
