@@ -47,6 +47,7 @@ def lib():
         L.ref_gbsw_table.argtypes = [ci, vp, vp, vp, vp, vp, cl, vp, cl]
         L.ref_gbsw_table.restype = cl
         L.ref_integral_evaluate.argtypes = [ci, ci, vp, vp, ci, vp, vp, vp, vp]
+        L.ref_integral_evaluate_periodic.argtypes = [ci, ci, vp, vp, ci, vp, vp, vp]
         L.ref_integral_table.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, cl, vp, cl]
         L.ref_integral_table.restype = cl
         _LIB = L
@@ -147,6 +148,19 @@ def integral_evaluate(itype, pos, radius, orders=(4, 7), box=None, grads=True):
     if grads:
         out["grads"] = G.reshape(len(orders), n, n, 3)
     return out
+
+
+def integral_evaluate_periodic(itype, pos, radius, box, orders=(4, 7)):
+    """Integrals of a CharmmGBMVForce with CutoffPeriodic (minimum-image distances)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    R = np.ascontiguousarray(radius, np.float64)
+    n = len(R)
+    o = np.array(orders, np.int32)
+    I = np.zeros(len(orders) * n)
+    b = np.ascontiguousarray(box, np.float64)
+    if lib().ref_integral_evaluate_periodic(itype, n, _p(pos), _p(R), len(orders), _p(o), _p(b), _p(I)):
+        raise RuntimeError("reference integral evaluation failed")
+    return {"integrals": I.reshape(len(orders), n)}
 
 
 def integral_table(itype, pos, radius, box=None):

@@ -172,8 +172,9 @@ struct IntegralRun {
 // box != NULL supplies the context's periodic box (the GBMV classes always
 // read it; GBSWIntegral only with CutoffPeriodic).
 static IntegralRun* make_integral(int type, int n, const double* radius, int n_int, const int* orders,
-                                  const double* box) {
+                                  const double* box, bool periodic = false) {
   IntegralRun* r = new IntegralRun();
+  if (periodic) r->force.method = OpenMM::CharmmGBMVForce::CutoffPeriodic;  // minimum-image distances
   for (int i = 0; i < n; ++i) r->force.particles.push_back(std::vector<double>(1, radius[i]));
   for (int k = 0; k < n_int; ++k) r->force.integralOrders.push_back(std::vector<int>(1, orders[k]));
   double b[3] = {10.0, 10.0, 10.0};
@@ -207,6 +208,26 @@ int ref_integral_evaluate(int type, int n, const double* pos, const double* radi
     return 0;
   } catch (std::exception& e) {
     std::cerr << "ref_integral_evaluate: " << e.what() << std::endl;
+    return -1;
+  }
+}
+
+// The same for a CharmmGBMVForce with CutoffPeriodic: the integral classes
+// then measure point-to-atom distances by minimum image (and GBSWIntegral
+// switches to the box-sampled table).
+int ref_integral_evaluate_periodic(int type, int n, const double* pos, const double* radius, int n_int,
+                                   const int* orders, const double* box, double* integrals) {
+  try {
+    IntegralRun* r = make_integral(type, n, radius, n_int, orders, box, true);
+    std::vector<Vec3> x = to_vec3(n, pos);
+    std::vector<double> I(n_int * n), G((size_t)n_int * n * n * 3);
+    r->impl->BeforeComputation(*r->ctx, x);
+    r->impl->evaluate(*r->ctx, x, I, G, false);
+    memcpy(integrals, I.data(), sizeof(double) * I.size());
+    delete r;
+    return 0;
+  } catch (std::exception& e) {
+    std::cerr << "ref_integral_evaluate_periodic: " << e.what() << std::endl;
     return -1;
   }
 }

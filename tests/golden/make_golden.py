@@ -83,6 +83,16 @@ def main():
             arrays[f"{tag}_table_atoms"] = t["atoms"]
         save(f"integrals_{n}.npz", **arrays)
 
+    # the integral classes of a CharmmGBMVForce with CutoffPeriodic: minimum-image point-to-atom distances
+    # (GBSWIntegral also switches to the box-sampled table) in a box barely larger than the molecule
+    g = make_globule(200, seed=5, cache=False)
+    pos = g.positions - g.positions.min(axis=0)
+    box = np.array([2.5, 2.5, 2.6])
+    arrays = dict(positions=pos, radius=g.radius, box=box, qoff=qoff, qrad=qrad, qw=qw)
+    for itype, tag in ((0, "gbsw"), (1, "gbmv1"), (2, "gbmv2")):
+        arrays[f"{tag}_integrals"] = R.integral_evaluate_periodic(itype, pos, g.radius, box)["integrals"]
+    save("integrals_200_periodic.npz", **arrays)
+
 
 if __name__ == "__main__":
     main()

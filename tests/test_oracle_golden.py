@@ -98,3 +98,20 @@ def test_isolated_atom_known_answer():
     for k, R in enumerate(radius):
         c4, c7 = continuous_integrals(m, R)
         assert abs(I4[k] / c4 - 1) < 2e-2 and abs(I7[k] / c7 - 1) < 2e-2
+
+
+@pytest.mark.parametrize("tag", ["gbsw", "gbmv1", "gbmv2"])
+def test_integral_classes_cutoff_periodic(tag):
+    """A CharmmGBMVForce with CutoffPeriodic: the integral classes measure
+    point-to-atom distances by minimum image (GBSWIntegral on the box-sampled
+    table), bit for bit against the classes compiled in place."""
+    from openmmcustomgbintegralforce_gb300.spec import TABLE_PERIODIC
+
+    g = golden("integrals_200_periodic.npz")
+    box = tuple(float(b) for b in g["box"])
+    base = {"gbsw": GBModel.gbsw_integral(table_mode=TABLE_PERIODIC, box=box), "gbmv1": GBModel.gbmv1(box=box),
+            "gbmv2": GBModel.gbmv2(box=box)}[tag]
+    m = base.replace(periodic=True, cutoff=1.2)
+    I, _ = O.Oracle(m, quadrature=(g["qoff"], g["qrad"], g["qw"])).integrals(g["positions"], g["radius"])
+    assert np.array_equal(I, g[f"{tag}_integrals"])
+
