@@ -24,7 +24,7 @@ import re
 import numpy as np
 
 from ._lib import Context, GBXError
-from .spec import GBModel
+from .spec import TABLE_PERIODIC, GBModel
 
 # CharmmGBMVForce.h:87-104
 SingleParticle, ParticlePair, ParticlePairNoExclusions = 0, 1, 2
@@ -431,7 +431,13 @@ class CalcCharmmGBMVForceKernel:
                 GBMVIntegralTypeII: GBModel.gbmv2(box=box)}[t]
         m = self.model or base
         if force.getNonbondedMethod() == CutoffPeriodic:
-            raise GBXError(4, "CutoffPeriodic is not implemented on the device path")
+            # the integral classes measure distances by minimum image, GBSWIntegral on the
+            # box-sampled table (GBSWIntegral.cpp:63-68,109), and the pair terms too
+            # (CharmmReferenceGBMV.cpp:294-297)
+            if self.box is None:
+                raise OpenMMException("CutoffPeriodic needs the periodic box: pass box= to the kernel")
+            m = m.replace(cutoff=force.getCutoffDistance(), periodic=True, box=tuple(float(b) for b in self.box),
+                          table_mode=TABLE_PERIODIC)
         if force.getNonbondedMethod() == CutoffNonPeriodic:
             m = m.replace(cutoff=force.getCutoffDistance())
         globals_ = {force.getGlobalParameterName(k): force.getGlobalParameterDefaultValue(k)

@@ -107,9 +107,10 @@ gbx_status validate_config(const gbx_config& c, std::string& why) {
     for (int k = 0; k < 3; ++k)
       if (!(c.box[k] > 0)) return why = "periodic table needs a positive box", GBX_ERR_INVALID_ARGUMENT;
   if (c.table_cap > gbx::kMaxSortSegment) return why = "table_cap too large", GBX_ERR_INVALID_ARGUMENT;
-  if (c.periodic) {  // CutoffPeriodic: CharmmGBSWForce only (CharmmReferenceGBSW.cpp:147-159)
-    if (c.model != GBX_MODEL_GBSW || c.table_mode != GBX_TABLE_STANDALONE)
-      return why = "CutoffPeriodic is supported for the standalone GBSW model", GBX_ERR_UNSUPPORTED;
+  if (c.periodic) {  // CutoffPeriodic (CharmmReferenceGBSW.cpp:147-159, CharmmReferenceGBMV.cpp:138-149)
+    // the standalone GBSW table (wrapped query) or the box-sampled table of the integral classes
+    if (c.table_mode == GBX_TABLE_GRID || (c.table_mode == GBX_TABLE_STANDALONE && c.model != GBX_MODEL_GBSW))
+      return why = "CutoffPeriodic needs the standalone GBSW table or the box-sampled table", GBX_ERR_UNSUPPORTED;
     if (!(c.cutoff > 0)) return why = "CutoffPeriodic needs a cutoff", GBX_ERR_INVALID_ARGUMENT;
     for (int k = 0; k < 3; ++k)
       if (!(c.box[k] >= 2.0 * c.cutoff) || !isfinite(c.box[k]))

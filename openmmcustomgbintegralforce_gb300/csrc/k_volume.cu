@@ -123,6 +123,27 @@ struct RefQuery {
   }
 };
 
+// A box-sampled (periodic-branch) table of a CutoffPeriodic system: the
+// reference query, distances by minimum image (the integral classes with
+// CutoffPeriodic, GBMVIntegralTypeI.cpp:59-62, TypeII.cpp:64-67,
+// GBSWIntegral.cpp:63-68).
+struct MinImageQuery : RefQuery {
+  float L[3], iL[3];
+  __device__ __forceinline__ void init(const TableGeom& geom, const float4 xi, const double* qo, long long cap) {
+    RefQuery::init(geom, xi, qo, cap);
+    for (int k = 0; k < 3; ++k) {
+      L[k] = (float)geom.box[k];
+      iL[k] = (float)(1.0 / geom.box[k]);
+    }
+  }
+  __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
+    float d[3] = {(a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = fmaf(-L[k], floorf(fmaf(d[k], iL[k], 0.5f)), d[k]);
+    return make_float3(d[0], d[1], d[2]);
+  }
+};
+
 // Standalone table of a periodic system (CutoffPeriodic): the point is moved
 // by one box length along each axis where it lies below the grid's lower
 // edge, then back where it lies above the upper edge, and misses if it is
@@ -245,13 +266,10 @@ struct Work<true> {
 };
 
 // ---------------------------------------------------------------------------
-// Volume models on inline entries.  d = x_j - p is formed as (x_j - x_i) - v
-// so the FP32 difference of nearby atoms is exact.
+// Volume models on inline entries.  d = x_j - p comes from the query's
+// delta(): (x_j - x_i) - v, so the FP32 difference of nearby atoms is exact,
+// and in a periodic system its minimum image.
 // ---------------------------------------------------------------------------
-
-__device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) {
-  return make_float3((a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z);
-}
 
 // GBSW, CharmmReferenceGBSW.cpp:616-639 / GBSWIntegral.cpp:187-224: V is the
 // product of u_j over the switching shells, 0 once an atom buries the point.
@@ -276,13 +294,13 @@ __device__ __forceinline__ float gbsw_volume(const Q& qy, const ModelConst& m, c
 }
 
 // GBMV-I, GBMVIntegralTypeI.cpp:155-173: S = sum_j exp(gamma_j r^4).
-template <class W>
-__device__ __forceinline__ float gbmv1_sum(const float4* __restrict__ list, int cnt, const float4 xi,
+template <class Q, class W>
+__device__ __forceinline__ float gbmv1_sum(const Q& qy, const float4* __restrict__ list, int cnt, const float4 xi,
                                            const float4 v, W& wk) {
   float S = 0.0f;
   for (int l = 0; l < cnt; ++l) {
     const float4 a = __ldg(list + l);
-    const float3 d = delta(a, xi, v);
+    const float3 d = qy.delta(a, xi, v);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     S += __expf(a.w * (r2 * r2));
     wk.eval();
@@ -296,14 +314,15 @@ struct Gbmv2State {
 
 // GBMV-II, GBMVIntegralTypeII.cpp:163-191:
 // F_j = (C_j / (C_j + 100 r^2 - 100 R_j^2))^2, sums of F, r^2 F^2 and F d.
-template <class W>
-__device__ __forceinline__ Gbmv2State gbmv2_sums(const float4* __restrict__ list, const float2* __restrict__ par,
+template <class Q, class W>
+__device__ __forceinline__ Gbmv2State gbmv2_sums(const Q& qy, const float4* __restrict__ list,
+                                                 const float2* __restrict__ par,
                                                  int cnt, const float4 xi, const float4 v, W& wk) {
   Gbmv2State s{0.f, 0.f, 0.f, 0.f, 0.f};
   for (int l = 0; l < cnt; ++l) {
     const float4 a = __ldg(list + l);
     const float K = __ldg(&par[l].x);
-    const float3 d = delta(a, xi, v);
+    const float3 d = qy.delta(a, xi, v);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     float F = __fdividef(a.w, fmaf(100.0f, r2, K));
     F = F * F;
@@ -363,9 +382,9 @@ __device__ __forceinline__ float solvent_fraction(const Q& qy, const ModelConst&
   }
   if (MODEL == GBX_MODEL_GBSW) return cnt > 0 ? gbsw_volume(qy, m, t.e + s, cnt, xi, v, wk) : 1.0f;
   float p;
-  if (MODEL == GBX_MODEL_GBMV1) return logistic_solvent(m.beta, m.lambda, gbmv1_sum(t.e + s, cnt, xi, v, wk), p);
+  if (MODEL == GBX_MODEL_GBMV1) return logistic_solvent(m.beta, m.lambda, gbmv1_sum(qy, t.e + s, cnt, xi, v, wk), p);
   if (cnt == 0) return 1.0f;  // empty list: V = 0 (GBMVIntegralTypeII.cpp:140)
-  return logistic_solvent(m.beta, m.lambda, gbmv2_S(m, gbmv2_sums(t.e + s, t.par + s, cnt, xi, v, wk)), p);
+  return logistic_solvent(m.beta, m.lambda, gbmv2_S(m, gbmv2_sums(qy, t.e + s, t.par + s, cnt, xi, v, wk)), p);
 }
 
 // ---------------------------------------------------------------------------
@@ -373,8 +392,8 @@ __device__ __forceinline__ float solvent_fraction(const Q& qy, const ModelConst&
 // ---------------------------------------------------------------------------
 // GBMV point state kept for the chain rule (saves it re-summing every list):
 // GBMV-I S at state[i Q + q]; GBMV-II s1, s2, vx, vy, vz in five planes of N Q.
-template <int MODEL, class W>
-__device__ __forceinline__ float gbmv_fraction_keep(const ModelConst& m, const Entries& t, long long cell,
+template <int MODEL, class Q, class W>
+__device__ __forceinline__ float gbmv_fraction_keep(const Q& qy, const ModelConst& m, const Entries& t, long long cell,
                                                     const float4 xi, const float4 v, W& wk, float* state,
                                                     size_t idx, size_t plane) {
   int cnt = 0, s = 0;
@@ -385,12 +404,12 @@ __device__ __forceinline__ float gbmv_fraction_keep(const ModelConst& m, const E
   }
   float p;
   if constexpr (MODEL == GBX_MODEL_GBMV1) {
-    const float S = gbmv1_sum(t.e + s, cnt, xi, v, wk);
+    const float S = gbmv1_sum(qy, t.e + s, cnt, xi, v, wk);
     state[idx] = S;
     return logistic_solvent(m.beta, m.lambda, S, p);
   } else {
     if (cnt == 0) return 1.0f;  // empty list: V = 0 (GBMVIntegralTypeII.cpp:140)
-    const Gbmv2State st = gbmv2_sums(t.e + s, t.par + s, cnt, xi, v, wk);
+    const Gbmv2State st = gbmv2_sums(qy, t.e + s, t.par + s, cnt, xi, v, wk);
     state[idx] = st.s1;
     state[idx + plane] = st.s2;
     state[idx + 2 * plane] = st.vx;
@@ -422,7 +441,7 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
     const long long cell = query.cell(xi, v, q);
     float s;
     if constexpr (MODEL != GBX_MODEL_GBSW)
-      s = state ? gbmv_fraction_keep<MODEL>(m, tab, cell, xi, v, wk, state, (size_t)i * m.nq + q, (size_t)n * m.nq)
+      s = state ? gbmv_fraction_keep<MODEL>(query, m, tab, cell, xi, v, wk, state, (size_t)i * m.nq + q, (size_t)n * m.nq)
                 : solvent_fraction<MODEL>(query, m, tab, cell, xi, v, wk);
     else
       s = solvent_fraction<MODEL>(query, m, tab, cell, xi, v, wk);
@@ -496,7 +515,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* _
     float S1 = 0.f, S2 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f;
     for (int l = r; l < cnt; l += kGroup) {
       const float4 a = __ldg(tab.e + s + l);
-      const float3 d = delta(a, xi, v);
+      const float3 d = query.delta(a, xi, v);
       const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
       if constexpr (MODEL == GBX_MODEL_GBMV1) {
         S1 += __expf(a.w * (r2 * r2));
@@ -945,14 +964,14 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
       } else if (MODEL == GBX_MODEL_GBMV1) {
         Work<false> wk;
         float p;
-        const float Ssum = rr.state ? rr.state[(size_t)i * m.nq + q] : gbmv1_sum(E, cnt, xi, v, wk);
+        const float Ssum = rr.state ? rr.state[(size_t)i * m.nq + q] : gbmv1_sum(query, E, cnt, xi, v, wk);
         logistic_solvent(m.beta, m.lambda, Ssum, p);
         const float cS = cq * __fdividef(m.beta * p, (1.0f + p) * (1.0f + p));  // c ds/dS
         if (cS == 0.0f) continue;
         float px = 0.f, py = 0.f, pz = 0.f;
         for (int l = 0; l < cnt; ++l) {
           const float4 a = __ldg(E + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float r4 = r2 * r2;
           const float e = __expf(a.w * r4);
@@ -978,7 +997,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           st = Gbmv2State{rr.state[idx], rr.state[idx + plane], rr.state[idx + 2 * plane], rr.state[idx + 3 * plane],
                           rr.state[idx + 4 * plane]};
         } else {
-          st = gbmv2_sums(E, tab.par + s, cnt, xi, v, wk);
+          st = gbmv2_sums(query, E, tab.par + s, cnt, xi, v, wk);
         }
         const float s3sq = fmaf(st.vx, st.vx, fmaf(st.vy, st.vy, st.vz * st.vz));
         float p;
@@ -993,7 +1012,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         for (int l = 0; l < cnt; ++l) {
           const float4 a = __ldg(E + l);
           const float2 pk = __ldg(tab.par + s + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float T = fmaf(100.0f, r2, pk.x);
           const float CT = __fdividef(a.w, T);
@@ -1109,7 +1128,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
       if constexpr (MODEL == GBX_MODEL_GBMV1) {
         for (int l = lane; l < cnt; l += kWarp) {
           const float4 a = __ldg(tab.e + s + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float r4 = r2 * r2;
           const float e = __expf(a.w * r4);
@@ -1131,7 +1150,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
         for (int l = lane; l < cnt; l += kWarp) {
           const float4 a = __ldg(tab.e + s + l);
           const float2 pk = __ldg(tab.par + s + l);
-          const float3 d = delta(a, xi, v);
+          const float3 d = query.delta(a, xi, v);
           const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
           const float T = fmaf(100.0f, r2, pk.x);
           const float CT = __fdividef(a.w, T);
@@ -1245,8 +1264,14 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
   const ModelConst m = make_model_const(ctx);
   if (ctx->use_tight) {
     launch_integrals_t<GBX_MODEL_GBSW, TightQuery>(ctx, pos, m, count_work);
-  } else if (ctx->cfg.periodic) {
+  } else if (ctx->cfg.periodic && ctx->cfg.table_mode == GBX_TABLE_STANDALONE) {
     launch_integrals_t<GBX_MODEL_GBSW, PeriodicQuery>(ctx, pos, m, count_work);
+  } else if (ctx->cfg.periodic) {
+    switch (ctx->cfg.model) {
+      case GBX_MODEL_GBSW: launch_integrals_t<GBX_MODEL_GBSW, MinImageQuery>(ctx, pos, m, count_work); break;
+      case GBX_MODEL_GBMV1: launch_integrals_t<GBX_MODEL_GBMV1, MinImageQuery>(ctx, pos, m, count_work); break;
+      default: launch_integrals_t<GBX_MODEL_GBMV2, MinImageQuery>(ctx, pos, m, count_work); break;
+    }
   } else {
     switch (ctx->cfg.model) {
       case GBX_MODEL_GBSW: launch_integrals_t<GBX_MODEL_GBSW, RefQuery>(ctx, pos, m, count_work); break;
@@ -1262,9 +1287,18 @@ gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* for
   if (ctx->use_tight) {
     if (adjoint) launch_chain_t<GBX_MODEL_GBSW, TightQuery, true>(ctx, pos, m, force, stride);
     else launch_chain_t<GBX_MODEL_GBSW, TightQuery, false>(ctx, pos, m, force, stride);
-  } else if (ctx->cfg.periodic) {
+  } else if (ctx->cfg.periodic && ctx->cfg.table_mode == GBX_TABLE_STANDALONE) {
     if (adjoint) launch_chain_t<GBX_MODEL_GBSW, PeriodicQuery, true>(ctx, pos, m, force, stride);
     else launch_chain_t<GBX_MODEL_GBSW, PeriodicQuery, false>(ctx, pos, m, force, stride);
+  } else if (ctx->cfg.periodic) {
+    switch (ctx->cfg.model * 2 + (adjoint ? 1 : 0)) {
+      case 0: launch_chain_t<GBX_MODEL_GBSW, MinImageQuery, false>(ctx, pos, m, force, stride); break;
+      case 1: launch_chain_t<GBX_MODEL_GBSW, MinImageQuery, true>(ctx, pos, m, force, stride); break;
+      case 2: launch_chain_t<GBX_MODEL_GBMV1, MinImageQuery, false>(ctx, pos, m, force, stride); break;
+      case 3: launch_chain_t<GBX_MODEL_GBMV1, MinImageQuery, true>(ctx, pos, m, force, stride); break;
+      case 4: launch_chain_t<GBX_MODEL_GBMV2, MinImageQuery, false>(ctx, pos, m, force, stride); break;
+      default: launch_chain_t<GBX_MODEL_GBMV2, MinImageQuery, true>(ctx, pos, m, force, stride); break;
+    }
   } else {
     switch (ctx->cfg.model * 2 + (adjoint ? 1 : 0)) {
       case 0: launch_chain_t<GBX_MODEL_GBSW, RefQuery, false>(ctx, pos, m, force, stride); break;

@@ -64,11 +64,12 @@ def test_create_rejects_bad_arguments_before_touching_the_device(lib):
 
 
 def test_create_checks_cutoff_periodic_settings_before_touching_the_device(lib):
-    """CutoffPeriodic: GBSW standalone only, a cutoff, and box edges of at
-    least twice the cutoff (CharmmReferenceGBSW.cpp:147-159)."""
+    """CutoffPeriodic: the standalone GBSW table or the box-sampled table, a
+    cutoff, and box edges of at least twice the cutoff
+    (CharmmReferenceGBSW.cpp:147-159)."""
     cfg = _lib.GbxConfig()
     h = ctypes.c_void_p()
-    lib.gbx_config_preset(3, ctypes.byref(cfg))  # GBMV-II
+    lib.gbx_config_preset(1, ctypes.byref(cfg))  # the grid table has no periodic form
     cfg.periodic, cfg.cutoff = 1, 1.0
     assert lib.gbx_create(ctypes.byref(cfg), 10, ctypes.byref(h)) == 4  # unsupported
     lib.gbx_config_preset(0, ctypes.byref(cfg))

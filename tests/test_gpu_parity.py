@@ -416,3 +416,34 @@ def test_cutoff_periodic_against_the_oracle_with_adjoint():
     flat = O.Oracle(m.replace(periodic=False)).energy_forces(pos, g.charge, g.radius)
     assert abs(flat["energy"] / ref["energy"] - 1) > 1e-3
     ctx.close()
+
+
+@pytest.mark.parametrize("itype", ["gbsw", "gbmv1", "gbmv2"])
+def test_gbmv_force_cutoff_periodic_against_the_oracle(itype):
+    """A CharmmGBMVForce with CutoffPeriodic through the kernel mirror: the
+    integral classes and the pair terms by minimum image (GBSWIntegral on the
+    box-sampled table), against the FP64 oracle in a box barely larger than
+    twice the cutoff."""
+    from openmmcustomgbintegralforce_gb300 import api
+    from openmmcustomgbintegralforce_gb300.spec import TABLE_PERIODIC
+
+    g = make_globule(600, seed=23)
+    pos = g.positions - g.positions.min(axis=0)
+    box = (2.8, 2.8, 2.9)
+    t = {"gbsw": api.GBSWIntegral, "gbmv1": api.GBMVIntegralTypeI, "gbmv2": api.GBMVIntegralTypeII}[itype]
+    f = api.canonical_gbmv_force(t)
+    for i in range(g.n):
+        f.addParticle([g.charge[i], g.radius[i]])
+    f.setNonbondedMethod(api.CutoffPeriodic)
+    f.setCutoffDistance(1.3)
+    k = api.CalcCharmmGBMVForceKernel(box=box)
+    k.initialize(g.n, f)
+    E, F = k.execute(pos)
+    base = {"gbsw": GBModel.gbsw_integral(), "gbmv1": GBModel.gbmv1(), "gbmv2": GBModel.gbmv2()}[itype]
+    m = base.replace(cutoff=1.3, periodic=True, box=box, table_mode=TABLE_PERIODIC)
+    ref = O.Oracle(m).energy_forces(pos, g.charge, g.radius)
+    assert abs(E / ref["energy"] - 1) < 2e-5
+    assert rel_rms(F, ref["forces"]) < 1e-4
+    flat = O.Oracle(m.replace(periodic=False, cutoff=0.0)).energy_forces(pos, g.charge, g.radius)
+    assert abs(flat["energy"] / ref["energy"] - 1) > 1e-3
+
