@@ -78,8 +78,10 @@ bool tables_sized(const Context* ctx) {
 
 void drop_graph(Context* ctx) {
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-  ctx->graph = nullptr;
-  ctx->graph_kernels = 0;
+  if (ctx->host_graph) cudaGraphExecDestroy(ctx->host_graph);
+  ctx->graph = ctx->host_graph = nullptr;
+  ctx->graph_kernels = ctx->host_graph_kernels = 0;
+  ctx->host_graph_forces = -1;
   ++ctx->epoch;
 }
 
@@ -502,7 +504,9 @@ gbx_status set_chunks(Context* ctx, int chunks) {
 
 gbx_status fix_chain_records(Context* ctx) {
   // freeze the record regions at the largest need seen so far (no further
-  // event queries: the call sequence can be captured in a CUDA graph)
+  // event queries: the call sequence can be captured in a CUDA graph); a
+  // size the caller fixed (or an earlier freeze) stands
+  if (!ctx->srec_auto) return GBX_OK;
   if (ctx->srec_pending) {
     GBX_CUDA(cudaEventSynchronize(ctx->srec_ev));
     ctx->srec_pending = false;
@@ -783,10 +787,10 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
 
 namespace {
 
-gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work, bool check = true) {
+// Host positions -> pinned float4 staging (checked for finite values in the same pass).
+gbx_status host_stage(Context* ctx, const double* positions) {
   const int n = ctx->n;
-  ctx->stream = ctx->own_stream;
-  bool finite = true;  // checked in the same pass as the conversion
+  bool finite = true;
   for (int i = 0; i < n; ++i) {
     const double x = positions[3 * i], y = positions[3 * i + 1], z = positions[3 * i + 2];
     finite &= std::isfinite(x) & std::isfinite(y) & std::isfinite(z);
@@ -796,26 +800,40 @@ gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool co
     ctx->last_error = "non-finite position";
     return GBX_ERR_INVALID_ARGUMENT;
   }
+  return GBX_OK;
+}
+
+// Upload, evaluation, and the readback of forces (optional), energy and the
+// status word, all on the context's own stream.
+gbx_status host_enqueue(Context* ctx, bool adjoint, bool count_work, bool check, bool forces) {
+  const int n = ctx->n;
+  ctx->stream = ctx->own_stream;
   GBX_CUDA(cudaMemcpyAsync(ctx->d_pos, ctx->h_pos, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
   GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));
   GBX_CUDA(cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream));
   // d_pos holds the raw copy; staging rewrites it in place with the model parameter
-  return run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, check, adjoint, count_work);
+  GBX_TRY(run_pipeline(ctx, ctx->d_pos, ctx->d_force_fx, n, ctx->d_energy, check, adjoint, count_work));
+  if (forces)
+    GBX_CUDA(cudaMemcpyAsync(ctx->h_force_fx, ctx->d_force_fx, sizeof(unsigned long long) * 3 * n,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(ctx->h_energy, ctx->d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GBX_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  return GBX_OK;
 }
 
-// Reads the call's results back.  With `optimistic` (an unchecked run) a table
-// that outgrew its buffers sets *rerun and leaves the outputs untouched: the
-// caller runs again checked, which grows the buffers.
+gbx_status host_run(Context* ctx, const double* positions, bool adjoint, bool count_work, bool check = true,
+                    bool forces = true) {
+  GBX_TRY(host_stage(ctx, positions));
+  return host_enqueue(ctx, adjoint, count_work, check, forces);
+}
+
+// Waits for the call and writes its results.  With `optimistic` (an
+// unchecked run) a table that outgrew its buffers sets *rerun and leaves the
+// outputs untouched: the caller runs again checked, which grows the buffers.
 gbx_status host_results(Context* ctx, double* forces, double* energy, bool optimistic = false,
                         bool* rerun = nullptr) {
   const int n = ctx->n;
   if (rerun) *rerun = false;
-  if (forces) {
-    GBX_CUDA(cudaMemcpyAsync(ctx->h_force_fx, ctx->d_force_fx, sizeof(unsigned long long) * 3 * n,
-                             cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  GBX_CUDA(cudaMemcpyAsync(ctx->h_energy, ctx->d_energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  GBX_CUDA(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   GBX_CUDA(cudaStreamSynchronize(ctx->stream));
   const unsigned st = *ctx->h_status;
   if (optimistic && (st & (gbx::kStatusTableCells | gbx::kStatusTableEntries | gbx::kStatusSegmentTooLong))) {
@@ -838,6 +856,40 @@ gbx_status host_results(Context* ctx, double* forces, double* energy, bool optim
   return GBX_OK;
 }
 
+// The unchecked host call as one CUDA graph (upload, evaluation, readback
+// between the context's pinned buffers), captured on first use.
+gbx_status host_graph_launch(Context* ctx, bool forces) {
+  ctx->stream = ctx->own_stream;
+  if (!ctx->host_graph || ctx->host_graph_forces != (forces ? 1 : 0)) {
+    if (ctx->host_graph) cudaGraphExecDestroy(ctx->host_graph);
+    ctx->host_graph = nullptr;
+    GBX_TRY(fix_chain_records(ctx));
+    GBX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = ctx->launches;
+    gbx_status s = host_enqueue(ctx, false, false, false, forces);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->host_graph_kernels = ctx->launches - before;  // captured, not yet run
+    ctx->launches = before;
+    if (s != GBX_OK || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (s == GBX_OK) {
+        ctx->last_error = std::string("graph capture: ") + cudaGetErrorString(ce);
+        s = GBX_ERR_CUDA;
+      }
+      return s;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->host_graph, g, 0);
+    cudaGraphDestroy(g);
+    GBX_CUDA(ei);
+    ctx->host_graph_forces = forces ? 1 : 0;
+  }
+  GBX_CUDA(cudaGraphLaunch(ctx->host_graph, ctx->stream));
+  ctx->launches += ctx->host_graph_kernels;
+  ctx->have_result = true;
+  return GBX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -848,11 +900,18 @@ gbx_status gbx_execute_host(gbx_context* handle, const double* positions, double
   const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0;
   double* f = (flags & GBX_EXEC_FORCES) ? forces : nullptr;
   const bool optimistic = !count && !(flags & GBX_EXEC_CHECK) && tables_sized(ctx);
-  GBX_TRY(host_run(ctx, positions, false, count, !optimistic));
   bool rerun = false;
-  GBX_TRY(host_results(ctx, f, energy, optimistic, &rerun));
-  if (!rerun) return GBX_OK;
-  GBX_TRY(host_run(ctx, positions, false, count, true));
+  if (optimistic && !ctx->timing) {  // one graph launch and one synchronisation
+    GBX_TRY(host_stage(ctx, positions));
+    GBX_TRY(host_graph_launch(ctx, f != nullptr));
+    GBX_TRY(host_results(ctx, f, energy, true, &rerun));
+    if (!rerun) return GBX_OK;
+  } else {
+    GBX_TRY(host_run(ctx, positions, false, count, !optimistic, f != nullptr));
+    GBX_TRY(host_results(ctx, f, energy, optimistic, &rerun));
+    if (!rerun) return GBX_OK;
+  }
+  GBX_TRY(host_run(ctx, positions, false, count, true, f != nullptr));
   return host_results(ctx, f, energy);
 }
 

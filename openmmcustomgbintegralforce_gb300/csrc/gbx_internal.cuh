@@ -164,6 +164,9 @@ struct Context {
   // every reallocation
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;  // kernels one replay launches
+  cudaGraphExec_t host_graph = nullptr;  // the host-buffer call: upload, evaluation, readback
+  long long host_graph_kernels = 0;
+  int host_graph_forces = -1;            // whether the captured call reads forces back
   unsigned long long epoch = 0; // bumped whenever captured arguments may change
                                 // (setters, reallocation): graphs that hold this
                                 // context's launches (its own, a batch's) are stale
