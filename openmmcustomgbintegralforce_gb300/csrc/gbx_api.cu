@@ -225,11 +225,14 @@ gbx_status alloc_atom_buffers(Context* ctx) {
 // (Re)allocates the chain-record buffer for R records per warp, within half
 // of the free device memory; on failure the context runs without records.
 gbx_status alloc_records(Context* ctx, int R) {
+  drop_graph(ctx);  // a captured graph holds the old pointers
   if (ctx->d_srec) {
     GBX_CUDA(cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_srec);
+    cudaFree(ctx->d_srec_st);
   }
   ctx->d_srec = nullptr;
+  ctx->d_srec_st = nullptr;
   ctx->srec_R = 0;
   const long long warps = (long long)ctx->n * ctx->n_chunks;
   if (R <= 0) return GBX_OK;
@@ -239,11 +242,14 @@ gbx_status alloc_records(Context* ctx, int R) {
   }
   size_t free_b = 0, total_b = 0;
   GBX_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const long long fit = (long long)(free_b / 2 / sizeof(int4)) / warps;
+  const long long fit = (long long)(free_b / 2 / (sizeof(int4) + sizeof(int))) / warps;
   if ((long long)R > fit) R = (int)(fit / 32 * 32);
-  if (R <= 0 || cudaMalloc((void**)&ctx->d_srec, sizeof(int4) * (size_t)warps * R) != cudaSuccess) {
+  if (R <= 0 || cudaMalloc((void**)&ctx->d_srec, sizeof(int4) * (size_t)warps * R) != cudaSuccess ||
+      cudaMalloc((void**)&ctx->d_srec_st, sizeof(int) * (size_t)warps * R) != cudaSuccess) {
     (void)cudaGetLastError();
+    if (ctx->d_srec) cudaFree(ctx->d_srec);
     ctx->d_srec = nullptr;
+    ctx->d_srec_st = nullptr;
     ctx->srec_auto = false;
     return GBX_OK;
   }
@@ -650,7 +656,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
                   ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -146,6 +146,7 @@ struct Context {
   bool records = false;          // this call writes and reads records
   bool srec_auto = true;         // size R from the largest need seen
   int4* d_srec = nullptr;
+  int* d_srec_st = nullptr;      // the recorded point's list start, beside each record
   int srec_R = 0;                // records per warp (0: no buffer)
   long long srec_warps = 0;      // warps the buffer was sized for
   int* d_rcount = nullptr;       // [warps] records written, or -1 - needed

@@ -586,6 +586,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* _
 // ---------------------------------------------------------------------------
 struct ShellSink {
   int4* rec;
+  int* st;             // the point's list start, beside each record
   int* count;          // [warps]
   unsigned* max_seen;  // largest per-warp need of this call
   int R;               // records per warp
@@ -756,8 +757,10 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
       const unsigned em = __ballot_sync(0xffffffffu, emit);
       if (emit) {
         const int slot = fill + __popc(em & lt);
-        if (slot < sink.R)
+        if (slot < sink.R) {
           __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
+          __stcs(sink.st + (size_t)warp * sink.R + slot, s);
+        }
       }
       fill += __popc(em);
     }
@@ -797,6 +800,7 @@ struct ChainOut {
 // Records of the emitting integral pass (rec == nullptr: none this call).
 struct ChainRecords {
   const int4* rec;  // (q, V, mask low, mask high) per recorded point
+  const int* st;    // the point's list start
   const int* count;
   int R;
   const float* state;  // GBMV point state of the integral pass (nullptr: re-sum the lists)
@@ -851,15 +855,25 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
     // recorded points, 32 at a time; lanes over their shaping entries
     const int4* region = rr.rec + (size_t)warp * rr.R;
-    int4 prn = make_int4(0, 0, 0, 0);  // the next batch's records, loaded one batch ahead
-    if (lane < npts) prn = __ldcs(region + lane);
+    const int* sregion = rr.st + (size_t)warp * rr.R;
+    // the next batch's records and list starts, loaded one batch ahead
+    int4 prn = make_int4(0, 0, 0, 0);
+    int psn = 0;
+    if (lane < npts) {
+      prn = __ldcs(region + lane);
+      psn = __ldcs(sregion + lane);
+    }
     for (int b = 0; b < npts; b += kWarp) {
       unsigned mlo = 0u, mhi = 0u;
       int st = 0;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       float V = 0.0f, cq = 0.0f;
       const int4 pr = prn;
-      if (b + kWarp + lane < npts) prn = __ldcs(region + b + kWarp + lane);
+      const int ps = psn;
+      if (b + kWarp + lane < npts) {
+        prn = __ldcs(region + b + kWarp + lane);
+        psn = __ldcs(sregion + b + kWarp + lane);
+      }
       if (b + lane < npts) {
         V = __int_as_float(pr.y);
         mlo = (unsigned)pr.z;
@@ -867,7 +881,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         v = quad.qv[pr.x];
         const float2 w = quad.qw[pr.x];
         cq = fmaf(de.x, w.x, de.y * w.y);
-        st = __ldg(tab.cell + query.cell(xi, v, pr.x)).y;  // a recorded point has a list
+        st = ps;  // written by the integral pass beside the record
       }
       const int len = __popc(mlo) + __popc(mhi);
       int incl = len;
@@ -1208,7 +1222,7 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   const Entries t = entries_of(ctx);
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
-  const ShellSink sink{ctx->d_srec, ctx->d_rcount, ctx->d_rmax, ctx->srec_R};
+  const ShellSink sink{ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->srec_R};
   if (MODEL == GBX_MODEL_GBSW && ctx->records && !count_work)
     gbsw_integral_kernel<Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
@@ -1234,7 +1248,8 @@ void launch_chain_t(Context* ctx, const float4* pos, const ModelConst& m, unsign
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
   ChainOut o{force, stride, ctx->d_dEdR_fx, m.cutoff_chain_quirk && m.cutoff2 > 0.0f, m.cutoff2};
   const bool records = MODEL == GBX_MODEL_GBSW && !ADJ && ctx->records;
-  const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_rcount : nullptr, ctx->srec_R,
+  const ChainRecords rr{records ? ctx->d_srec : nullptr, records ? ctx->d_srec_st : nullptr,
+                        records ? ctx->d_rcount : nullptr, ctx->srec_R,
                         MODEL == GBX_MODEL_GBSW ? nullptr : ctx->d_pstate};
   bool coop = false;
   if constexpr (MODEL != GBX_MODEL_GBSW) {
