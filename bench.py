@@ -12,7 +12,7 @@ A step is one energy + force evaluation of the whole molecule.
   positions copied host->device and forces/energy device->host every step.
 * roofline: the dominant stage, from events the library records around each
   stage on its own stream, against the FP32 pipe (the path has no dense
-  contraction and moves a few MB per step).
+  contraction; its table gathers and point records stay far below the HBM rate).
 * cpu_baseline: the FP64 oracle (a restatement of the reference CPU
   algorithm) on the machine's host cores for the same workload.
 

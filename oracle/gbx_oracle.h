@@ -1,8 +1,8 @@
 /*
  * FP64 CPU oracle for the CHARMM GBSW / GBMV hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA path is compared
- * against; nothing in the product links, loads or calls it.  Only tests/,
+ * TEST INFRASTRUCTURE ONLY.  The CUDA path's results are compared against
+ * it; nothing in the product links, loads or calls it.  Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
  *
  * It restates the reference's CPU algorithms (file:line citations are into

@@ -1,7 +1,8 @@
 """ctypes binding of the FP64 oracle (``gbx_oracle.c``) -- TEST INFRASTRUCTURE.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
-import this module.  It is the checker, never the thing measured or shipped.
+import this module.  It is what results are compared against, never the thing
+measured or shipped.
 """
 from __future__ import annotations
 

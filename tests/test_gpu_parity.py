@@ -4,7 +4,7 @@ the C ABI.  Tolerances (FP32 arithmetic, FP64 Born-radius assembly):
 * lookup tables: bit-exact (counts and ascending lists)
 * Born radii: max relative error <= 1e-4
 * energy: relative error <= 2e-5
-* forces: relative RMS error <= 1e-4 (the benchmark spec's bound)
+* forces: relative RMS error <= 1e-4 (the accuracy target of the path)
 """
 import numpy as np
 import pytest

@@ -39,7 +39,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_reduce_to_the_slowest():
     world, port = 2, _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.start_processes(_rank, args=(world, port, out), nprocs=world, start_method="spawn", join=True)
         res = dict(out)
