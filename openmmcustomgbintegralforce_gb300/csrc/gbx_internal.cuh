@@ -39,6 +39,27 @@ struct TableGeom {
   long long total;  // list entries before capping
 };
 
+// Exact GBSW table, per cell: the list's first (sorted) entry and the cell's
+// (count or -1 if buried, start) record, read together by one 32-byte load.
+struct __align__(32) TightCell {
+  float4 first;
+  int2 cs;
+  int2 pad;
+};
+
+// Two consecutive 16-byte entries at a 32-byte aligned address in one
+// 256-bit non-coherent load (sm_100 and later).
+struct __align__(32) Float4x2 {
+  float4 a, b;
+};
+__device__ __forceinline__ Float4x2 ldg_pair(const void* p) {
+  Float4x2 r;
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z), "=f"(r.b.w)
+      : "l"(p));
+  return r;
+}
+
 // Per-model constants used inside the kernels (FP32 hot path + FP64 exact paths).
 struct ModelConst {
   int model;
@@ -104,9 +125,9 @@ struct Context {
   int* d_tcursor = nullptr;
   int* d_tburied = nullptr;
   int2* d_tcell = nullptr;       // (count or -1 if buried, start)
-  float4* d_tfirst = nullptr;    // per cell: its list's first (sorted) entry
+  TightCell* d_tfirst = nullptr; // per cell: first entry and (count, start)
   int* d_tblock_sums = nullptr;
-  float4* d_tentry = nullptr;    // (x, y, z, R') per list entry
+  float4* d_tentry = nullptr;    // (x, y, z, R') per list entry; lists start at even entries
   int* d_tindex = nullptr;       // atom index per list entry
   bool tight_valid = false;
 

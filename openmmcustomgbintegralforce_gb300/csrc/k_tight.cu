@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
                                                                         float4* __restrict__ entry,
                                                                         int* __restrict__ index,
                                                                         int2* __restrict__ cell,
-                                                                        float4* __restrict__ first,
+                                                                        TightCell* __restrict__ first,
                                                                         const TableGeom* __restrict__ gp, float w,
                                                                         long long cell_cap, long long entry_cap,
                                                                         unsigned* __restrict__ status) {
@@ -209,6 +209,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
       s = start[c];
       bur = cnt > 0 ? buried[c] : 0;
       cell[c] = make_int2(bur ? -1 : cnt, s);
+      first[c].cs = make_int2(bur ? -1 : cnt, s);
       if (bur) count[c] = -1;
     }
     // lists of up to kSortSmall entries: four cells at a time, eight lanes
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
         }
         entry[cs + r] = ge[q];
         index[cs + r] = iq;
-        if (r == 0) first[c0 + src] = ge[q];
+        if (r == 0) first[c0 + src].first = ge[q];
       }
       __syncwarp();
     }
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
         }
         entry[cs + r] = s_e[wib][q];
         index[cs + r] = iq;
-        if (r == 0) first[cc] = s_e[wib][q];
+        if (r == 0) first[cc].first = s_e[wib][q];
       }
       __syncwarp();
     }
@@ -316,7 +317,7 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
     if (blocks > 65535) blocks = 65535;
     tight_members_kernel<false><<<(int)blocks, threads, 0, st>>>(a);
     ++ctx->launches;
-    launch_scan(ctx->d_tcount, ctx->d_tgeom, ctx->d_tblock_sums, ctx->d_tstart, ctx->d_tcursor, cells,
+    launch_scan<true>(ctx->d_tcount, ctx->d_tgeom, ctx->d_tblock_sums, ctx->d_tstart, ctx->d_tcursor, cells,
                 ctx->tentry_cap, ctx->d_status, st);
     ctx->launches += 3;  // the scan's three kernels
     tight_members_kernel<true><<<(int)blocks, threads, 0, st>>>(a);

@@ -28,6 +28,8 @@
 // wraps the point as the reference does and measures minimum-image distances.
 #include <math.h>
 
+#include <type_traits>
+
 #include "gbx_internal.cuh"
 
 namespace gbx {
@@ -50,8 +52,17 @@ struct Entries {
   const int* index;    // atom index of each entry
   long long cell_cap;  // cells allocated: a geometry with more (a table that
                        // outgrew its buffers, not yet resized) is never indexed
-  const float4* first; // exact table: each cell's first list entry (else nullptr)
+  const TightCell* first; // exact table: each cell's first list entry and record (else nullptr)
+  long long entry_cap;    // entries allocated: a table with more was not sorted
+                          // this step, its cell records are an earlier step's
 };
+
+// Cells a query may index: none when the table outgrew either buffer this
+// step (the build then wrote no cell record, and the records left in place
+// may belong to another geometry).
+__device__ __forceinline__ long long usable_cells(const Entries& t) {
+  return t.geom->total > t.entry_cap ? -1 : t.cell_cap;
+}
 
 // ---------------------------------------------------------------------------
 // Cell queries
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
+  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   Work<COUNT> wk;
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* _
   const int g = lane / kGroup, r = lane % kGroup;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
+  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   float J4 = 0.0f, J7 = 0.0f;
@@ -619,6 +630,7 @@ constexpr int kRefill = 128;       // points classified per refill
 constexpr int kRefillBelow = 64;   // refill when fewer entries are pending
 static_assert(kRefillBelow - 1 + kRefill <= kStage, "ring overwrite");
 constexpr int kEnt = 2;            // list entries per lane step, loaded one step ahead (3 and 4 measured slower)
+static_assert(kEnt == 2, "the exact table's lists are read in aligned pairs");
 
 template <class Q, bool EMIT>
 __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
@@ -626,6 +638,9 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
                                                                  float* __restrict__ Jpart, ShellSink sink) {
   __shared__ int3 s_queue[kThreads / kWarp][kStage];  // (q, list start, list length)
   __shared__ int s_long[kThreads / kWarp];  // a shaping entry beyond list position 63
+  // the exact table: lists start at even entries and each cell's record sits
+  // beside its first entry, so both are read 32 bytes at a time
+  constexpr bool kTight = std::is_same<Q, TightQuery>::value;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
@@ -639,7 +654,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
+  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
@@ -664,11 +679,19 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
         if (qc < q1) {
           const float4 vc = quad.qv[qc];
           const long long cell = query.cell(xi, vc, qc);
-          cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
-          // the exact table keeps each cell's first entry by cell: loaded
-          // alongside the cell, not after it
           float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (tab.first && cell >= 0) a0 = __ldg(tab.first + cell);
+          if constexpr (kTight) {
+            // the exact table keeps each cell's first entry beside its
+            // record: one load, not one after the other
+            cs = make_int2(0, 0);
+            if (cell >= 0) {
+              const Float4x2 r = ldg_pair(tab.first + cell);
+              a0 = r.a;
+              cs = make_int2(__float_as_int(r.b.x), __float_as_int(r.b.y));
+            }
+          } else {
+            cs = cell >= 0 ? __ldg(tab.cell + cell) : make_int2(0, 0);
+          }
           if (cs.x == 0) {
             const float2 wc = quad.qw[qc];
             J4 += wc.x;
@@ -676,7 +699,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
           } else if (cs.x > 0) {
             // the list's first entry, the likeliest burying atom, buries most
             // listed points: V = 0 adds nothing, the point is not queued
-            if (!tab.first) a0 = __ldg(tab.e + cs.y);
+            if constexpr (!kTight) a0 = __ldg(tab.e + cs.y);
             const float3 d = query.delta(a0, xi, vc);
             const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
             const float lo = a0.w - m.sw;
@@ -704,9 +727,15 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
         has = true;
         v = quad.qv[q];
         w = quad.qw[q];
+        if constexpr (kTight) {
+          const Float4x2 p = ldg_pair(tab.e + s);
+          an[0] = p.a;
+          an[1] = p.b;
+        } else {
 #pragma unroll
-        for (int u = 0; u < kEnt; ++u)
-          if (u < cnt) an[u] = __ldg(tab.e + s + u);
+          for (int u = 0; u < kEnt; ++u)
+            if (u < cnt) an[u] = __ldg(tab.e + s + u);
+        }
       }
     }
     head = min(head + __popc(need), tail);
@@ -719,9 +748,19 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
       // kEnt list entries per step (entries l .. l + kEnt - 1 were loaded one step ahead)
       float4 cur[kEnt];
 #pragma unroll
-      for (int u = 0; u < kEnt; ++u) {
-        cur[u] = an[u];
-        if (l + kEnt + u < cnt) an[u] = __ldg(tab.e + s + l + kEnt + u);
+      for (int u = 0; u < kEnt; ++u) cur[u] = an[u];
+      if constexpr (kTight) {
+        // l is even here (a point advances kEnt entries per step until it
+        // ends); a pair past an odd list's end reads its padding entry
+        if (l + kEnt < cnt) {
+          const Float4x2 p = ldg_pair(tab.e + s + l + kEnt);
+          an[0] = p.a;
+          an[1] = p.b;
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < kEnt; ++u)
+          if (l + kEnt + u < cnt) an[u] = __ldg(tab.e + s + l + kEnt + u);
       }
 #pragma unroll
       for (int u = 0; u < kEnt; ++u) {
@@ -850,7 +889,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   // the record and the list-walk paths give the same bits
   long long fix = 0, fiy = 0, fiz = 0;
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
+  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
   const int npts = rr.count ? rr.count[warp] : -1;
   if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
     // recorded points, 32 at a time; lanes over their shaping entries
@@ -1086,7 +1125,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
   const float4 xi = pos[i];
   const float2 de = dEdJ[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, tab.cell_cap);
+  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   long long fix = 0, fiy = 0, fiz = 0;
@@ -1208,8 +1247,10 @@ __global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __re
 
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
-    return Entries{ctx->d_tgeom, ctx->d_tcell, ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap, ctx->d_tfirst};
-  return Entries{ctx->d_geom, ctx->d_cell2, ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap, nullptr};
+    return Entries{ctx->d_tgeom, ctx->d_tcell,   ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap, ctx->d_tfirst,
+                   ctx->tentry_cap};
+  return Entries{ctx->d_geom,    ctx->d_cell2,    ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap,
+                 nullptr,        ctx->entry_cap};
 }
 
 int volume_blocks(const Context* ctx) {

@@ -1,5 +1,8 @@
 // Exclusive prefix sum of per-cell counts into CSR offsets (three phases:
 // per-tile sums, a single-block scan of the tile sums, per-tile apply).
+// EVEN rounds each cell's allocation up to an even entry count, so every
+// list starts at an even entry (a 32-byte boundary for 16-byte entries) and
+// a list's entries can be read in aligned pairs without leaving the table.
 // Included by the table translation units; internal linkage in each.
 #pragma once
 
@@ -35,6 +38,12 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* tot
   return base + x - v;
 }
 
+template <bool EVEN>
+__device__ __forceinline__ int scan_alloc(int count) {
+  return EVEN ? (count + 1) & ~1 : count;
+}
+
+template <bool EVEN>
 __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int* __restrict__ count,
                                                                   const TableGeom* __restrict__ gp,
                                                                   int* __restrict__ block_sums, long long cell_cap) {
@@ -43,7 +52,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int* __r
   const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
   int v = 0;
   for (int k = 0; k < kScanItems; ++k)
-    if (base + k < ncell) v += count[base + k];
+    if (base + k < ncell) v += scan_alloc<EVEN>(count[base + k]);
   int total;
   block_exclusive_scan(v, s_warp, &total);
   if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
@@ -66,6 +75,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int* __restrict_
   }
 }
 
+template <bool EVEN>
 __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __restrict__ count,
                                                                   TableGeom* __restrict__ gp,
                                                                   const int* __restrict__ block_sums,
@@ -78,7 +88,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __r
   int v[kScanItems];
   int sum = 0;
   for (int k = 0; k < kScanItems; ++k) {
-    v[k] = (base + k < ncell) ? count[base + k] : 0;
+    v[k] = (base + k < ncell) ? scan_alloc<EVEN>(count[base + k]) : 0;
     sum += v[k];
   }
   int total;
@@ -99,13 +109,14 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __r
 
 
 // Enqueue the three phases; start[ncell] and geom->total receive the sum.
+template <bool EVEN = false>
 inline void launch_scan(const int* count, TableGeom* geom, int* block_sums, int* start, int* cursor,
                         long long cell_cap, long long entry_cap, unsigned* status, cudaStream_t st) {
   long long nb = (cell_cap + (long long)kScanThreads * kScanItems - 1) / ((long long)kScanThreads * kScanItems);
   if (nb < 1) nb = 1;
-  scan_tiles_kernel<<<(int)nb, kScanThreads, 0, st>>>(count, geom, block_sums, cell_cap);
+  scan_tiles_kernel<EVEN><<<(int)nb, kScanThreads, 0, st>>>(count, geom, block_sums, cell_cap);
   scan_top_kernel<<<1, kScanThreads, 0, st>>>(block_sums, (int)nb);
-  scan_apply_kernel<<<(int)nb, kScanThreads, 0, st>>>(count, geom, block_sums, start, cursor, cell_cap, entry_cap,
+  scan_apply_kernel<EVEN><<<(int)nb, kScanThreads, 0, st>>>(count, geom, block_sums, start, cursor, cell_cap, entry_cap,
                                                       status);
 }
 
