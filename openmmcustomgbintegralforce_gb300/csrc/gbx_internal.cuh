@@ -67,6 +67,7 @@ struct ModelConst {
   int cap;
   int skip_empty;
   int nq;
+  int nshell;                // points per radial shell (index = radial * nshell + angular)
   int cutoff_chain_quirk;
   float sw, c1, c3;          // GBSW: u = 1/2 + c1 dr - c3 dr^3, c1 = 3/(4w), c3 = 1/(4w^3)
   float gamma0_lnlambda;     // GBMV-I gamma_j = gamma0 ln(lambda) / R^4

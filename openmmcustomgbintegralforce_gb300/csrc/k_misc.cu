@@ -14,6 +14,7 @@ ModelConst make_model_const(const Context* ctx) {
   m.cap = c.table_cap;
   m.skip_empty = c.skip_empty;
   m.nq = c.n_radial * c.lebedev_order;
+  m.nshell = c.lebedev_order;
   m.cutoff_chain_quirk = c.cutoff_chain_quirk;
   const double w = c.switch_width;
   m.sw = (float)w;

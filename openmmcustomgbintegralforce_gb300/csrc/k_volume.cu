@@ -659,6 +659,24 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   float J4 = 0.0f, J7 = 0.0f;
   int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
   int next = q0;           // warp-uniform: first point not yet classified
+  if constexpr (kTight) {
+    // Radial shells well inside atom i's own burying sphere (r below
+    // R'_i - w by more than FP32 rounding of |v|^2 can reach) hold only
+    // points with V = 0: the exact table lists atom i in every cell they
+    // fall in, so the walk would end on it at the latest.  V = 0 adds
+    // nothing to J and records nothing, so they are skipped unclassified.
+    const float lo = xi.w - m.sw;
+    const int nrad = m.nq / m.nshell;
+    int inner = 0;  // the leading shells that lie inside
+    for (int r0 = 0; r0 < nrad; r0 += kWarp) {
+      const int ir = r0 + lane;
+      const bool in = ir < nrad && quad.qv[ir * m.nshell].w * (1.0f + 1.0f / 1024.0f) < lo;
+      const unsigned out = __ballot_sync(0xffffffffu, !in);
+      inner = r0 + (out ? __ffs(out) - 1 : kWarp);
+      if (out) break;
+    }
+    next = max(q0, inner * m.nshell);
+  }
   int q = 0, s = 0, cnt = 0, l = 0;
   float4 an[kEnt];  // the next kEnt list entries
 #pragma unroll
@@ -858,12 +876,12 @@ __device__ __forceinline__ void push_force(const ChainOut& o, int k, float gx, f
 // GBSW: the force -g on a shaping atom k (unless the cutoff quirk drops it)
 // and +g on atom i, as one fixed-point integer triple: atom i gets the
 // negation of what k gets, so the pair's momentum balances exactly and one
-// conversion serves both.
-__device__ __forceinline__ void push_shaping(const ChainOut& o, const int* __restrict__ index, bool push, float gx,
-                                             float gy, float gz, long long& fix, long long& fiy, long long& fiz) {
+// conversion serves both.  The caller loads k together with the entry, so
+// the two reads overlap instead of the index waiting on the arithmetic.
+__device__ __forceinline__ void push_shaping(const ChainOut& o, int k, bool push, float gx, float gy, float gz,
+                                             long long& fix, long long& fiy, long long& fiz) {
   const long long fx = float_to_fixed_split(-gx), fy = float_to_fixed_split(-gy), fz = float_to_fixed_split(-gz);
   if (push) {
-    const int k = __ldg(index);
     if (fx) atomicAdd(&o.force[k], (unsigned long long)fx);
     if (fy) atomicAdd(&o.force[k + o.stride], (unsigned long long)fy);
     if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
@@ -946,6 +964,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const int l = nth < nlo ? (int)__fns(olo, 0, nth + 1) : 32 + (int)__fns(ohi, 0, nth - nlo + 1);
         const int e = ost + l;
         const float4 a = __ldg(tab.e + e);
+        const int k = __ldg(tab.index + e);
         const float3 d = query.delta(a, xi, ov);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         // the same expressions as the list walk below
@@ -954,7 +973,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
         const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
         const float3 dd = query.delta(a, xi, make_float4(0.f, 0.f, 0.f, 0.f));  // x_k - x_i
         const float ex = dd.x, ey = dd.y, ez = dd.z;
-        push_shaping(out, tab.index + e, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx, gy, gz,
+        push_shaping(out, k, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx, gy, gz,
                      fix, fiy, fiz);
       }
     }
@@ -1011,7 +1030,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
           const float gx = gs * d.x, gy = gs * d.y, gz = gs * d.z;
           const float3 dd = query.delta(a, xi, make_float4(0.f, 0.f, 0.f, 0.f));  // x_k - x_i
           const float ex = dd.x, ey = dd.y, ez = dd.z;
-          push_shaping(out, tab.index + s + l, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx,
+          push_shaping(out, k, !out.quirk || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= out.cutoff2, gx,
                        gy, gz, fix, fiy, fiz);
         }
       } else if (MODEL == GBX_MODEL_GBMV1) {
