@@ -609,6 +609,14 @@ __device__ __forceinline__ float shell_g(const ModelConst& m, float V, float dr)
   return __fdividef(V, u) * du;
 }
 
+// x << n with PTX semantics: a shift of 32 or more gives 0 (two 32-bit
+// halves of the 64-bit mask, each set without a branch on l).
+__device__ __forceinline__ unsigned shl_clamped(unsigned x, unsigned n) {
+  unsigned r;
+  asm("shl.b32 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(n));
+  return r;
+}
+
 // True if list entry l is atom i itself: its inline position is bitwise
 // atom i's, and only then is the index read.
 __device__ __forceinline__ bool is_self(const float4 a, const float4 xi, const int* __restrict__ index, int l, int i) {
@@ -682,7 +690,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
 #pragma unroll
   for (int u = 0; u < kEnt; ++u) an[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   bool has = false;
-  unsigned long long shaped = 0;  // bit l: in-shell entry l is not atom i
+  unsigned sm_lo = 0u, sm_hi = 0u;  // bit l of (hi:lo): in-shell entry l is not atom i
   float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
   float2 w = make_float2(0.f, 0.f);
   float V = 1.0f;
@@ -740,7 +748,8 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
         s = e.y;
         cnt = e.z;
         l = 0;
-        shaped = 0;
+        sm_lo = 0u;
+        sm_hi = 0u;
         V = 1.0f;
         has = true;
         v = quad.qv[q];
@@ -795,8 +804,9 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
             const float dr = r2 * rsqrtf(r2) - a.w;
             V *= fmaf(dr, fmaf(-m.c3 * dr, dr, m.c1), 0.5f);
             if (EMIT && !is_self(a, xi, tab.index + s, l, i)) {
-              if (l < 64) shaped |= 1ull << l;
-              else s_long[wib] = 1;
+              sm_lo |= shl_clamped(1u, (unsigned)l);
+              sm_hi |= shl_clamped(1u, (unsigned)(l - 32));
+              if (l >= 64) s_long[wib] = 1;
             }
           }
           fin = ++l == cnt;
@@ -810,12 +820,12 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
     }
     if (EMIT) {
       // slots in finishing order (the chain rule's sums do not depend on it)
-      const bool emit = fin && shaped != 0ull && V != 0.0f;
+      const bool emit = fin && (sm_lo | sm_hi) != 0u && V != 0.0f;
       const unsigned em = __ballot_sync(0xffffffffu, emit);
       if (emit) {
         const int slot = fill + __popc(em & lt);
         if (slot < sink.R) {
-          __stcs(region + slot, make_int4(q, __float_as_int(V), (int)(unsigned)shaped, (int)(unsigned)(shaped >> 32)));
+          __stcs(region + slot, make_int4(q, __float_as_int(V), (int)sm_lo, (int)sm_hi));
           __stcs(sink.st + (size_t)warp * sink.R + slot, s);
         }
       }
@@ -1133,7 +1143,9 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
 // their atom's force and accumulate the point's pull on atom i.  Lanes first
 // take 32 points' cells together, then the warp walks those points in turn.
 template <int MODEL, class Q, bool ADJ>
-__global__ void __launch_bounds__(kThreads) gbmv_chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
+// Six blocks per SM (at most 80 registers): the occupancy this latency-bound
+// kernel was measured fastest at; left to itself the compiler takes 87.
+__global__ void __launch_bounds__(kThreads, 6) gbmv_chain_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                               Quad quad, ModelConst m, int chunk, int n_chunks,
                                                               const float2* __restrict__ dEdJ, ChainOut out,
                                                               const float* __restrict__ state) {
