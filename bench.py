@@ -78,7 +78,7 @@ FLOPS_PAIR = 39.0
 
 # DRAM bytes (read + write) per launch of each stage's main kernel, from one ncu
 # capture of the same workload (the files named in TRAFFIC_SOURCE).
-TRAFFIC = {"gbsw50k": {"integrals": 1268.1e6 + 714.2e6, "pair": 3.1e6 + 0.06e6, "chain_rule": 1012.6e6 + 0.12e6},
+TRAFFIC = {"gbsw50k": {"integrals": 1641.7e6 + 715.4e6, "pair": 3.04e6 + 0.04e6, "chain_rule": 1089.6e6 + 0.07e6},
            "gbmv10k": {"integrals": 129.6e6 + 213.7e6, "chain_rule": 317.1e6 + 5.6e6}}
 TRAFFIC_SOURCE = {"gbsw50k": "profiles/kernels_gbsw50k.md", "gbmv10k": "profiles/gbmv_kernels_gbmv10k.md"}
 
