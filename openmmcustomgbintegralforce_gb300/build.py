@@ -23,8 +23,8 @@ REPO = os.path.dirname(PKG)
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def _nvcc() -> str:
@@ -82,7 +82,7 @@ def build_cuda(verbose: bool = False, extra_flags=None) -> str:
             logs = list(ex.map(_run, jobs))
     out = library_path()
     if jobs or _newer(objs, out):
-        _run([nvcc, *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lcuda"])
+        _run([nvcc, *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lcuda", "-lgomp"])
     if verbose:
         for line in logs:
             if line.strip():

@@ -1,6 +1,7 @@
 // C-ABI entry points (include/gbx.h): context lifecycle, parameters, the
 // execute pipeline and result queries.  No exception crosses this boundary.
 #include <math.h>
+#include <omp.h>
 #include <string.h>
 
 #include <algorithm>
@@ -793,14 +794,31 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
 
 namespace {
 
+// The host-buffer call's two O(N) host loops (positions in, forces out) move
+// about 110 bytes per atom through memory; from this many atoms on they are
+// split over a few host threads (each element is written by one thread, so
+// the results do not depend on the split).
+constexpr int kHostParallelAtoms = 16384;
+int host_threads() {
+  static const int t = std::max(1, std::min(8, omp_get_num_procs()));
+  return t;
+}
+
 // Host positions -> pinned float4 staging (checked for finite values in the same pass).
 gbx_status host_stage(Context* ctx, const double* positions) {
   const int n = ctx->n;
   bool finite = true;
-  for (int i = 0; i < n; ++i) {
+  float4* hp = ctx->h_pos;
+  auto stage = [&](int i) {
     const double x = positions[3 * i], y = positions[3 * i + 1], z = positions[3 * i + 2];
-    finite &= std::isfinite(x) & std::isfinite(y) & std::isfinite(z);
-    ctx->h_pos[i] = make_float4((float)x, (float)y, (float)z, 0.f);
+    hp[i] = make_float4((float)x, (float)y, (float)z, 0.f);
+    return std::isfinite(x) && std::isfinite(y) && std::isfinite(z);
+  };
+  if (n >= kHostParallelAtoms) {
+#pragma omp parallel for reduction(&& : finite) num_threads(host_threads())
+    for (int i = 0; i < n; ++i) finite = stage(i) && finite;
+  } else {
+    for (int i = 0; i < n; ++i) finite = stage(i) && finite;
   }
   if (!finite) {
     ctx->last_error = "non-finite position";
@@ -851,9 +869,18 @@ gbx_status host_results(Context* ctx, double* forces, double* energy, bool optim
     ctx->last_error = "non-finite Born radius";
     return GBX_ERR_NONFINITE;
   }
-  if (forces)
-    for (int i = 0; i < n; ++i)
-      for (int k = 0; k < 3; ++k) forces[3 * i + k] += gbx::fixed_to_double(ctx->h_force_fx[(size_t)k * n + i]);
+  if (forces) {
+    const unsigned long long* hf = ctx->h_force_fx;
+    auto add = [&](int i) {
+      for (int k = 0; k < 3; ++k) forces[3 * i + k] += gbx::fixed_to_double(hf[(size_t)k * n + i]);
+    };
+    if (n >= kHostParallelAtoms) {
+#pragma omp parallel for num_threads(host_threads())
+      for (int i = 0; i < n; ++i) add(i);
+    } else {
+      for (int i = 0; i < n; ++i) add(i);
+    }
+  }
   if (energy) *energy = e;
   if (!isfinite(e)) {
     ctx->last_error = "non-finite energy";
