@@ -1,5 +1,5 @@
 // Batched evaluation of many independent molecules (uneven atom counts,
-// GBSW and GBMV mixed): the C4 form of the hot path.
+// GBSW and GBMV mixed): the batched form of the hot path.
 //
 // Each molecule keeps its own context (tables, record regions, quadrature),
 // so every kernel of the single-molecule path is reused unchanged.  A call
@@ -16,6 +16,8 @@
 // gbx_batch_tune is the autotuner: it times the captured batch for several
 // stream counts and quadrature chunkings (quadrature points per warp) and
 // keeps the fastest.
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -272,10 +274,23 @@ gbx_status gbx_batch_execute(gbx_batch* b, int flags, void* stream) {
   return gbx::run(b, stream ? (cudaStream_t)stream : b->own, (flags & GBX_EXEC_CHECK) != 0);
 }
 
+// The host loops over every atom of the batch run on up to 8 host threads
+// (each element is written by one thread: the results do not depend on it).
 gbx_status gbx_batch_execute_host(gbx_batch* b, const double* positions, double* forces, double* energies) {
   if (!b || !positions) return GBX_ERR_INVALID_ARGUMENT;
-  for (long long k = 0; k < b->total; ++k)
-    b->h_pos[k] = make_float4((float)positions[3 * k], (float)positions[3 * k + 1], (float)positions[3 * k + 2], 0.f);
+  const int threads = std::max(1, std::min(8, omp_get_num_procs()));
+  bool finite = true;
+  float4* hp = b->h_pos;
+#pragma omp parallel for reduction(&& : finite) num_threads(threads)
+  for (long long k = 0; k < b->total; ++k) {
+    const double x = positions[3 * k], y = positions[3 * k + 1], z = positions[3 * k + 2];
+    hp[k] = make_float4((float)x, (float)y, (float)z, 0.f);
+    finite = std::isfinite(x) && std::isfinite(y) && std::isfinite(z) && finite;
+  }
+  if (!finite) {
+    b->last_error = "non-finite position";
+    return GBX_ERR_INVALID_ARGUMENT;
+  }
   BCUDA(b, cudaMemcpyAsync(b->d_pos, b->h_pos, sizeof(float4) * b->total, cudaMemcpyHostToDevice, b->own));
   BTRY(gbx::run(b, b->own, false));
   BCUDA(b, cudaMemcpyAsync(b->h_force, b->d_force, sizeof(unsigned long long) * 3 * b->total, cudaMemcpyDeviceToHost,
@@ -283,7 +298,9 @@ gbx_status gbx_batch_execute_host(gbx_batch* b, const double* positions, double*
   BCUDA(b, cudaMemcpyAsync(b->h_energy, b->d_energy, sizeof(double) * b->mols.size(), cudaMemcpyDeviceToHost,
                            b->own));
   BCUDA(b, cudaStreamSynchronize(b->own));
-  for (size_t m = 0; m < b->mols.size(); ++m) {
+  const int nm = (int)b->mols.size();
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+  for (int m = 0; m < nm; ++m) {
     const int n = b->mols[m]->n;
     const unsigned long long* f = b->h_force + 3 * b->off[m];
     if (forces)

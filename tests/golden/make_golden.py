@@ -38,7 +38,7 @@ def main():
     save("quadrature.npz", gl24_x=gl24[0], gl24_w=gl24[1], gl32_x=gl32[0], gl32_w=gl32[1],
          leb26=R.lebedev(3), leb38=R.lebedev(4), leb50=R.lebedev(5), leb110=R.lebedev(8))
 
-    # CharmmGBSWForce on the Reference platform (C0 model settings)
+    # CharmmGBSWForce on the Reference platform (its built-in 24x38 quadrature and constants)
     qoff, qrad, qw = R.gbsw_quadrature()
     for n, seed, with_table in ((200, 3, True), (1000, 7, False)):
         g = make_globule(n, seed=seed, cache=False)

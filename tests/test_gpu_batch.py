@@ -123,3 +123,18 @@ def test_replay_after_a_molecule_parameter_change(setup):
     c.set_particle_parameters(gs[k].charge, gs[k].radius)
     E0, _ = b.execute_host(X)
     assert abs(E0[k] / E[k] - 1) > 1e-2
+
+
+def test_non_finite_position_is_rejected_before_upload(setup):
+    """A NaN among the batch's host positions is refused on the host (no
+    upload, no launch), and the next call with good positions is unaffected."""
+    from openmmcustomgbintegralforce_gb300._lib import GBXError
+
+    gs, ms, b, X = setup
+    E0, F0 = b.execute_host(X)
+    Xbad = X.copy()
+    Xbad[len(X) // 2, 1] = np.nan
+    with pytest.raises(GBXError):
+        b.execute_host(Xbad)
+    E1, F1 = b.execute_host(X)
+    assert np.array_equal(E0, E1) and np.array_equal(F0, F1)
