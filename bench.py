@@ -93,9 +93,21 @@ def workloads():
                         desc="GBSW 10,000-atom globule, 32x110 quadrature (profiling case)"),
         "gbmv10k": dict(n=10000, seed=2027, model=None, gbmv=2,
                         desc="GBMV-II 10,000-atom globule, 24x50 quadrature"),
+        "gbmv1_10k": dict(n=10000, seed=2027, model=None, gbmv=1,
+                          desc="GBMV-I 10,000-atom globule, 24x50 quadrature"),
+        "gbsw5k_adjoint": dict(n=5000, seed=2029, model=GBModel.charmm_gbsw(), adjoint=True,
+                               desc="GBSW 5,000-atom globule, 24x38 quadrature, adjoint (dE/dx, dE/dq, dE/dR, "
+                                    "dE/dalpha)"),
         "gbsw1k": dict(n=1000, seed=7, model=GBModel.charmm_gbsw(),
                        desc="GBSW 1,000-atom globule, 24x38 quadrature (reference CPU case)"),
     }
+
+
+def workload_config(name, w, model, world, jitter_A):
+    """The `config` of both arms' JSON lines: the same keys and values."""
+    return {"workload": name, "desc": w["desc"], "atoms": w["n"], "quadrature_points": model.n_quad,
+            "l2": "flushed (256 MiB write) between steps", "parallelism": "replicas" if world > 1 else "single",
+            "jitter_A": jitter_A}
 
 
 def model_for(w, g):
@@ -214,9 +226,10 @@ def oracle_baseline(model, g, sample_s: float = 20.0):
 
 
 def run_reference(args, world, rank):
-    """Reference arm: the FP64 oracle port of the reference CPU algorithm
-    (the reference's own classes need the reference tree, absent on the GPU
-    host, and O(N^2) memory: 60 GB at 50k atoms)."""
+    """Reference arm: the FP64 oracle port of the reference CPU algorithm on
+    all host cores, one whole energy + force evaluation per step (the
+    reference's own classes need the reference tree, absent on the GPU host,
+    and O(N^2) memory: 60 GB at 50k atoms)."""
     if rank != 0:
         return
     from oracle import oracle as O
@@ -225,27 +238,28 @@ def run_reference(args, world, rank):
     g = make_globule(w["n"], seed=w["seed"])
     model = model_for(w, g)
     cores = os.cpu_count() or 1
-    # each step evaluates every `stride`-th atom's quadrature points, chain
-    # rule and pair row (a bounded, unbiased sample of one full evaluation)
-    stride = max(1, w["n"] // 6000)
-    orc = O.Oracle(model, nthreads=cores, atom_stride=stride)
+    orc = O.Oracle(model, nthreads=cores)
     times = []
+    wall0 = time.perf_counter()
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         orc.energy_forces(g.positions, g.charge, g.radius)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
-            times.append(dt * stride)
-    v = 1.0 / float(np.mean(times))
+            times.append(dt)
+    wall = time.perf_counter() - wall0
+    ms = 1000.0 * float(np.mean(times))
+    v = 1000.0 / ms
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic seeded globule", "config": {"workload": args.workload, "desc": w["desc"],
-                                                           "atoms": w["n"], "quadrature_points": model.n_quad},
+            "data": "synthetic seeded globule (no dataset)",
+            "config": workload_config(args.workload, w, model, world, args.jitter),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"every {stride}-th atom's points, chain rule and pair row per step "
-                                       f"({w['n']} atoms), time scaled by {stride}"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": f"one whole FP64 evaluation per step ({w['n']} atoms, {model.n_quad} points, "
+                                       f"OpenMP on {cores} host cores)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
     print(json.dumps(line))
 
 
@@ -345,6 +359,120 @@ def measure_batched(gs, steps: int):
                                    "force_rel_rms_max": max(b_ for _, b_ in errs)}}
 
 
+# The other BASELINE configurations, measured in the same run as extra keys of
+# the line: (workload, timed steps, jitter in A between steps, check vs FP64).
+CONFIG_RUNS = {
+    "c0_gbsw1k": ("gbsw1k", 50, 0.0),
+    "c1_gbmv2_10k_1000_jittered": ("gbmv10k", 1000, 0.01),
+    "c1_gbmv1_10k_1000_jittered": ("gbmv1_10k", 1000, 0.01),
+    "c2_gbsw50k_cutoff2nm": ("gbsw50k_cutoff", 20, 0.0),
+    "c3_gbsw5k_adjoint": ("gbsw5k_adjoint", 20, 0.0),
+}
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def measure_config(name, steps, jitter_A, dev, flush):
+    """One configuration end to end on device-resident inputs: evals/s from
+    CUDA events around each call (L2 flushed between calls; with jitter the
+    positions take a fresh N(0, jitter) step before every call, accumulating
+    as in MD), e2e through host arrays, and the error of the last
+    conformation against the FP64 oracle, whose time is this
+    configuration's CPU baseline."""
+    import torch
+
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_CHECK, EXEC_ENERGY, EXEC_FORCES, Context
+    from oracle import oracle as O
+
+    w = workloads()[name]
+    g = make_globule(w["n"], seed=w["seed"])
+    model = model_for(w, g)
+    n = g.n
+    adjoint = bool(w.get("adjoint"))
+    ctx = Context(model, n)
+    ctx.set_particle_parameters(g.charge, g.radius)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    posq = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    posq[:, :3] = torch.from_numpy(g.positions.astype(np.float32)).to(dev)
+    force = torch.zeros(3 * n, dtype=torch.int64, device=dev)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    out = {k: torch.zeros(s_, dtype=torch.float64, device=dev) for k, s_ in
+           (("energy", 1), ("forces", 3 * n), ("dEdq", n), ("dEdR", n), ("dEdalpha", 2))}
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(w["seed"])
+
+    def step(flags):
+        if adjoint:
+            ctx.adjoint_device(posq.data_ptr(), out["energy"].data_ptr(), out["forces"].data_ptr(),
+                               out["dEdq"].data_ptr(), out["dEdR"].data_ptr(), out["dEdalpha"].data_ptr(),
+                               flags & EXEC_CHECK, sptr)
+        else:
+            ctx.execute_device(posq.data_ptr(), force.data_ptr(), n, energy.data_ptr(), flags, sptr)
+
+    torch.cuda.synchronize()
+    for _ in range(3):
+        step(EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    launches0 = ctx.launches()
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.fill_(float(k))
+            if jitter_A > 0:
+                posq[:, :3] += 0.1 * jitter_A * torch.randn(posq[:, :3].shape, generator=gen, device=dev)
+            starts[k].record(stream)
+            step(EXEC_FORCES | EXEC_ENERGY)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches() - launches0
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    x = posq[:, :3].double().cpu().numpy()
+    res = {"workload": name, "desc": w["desc"], "atoms": n, "quadrature_points": model.n_quad, "steps": steps,
+           "evals_per_s": 1000.0 / ms, "ms_per_step": ms, "gpu_launches_per_step": launches / steps,
+           "jitter_A": jitter_A, "l2": "flushed (256 MiB write) between steps"}
+    if adjoint:
+        # host arrays in, every gradient out
+        ctx.adjoint(x)
+        t = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            got = ctx.adjoint(x)
+            t.append(time.perf_counter() - t0)
+        res["e2e"] = {"evals_per_s": 1.0 / float(np.mean(t)), "call": "gbx_adjoint_host"}
+        t0 = time.perf_counter()
+        ref = O.Oracle(model, nthreads=os.cpu_count() or 1).energy_forces(x, g.charge, g.radius, adjoint=True)
+        dt = time.perf_counter() - t0
+        res["err_vs_fp64"] = {"energy_rel": abs(got["energy"] / ref["energy"] - 1.0),
+                              "force_rel_rms": rel_rms(got["forces"], ref["forces"]),
+                              "dEdq_rel_rms": rel_rms(got["dEdq"], ref["dEdq"]),
+                              "dEdR_rel_rms": rel_rms(got["dEdR"], ref["dEdR"]),
+                              "dEdalpha_rel_max": float(np.abs(got["dEdalpha"] / ref["dEdalpha"] - 1).max())}
+    else:
+        ctx.execute_host(x)
+        t = []
+        for _ in range(5 if n > 20000 else 20):
+            t0 = time.perf_counter()
+            E, F = ctx.execute_host(x)
+            t.append(time.perf_counter() - t0)
+        res["e2e"] = {"evals_per_s": 1.0 / float(np.mean(t)), "call": "gbx_execute_host",
+                      "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 3 * 8 + 8}
+        t0 = time.perf_counter()
+        ref = O.Oracle(model, nthreads=os.cpu_count() or 1).energy_forces(x, g.charge, g.radius)
+        dt = time.perf_counter() - t0
+        res["err_vs_fp64"] = {"energy_rel": abs(E / ref["energy"] - 1.0),
+                              "force_rel_rms": rel_rms(F, ref["forces"])}
+    res["err_vs_fp64"]["conformation"] = (f"last of {steps} jittered (N(0, {jitter_A} A) per step, accumulated)"
+                                          if jitter_A > 0 else "the workload's globule")
+    res["cpu_baseline"] = {"evals_per_s": 1.0 / dt, "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": "the FP64 oracle's evaluation of the checked conformation"}
+    ctx.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,6 +482,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-molecule measurement")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' measurements")
     ap.add_argument("--jitter", type=float, default=0.0,
                     help="A: fresh N(0, jitter) position noise before every timed step (MD-like back-to-back "
                          "evaluations); the FP64 error is then taken on the last jittered conformation")
@@ -454,7 +583,8 @@ def main():
 
     peaks, peak_src = measured_peaks()
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sms * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
     points = float(n) * model.n_quad
     if model.model == 0:
         integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
@@ -476,7 +606,7 @@ def main():
                 "traffic": TRAFFIC.get(args.workload, {}).get(dominant),
                 "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                                    + TRAFFIC_SOURCE[args.workload]) if args.workload in TRAFFIC_SOURCE else None,
-                "peak_source": "nominal FP32 (152 SM x 128 lanes x 2 flop x max SM clock); "
+                "peak_source": f"nominal FP32 ({sms} SM x 128 lanes x 2 flop x max SM clock); "
                                f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
                 "per_stage_tflops": cand, "stage_ms": stage_ms,
                 "work": {"volume_evals": work["volume_evals"], "shell_evals": work["shell_evals"],
@@ -525,13 +655,13 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded globule (no dataset)",
-                "config": {"workload": args.workload, "desc": w["desc"], "atoms": n,
-                           "quadrature_points": model.n_quad, "l2": "flushed (256 MiB write) between steps",
-                           "parallelism": "replicas" if world > 1 else "single", "jitter_A": args.jitter},
+                "config": workload_config(args.workload, w, model, world, args.jitter),
                 "gpu_launches": launches, "gpu_launches_per_step": launches / args.steps, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "err_vs_fp64": err, "clocks": clk, "wall_s": wall}
         if batch_set is not None:
             line["batched"] = measure_batched(batch_set, max(3, min(args.steps, 10)))
+        if not args.no_configs and world == 1:
+            line["configs"] = {k: measure_config(wl, st, jit, dev, flush) for k, (wl, st, jit) in CONFIG_RUNS.items()}
         print(json.dumps(line))
 
 

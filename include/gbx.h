@@ -9,8 +9,8 @@
  * objects: it is what CalcCharmmGBSWForceKernel / CalcCharmmGBMVForceKernel
  * (openmmapi/include/openmm/charmmKernels.h:49-129) hold between
  * initialize(), execute() and copyParametersToContext().  An OpenMM plugin
- * adapter is a thin C++ layer that forwards those three
- * virtuals to the calls below.
+ * adapter is a thin C++ layer that forwards those three virtuals to the
+ * calls below.
  *
  * Units: nm, e, kJ/mol.  Device buffers follow OpenMM's CUDA conventions:
  * positions as float4 (x, y, z, unused), forces as 64-bit fixed point
@@ -266,7 +266,8 @@ GBX_API gbx_status gbx_get_stage_times(gbx_context* ctx, double* ms, int max_sta
  * stage, from caller-supplied device arrays: posq float4[n] (x, y, z, -),
  * charge float[n], born float[n] (Born radii, nm).  force_fixed (fixed point,
  * stride as in gbx_execute) and *energy are ADDED to; dEdB double[n] is
- * written when not NULL.  cutoff <= 0: all pairs.
+ * written when not NULL.  cutoff <= 0: all pairs.  Distances are plain
+ * differences (no minimum image): non-periodic systems only.
  *
  * Nothing is allocated: the scratch is one static device array of about
  * 1 MiB that every GPU loading the library holds until exit, which limits
@@ -274,7 +275,9 @@ GBX_API gbx_status gbx_get_stage_times(gbx_context* ctx, double* ms, int max_sta
  * All calls on a device share that array, so calls whose kernels overlap on
  * the GPU (different streams, host threads) race: serialise them.  The first
  * call on each device looks the array's device address up
- * (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is remembered per CUDA context, so a call after a device
+ * reset looks it up again in the new context. */
 GBX_API gbx_status gbx_pair_noalloc(const void* posq, const float* charge, const float* born, int num_atoms,
                                     double prefactor, double cutoff, unsigned long long* force_fixed,
                                     int force_stride, double* energy, double* dEdB, void* stream);

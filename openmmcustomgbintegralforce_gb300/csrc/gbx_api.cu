@@ -162,10 +162,10 @@ gbx_status upload_quadrature(Context* ctx) {
 }
 
 // The volume kernels run one warp per (atom, chunk of quadrature points)
-// with lanes over points: enough warps for ~48 per SM on 152 SMs, and
-// >= 64 points (2 per lane) per chunk.
-int choose_chunks(int n, int Q) {
-  int c = (152 * 48 + n - 1) / n;
+// with lanes over points: enough warps for ~48 per SM on the device's SMs,
+// and >= 64 points (2 per lane) per chunk.
+int choose_chunks(int n, int Q, int sms) {
+  int c = (sms * 48 + n - 1) / n;
   c = std::max(1, std::min(c, std::max(1, Q / 64)));
   return c;
 }
@@ -173,7 +173,7 @@ int choose_chunks(int n, int Q) {
 gbx_status alloc_atom_buffers(Context* ctx) {
   const int n = ctx->n;
   const int Q = ctx->cfg.n_radial * ctx->cfg.lebedev_order;
-  ctx->n_chunks = choose_chunks(n, Q);
+  ctx->n_chunks = choose_chunks(n, Q, ctx->sms);
   GBX_TRY(dalloc(ctx, &ctx->d_radius, n));
   GBX_TRY(dalloc(ctx, &ctx->d_charge, n));
   GBX_TRY(dalloc(ctx, &ctx->d_par, n));
@@ -617,7 +617,9 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
   ctx->n = num_atoms;
   ctx->alpha0 = (float)cfg->alpha0;
   ctx->alpha1 = (float)cfg->alpha1;
-  if (cudaGetDevice(&ctx->device) != cudaSuccess) {
+  if (cudaGetDevice(&ctx->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+      ctx->sms < 1) {
     delete ctx;
     return GBX_ERR_CUDA;
   }

@@ -317,9 +317,17 @@ gbx_status gbx_batch_tune(gbx_batch* b, int* streams_chosen, int* chunk_scale_ch
   if (!b->sized) BTRY(gbx::run_checked(b, main));
   std::vector<int> base_chunks(b->mols.size());
   for (size_t m = 0; m < b->mols.size(); ++m) base_chunks[m] = b->mols[m]->n_chunks;
-  cudaEvent_t t0, t1;
-  BCUDA(b, cudaEventCreate(&t0));
-  BCUDA(b, cudaEventCreate(&t1));
+  // destroyed on every exit, early error returns included
+  struct Events {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~Events() {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+    }
+  } ev;
+  BCUDA(b, cudaEventCreate(&ev.a));
+  BCUDA(b, cudaEventCreate(&ev.b));
+  cudaEvent_t t0 = ev.a, t1 = ev.b;
   double best = 1e30;
   int best_s = b->n_streams, best_div = 1;
   const int nm = (int)b->mols.size();
@@ -345,8 +353,6 @@ gbx_status gbx_batch_tune(gbx_batch* b, int* streams_chosen, int* chunk_scale_ch
       }
     }
   }
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
   for (size_t m = 0; m < b->mols.size(); ++m) BTRY(gbx::set_chunks(b->mols[m], std::max(1, base_chunks[m] / best_div)));
   BTRY(gbx::make_streams(b, best_s));
   BTRY(gbx::run_checked(b, main));

@@ -83,6 +83,7 @@ struct Context {
   gbx_config cfg{};
   int n = 0;
   int device = 0;
+  int sms = 0;  // multiprocessors of `device` (grid sizing), read once at creation
   std::string last_error;
 
   // quadrature (host, FP64) and device copies
@@ -272,7 +273,7 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
 int pair_energy_parts(int n, int segments);
-int pair_segments(int n);
+int pair_segments(int n, int sms);
 ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);

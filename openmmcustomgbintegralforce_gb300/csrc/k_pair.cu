@@ -694,10 +694,10 @@ SymArgs sym_args(int n) {
 
 int pair_energy_parts(int n, int segments) { return ((n + kPairThreads - 1) / kPairThreads) * segments; }
 
-int pair_segments(int n) {
-  // enough CTAs for ~2 waves on 152 SMs with 8 resident CTAs each
+int pair_segments(int n, int sms) {
+  // enough CTAs for ~2 waves on the device's SMs with 8 resident CTAs each
   const int iblocks = (n + kPairThreads - 1) / kPairThreads;
-  int s = (2 * 152 * 8 + iblocks - 1) / iblocks;
+  int s = (2 * sms * 8 + iblocks - 1) / iblocks;
   const int max_s = (n + kJTile - 1) / kJTile;
   if (s > max_s) s = max_s;
   if (s < 1) s = 1;
@@ -705,9 +705,9 @@ int pair_segments(int n) {
 }
 
 // The same kernel on caller-supplied buffers (used by the allocation-free
-// entry point): energy_part needs pair_energy_parts(n, pair_segments(n))
+// entry point): energy_part needs pair_energy_parts(n, pair_segments(n, sms))
 // doubles and dEdB must be zero on entry.
-cudaError_t launch_pair_raw(const float4* pos, const float* charge, const float2* born, int n, float pref,
+cudaError_t launch_pair_raw(const float4* pos, const float* charge, const float2* born, int n, int sms, float pref,
                             float cutoff2, unsigned long long* force, int stride, unsigned long long* dEdB,
                             double* energy_part, cudaStream_t stream) {
   PairArgs a;
@@ -715,7 +715,7 @@ cudaError_t launch_pair_raw(const float4* pos, const float* charge, const float2
   a.charge = charge;
   a.born = born;
   a.n = n;
-  a.segments = pair_segments(n);
+  a.segments = pair_segments(n, sms);
   a.pref = pref;
   a.cutoff2 = cutoff2;
   a.force = force;
@@ -768,7 +768,7 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
     sort_count_kernel<<<nb, 256, 0, st>>>(pos, n, sg, ctx->d_cell_of, ctx->d_scount);
     sort_scan_kernel<<<1, kBoxThreads, 0, st>>>(ctx->d_scount, sg, ctx->d_sstart, ctx->d_scursor);
     sort_scatter_kernel<<<nb, 256, 0, st>>>(ctx->d_cell_of, n, ctx->d_sstart, ctx->d_scursor, ctx->d_perm_tmp);
-    sort_cells_by_atom_kernel<<<152 * 8, kSymThreads, 0, st>>>(ctx->d_scount, ctx->d_sstart, sg, ctx->d_perm_tmp,
+    sort_cells_by_atom_kernel<<<ctx->sms * 8, kSymThreads, 0, st>>>(ctx->d_scount, ctx->d_sstart, sg, ctx->d_perm_tmp,
                                                                ctx->d_perm);
     ctx->launches += 5;
     a.perm = ctx->d_perm;

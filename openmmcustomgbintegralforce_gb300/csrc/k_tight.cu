@@ -323,7 +323,7 @@ gbx_status launch_tight_build(Context* ctx, const float4* pos) {
     tight_members_kernel<true><<<(int)blocks, threads, 0, st>>>(a);
     ++ctx->launches;
     long long sb = (cells + kSortWarps * kWarp - 1) / (kSortWarps * kWarp);
-    if (sb > 152 * 64) sb = 152 * 64;
+    if (sb > (long long)ctx->sms * 64) sb = (long long)ctx->sms * 64;
     tight_sort_kernel<<<(int)sb, kSortWarps * kWarp, 0, st>>>(ctx->d_tcount, ctx->d_tstart, ctx->d_tburied,
                                                                ctx->d_tentry, ctx->d_tindex, ctx->d_tcell, ctx->d_tfirst,
                                                                ctx->d_tgeom,

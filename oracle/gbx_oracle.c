@@ -585,27 +585,11 @@ int orc_integral_chain(const orc_config* cfg, const orc_table* t, int n, const d
 /* Canonical energy + forces                                                 */
 /* ------------------------------------------------------------------------- */
 
-int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const double* charge, const double* radius,
-                      double* energy, double* forces, double* born, double* integrals_out, double* dEdB_out,
-                      double* dEdq, double* dEdR, double* dEdalpha, orc_work* work) {
-  if (cfg->n_int != 2 || cfg->orders[0] != 4 || cfg->orders[1] != 7) return -4;
-  orc_table t;
-  int rc = orc_table_build(cfg, n, pos, radius, &t);
-  if (rc) return rc;
-  double* I = (double*)calloc((size_t)2 * n, sizeof(double));
-  double* B = (double*)calloc((size_t)n, sizeof(double));
-  double* dEdB = (double*)calloc((size_t)n, sizeof(double));
-  double* F = (double*)calloc((size_t)3 * n, sizeof(double));
-  double* dq = (double*)calloc((size_t)n, sizeof(double));
-  if (!I || !B || !dEdB || !F || !dq) return -3;
-  orc_integrals(cfg, &t, n, pos, radius, I, work);
-  /* Born radii, CharmmReferenceGBSW.cpp:591-593 */
-  const double eta = cfg->r0, eta4 = eta * eta * eta * eta;
-  for (int i = 0; i < n; ++i) {
-    double inv = cfg->alpha0 * (1.0 / eta - I[i]) + cfg->alpha1 * pow((1.0 / (4.0 * eta4) - I[n + i]), 1.0 / 4.0);
-    B[i] = 1.0 / inv;
-  }
-  /* pair term, CharmmReferenceGBSW.cpp:237-283 (j >= i; self term 1/2) */
+/* The GB pair term for given Born radii, CharmmReferenceGBSW.cpp:237-283:
+ * every pair j >= i (the self term halved), energy, pair forces, dE/dB and
+ * dE/dq ADDED to the outputs (any of them may be NULL except energy). */
+int orc_pair_terms(const orc_config* cfg, int n, const double* pos, const double* charge, const double* B,
+                   double* energy, double* forces, double* dEdB_out, double* dEdq_out, orc_work* work) {
   const double pref = cfg->pref;
   double E = 0.0, npairs = 0;
   const int nt = nthreads_of(cfg);
@@ -662,15 +646,43 @@ int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const dou
   }
   for (int tid = 0; tid < nt; ++tid) {
     for (int a = 0; a < n; ++a) {
-      dEdB[a] += dbbuf[(size_t)tid * n + a];
-      dq[a] += qbuf[(size_t)tid * n + a];
+      if (dEdB_out) dEdB_out[a] += dbbuf[(size_t)tid * n + a];
+      if (dEdq_out) dEdq_out[a] += qbuf[(size_t)tid * n + a];
     }
-    for (int a = 0; a < 3 * n; ++a) F[a] += fbuf[(size_t)tid * n * 3 + a];
+    if (forces)
+      for (int a = 0; a < 3 * n; ++a) forces[a] += fbuf[(size_t)tid * n * 3 + a];
   }
   free(dbbuf);
   free(fbuf);
   free(qbuf);
   if (work) work->pairs += npairs;
+  *energy += E;
+  return 0;
+}
+
+int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const double* charge, const double* radius,
+                      double* energy, double* forces, double* born, double* integrals_out, double* dEdB_out,
+                      double* dEdq, double* dEdR, double* dEdalpha, orc_work* work) {
+  if (cfg->n_int != 2 || cfg->orders[0] != 4 || cfg->orders[1] != 7) return -4;
+  orc_table t;
+  int rc = orc_table_build(cfg, n, pos, radius, &t);
+  if (rc) return rc;
+  double* I = (double*)calloc((size_t)2 * n, sizeof(double));
+  double* B = (double*)calloc((size_t)n, sizeof(double));
+  double* dEdB = (double*)calloc((size_t)n, sizeof(double));
+  double* F = (double*)calloc((size_t)3 * n, sizeof(double));
+  double* dq = (double*)calloc((size_t)n, sizeof(double));
+  if (!I || !B || !dEdB || !F || !dq) return -3;
+  double E = 0.0;
+  orc_integrals(cfg, &t, n, pos, radius, I, work);
+  /* Born radii, CharmmReferenceGBSW.cpp:591-593 */
+  const double eta = cfg->r0, eta4 = eta * eta * eta * eta;
+  for (int i = 0; i < n; ++i) {
+    double inv = cfg->alpha0 * (1.0 / eta - I[i]) + cfg->alpha1 * pow((1.0 / (4.0 * eta4) - I[n + i]), 1.0 / 4.0);
+    B[i] = 1.0 / inv;
+  }
+  rc = orc_pair_terms(cfg, n, pos, charge, B, &E, F, dEdB, dq, work);
+  if (rc) return rc;
   /* chain rule through the integrals: dE/dI4 = dE/dB * B^2 alpha0,
    * dE/dI7 = dE/dB * B^2 alpha1/4 (..)^(-3/4)  (CharmmReferenceGBSW.cpp:597-611) */
   double* dEdI = (double*)calloc((size_t)2 * n, sizeof(double));

@@ -117,6 +117,12 @@ int orc_energy_forces(const orc_config* cfg, int n, const double* pos, const dou
                       double* integrals, double* dEdB, double* dEdq, double* dEdR,
                       double* dEdalpha, orc_work* work);
 
+/* The pair term alone for given Born radii B (CharmmReferenceGBSW.cpp:237-283):
+ * pair energy (self terms included), pair forces [n*3], dE/dB, dE/dq, all
+ * ADDED to; outputs other than energy may be NULL. */
+int orc_pair_terms(const orc_config* cfg, int n, const double* pos, const double* charge, const double* B,
+                   double* energy, double* forces, double* dEdB, double* dEdq, orc_work* work);
+
 #ifdef __cplusplus
 }
 #endif

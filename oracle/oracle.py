@@ -103,6 +103,7 @@ def lib():
         L.orc_integrals.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp]
         L.orc_integral_chain.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp, vp]
         L.orc_energy_forces.argtypes = [vp, ctypes.c_int, vp, vp, vp] + [vp] * 9
+        L.orc_pair_terms.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
         L.orc_table_query.argtypes = [vp, vp]
         L.orc_table_query.restype = ctypes.c_int64
         _LIB = L
@@ -233,3 +234,20 @@ class Oracle:
         if adjoint:
             out.update({"dEdq": dq, "dEdR": dR, "dEdalpha": da})
         return out
+
+    def pair_terms(self, pos, charge, born):
+        """The pair term alone for given Born radii (CharmmReferenceGBSW.cpp:237-283):
+        energy (self terms included), pair forces, dE/dB and dE/dq."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        q = np.ascontiguousarray(charge, dtype=np.float64)
+        B = np.ascontiguousarray(born, dtype=np.float64)
+        n = len(B)
+        E = np.zeros(1)
+        F = np.zeros(3 * n)
+        dB = np.zeros(n)
+        dq = np.zeros(n)
+        rc = lib().orc_pair_terms(ctypes.byref(self.cfg), n, _ptr(pos), _ptr(q), _ptr(B), _ptr(E), _ptr(F), _ptr(dB),
+                                  _ptr(dq), None)
+        if rc:
+            raise RuntimeError(f"oracle pair_terms failed ({rc})")
+        return {"energy": float(E[0]), "forces": F.reshape(n, 3), "dEdB": dB, "dEdq": dq}

@@ -14,7 +14,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libgbref.so")
-REF_ROOT = os.environ.get("GBX_REFERENCE_ROOT", "/root/reference")
+# the reference tree: GBX_REFERENCE_ROOT, else a sibling of this repository
+REF_ROOT = os.environ.get("GBX_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                       "reference"))
 
 _LIB = None
 

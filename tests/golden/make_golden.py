@@ -3,7 +3,7 @@ CPU classes, compiled in place from the reference tree (oracle/Makefile.ref).
 
     python tests/golden/make_golden.py
 
-Needs the reference tree (GBX_REFERENCE_ROOT, default /root/reference); the
+Needs the reference tree (GBX_REFERENCE_ROOT, default: a sibling of the repository); the
 fixtures it writes are committed so that the CPU tests can pin the oracle
 where the reference is absent.  Inputs are seeded globules rounded to
 float32, so the FP32 device path sees the same numbers.

@@ -4,10 +4,12 @@ It exists for callers that cannot let a library allocate device memory, such
 as an engine that owns all device memory through its own pool.  These
 checks call it through the C ABI, twice in a row on the same inputs (the
 static scratch keeps the previous call's contents, so the second call shows
-that everything that must start at zero is cleared), and compare each result
-with what the regular entry point reports for the same molecule: the total
-GB energy (the pair term carries all of it, self terms included) and dE/dB.
-The tolerances are the parity suite's.
+that everything that must start at zero is cleared), with and without a
+pair cutoff, and compare each result with what the regular entry point
+reports for the same molecule -- the total GB energy (the pair term carries
+all of it, self terms included) and dE/dB -- and the pair forces with the
+FP64 oracle's pair term evaluated on the same Born radii.  The tolerances
+are the parity suite's.
 """
 import ctypes
 
@@ -17,17 +19,24 @@ import pytest
 from openmmcustomgbintegralforce_gb300 import _lib
 from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
 E_TOL = 2e-5
 G_TOL = 1e-4
+F_TOL = 1e-4
 
 
-def test_noalloc_pair_matches_regular_entry_point_twice():
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+@pytest.mark.parametrize("cutoff", [0.0, 1.0])
+def test_noalloc_pair_matches_regular_entry_point_twice(cutoff):
     torch = pytest.importorskip("torch")
     g = make_globule(1000, seed=19)
-    m = GBModel.charmm_gbsw()
+    m = GBModel.charmm_gbsw(cutoff=cutoff)
     ctx = _lib.Context(m, g.n)
     ctx.set_particle_parameters(g.charge, g.radius)
     E_ref, _ = ctx.execute_host(g.positions)
@@ -50,15 +59,21 @@ def test_noalloc_pair_matches_regular_entry_point_twice():
         dEdB = torch.zeros(n, dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
         st = lib.gbx_pair_noalloc(ctypes.c_void_p(posq.data_ptr()), ctypes.c_void_p(q.data_ptr()),
-                                  ctypes.c_void_p(B.data_ptr()), n, m.pref, 0.0,
+                                  ctypes.c_void_p(B.data_ptr()), n, m.pref, cutoff,
                                   ctypes.c_void_p(force.data_ptr()), stride, ctypes.c_void_p(energy.data_ptr()),
                                   ctypes.c_void_p(dEdB.data_ptr()), ctypes.c_void_p(stream))
         torch.cuda.synchronize()
         assert st == 0, _lib.STATUS_NAMES.get(st, st)
         results.append((float(energy.cpu()[0]), dEdB.cpu().numpy().copy(), force.cpu().numpy().copy()))
-    for E, g_, _ in results:
+    # the pair term alone in FP64 on the same (FP32-rounded) Born radii
+    ref = O.Oracle(m).pair_terms(g.positions, g.charge, born.astype(np.float32).astype(np.float64))
+    for E, g_, f in results:
         assert abs(E / E_ref - 1) < E_TOL
-        assert np.sqrt(((g_ - dEdB_ref) ** 2).sum() / (dEdB_ref ** 2).sum()) < G_TOL
+        assert abs(E / ref["energy"] - 1) < E_TOL
+        assert rel_rms(g_, dEdB_ref) < G_TOL
+        fx = f.astype(np.float64) / 2.0 ** 32
+        F = np.stack([fx[:n], fx[stride:stride + n], fx[2 * stride:2 * stride + n]], axis=1)
+        assert rel_rms(F, ref["forces"]) < F_TOL
     # the two calls agree bit for bit: nothing leaks from the first call's scratch
     assert results[0][0] == results[1][0]
     assert np.array_equal(results[0][1], results[1][1])
