@@ -45,7 +45,10 @@ typedef enum {
   GBX_ERR_TABLE_TOO_LARGE = 6, /* lookup grid would exceed its limits (reference: length > 1000 nm) */
   GBX_ERR_NOT_READY = 7,      /* result queried before an execute */
   GBX_ERR_TIMEOUT = 8,        /* a device-side wait gave up (batched persistent kernel) */
-  GBX_ERR_EXCEEDS_STATIC_SCRATCH = 9 /* gbx_pair_noalloc: more atoms than its static scratch holds */
+  GBX_ERR_EXCEEDS_STATIC_SCRATCH = 9, /* gbx_pair_noalloc: more atoms than its static scratch holds */
+  GBX_ERR_STALE_RESULT = 10   /* gbx_execute: an earlier unchecked call's lookup table outgrew its
+                                 buffers, so that call's results lacked the volume terms; the
+                                 buffers were grown and the reporting call's results are complete */
 } gbx_status;
 
 /* Volume models: CharmmGBMVForce::GBIntegralType (CharmmGBMVForce.h:99-104). */
@@ -73,7 +76,10 @@ enum {
   GBX_EXEC_CHECK = 4,   /* synchronise the stream and report device status (table
                            capacity, non-finite values); grows buffers and
                            re-runs once if a capacity limit was hit */
-  GBX_EXEC_COUNT_WORK = 8 /* count (point, listed atom) evaluations (gbx_get_work) */
+  GBX_EXEC_COUNT_WORK = 8, /* count (point, listed atom) evaluations (gbx_get_work) */
+  GBX_EXEC_POSQ_DOUBLE = 16, /* gbx_execute: posq is double4 (OpenMM's double precision mode) */
+  GBX_EXEC_ENERGY_FLOAT = 32 /* gbx_execute: energy points to one float, added to (OpenMM's
+                                single precision energy buffer) */
 };
 
 typedef struct {
@@ -140,13 +146,30 @@ GBX_API gbx_status gbx_set_box(gbx_context* ctx, const double box[3]);
  * on the device.  force_fixed: fixed-point buffer, ADDED to, components at
  * [0, stride), [stride, 2 stride), [2 stride, 3 stride).  energy: one double on
  * the device, ADDED to.  Either may be NULL when not requested by flags.
- * Without GBX_EXEC_CHECK the call does not synchronise: if the atoms spread
- * so far that the lookup table outgrows its buffers, that call's results lack
- * the volume terms (the oversized table is never indexed) until a call with
- * GBX_EXEC_CHECK resizes it; callers that cannot check every step use
- * gbx_execute_host or the batch API, which detect this and re-run. */
+ * GBX_EXEC_POSQ_DOUBLE: posq is double4; GBX_EXEC_ENERGY_FLOAT: energy is a
+ * float (OpenMM's precision modes).
+ *
+ * Without GBX_EXEC_CHECK the call neither synchronises nor is silently
+ * wrong: every call's last kernel publishes the table's size and status to
+ * mapped host memory, which the next calls read without waiting.  Buffers
+ * grow ahead of need once the largest table seen reaches 90 % of them; if
+ * the atoms nevertheless outgrew the table within one call, that call lacks
+ * the volume terms (the oversized table is never indexed) and a later call
+ * (the next one once the GPU has finished it) grows the buffers, runs
+ * checked and returns GBX_ERR_STALE_RESULT; a non-finite Born radius is
+ * reported the same way as GBX_ERR_NONFINITE.  GBX_EXEC_CHECK synchronises
+ * and reports the call's own status. */
 GBX_API gbx_status gbx_execute(gbx_context* ctx, const void* posq, unsigned long long* force_fixed,
                                int force_stride, double* energy, int flags, void* stream);
+
+/* The caller's atom order (OpenMM reorders atoms for locality): slot k of
+ * posq and of the force buffer holds atom atom_index[k] (a permutation of
+ * 0..n-1; host array, copied; NULL: identity).  Parameters stay in atom
+ * order and the lookup-table lists keep ascending atom order, as the
+ * reference CPU classes (CharmmReferenceGBSW.cpp:440-514) -- so a reorder
+ * changes no result.  Replaces the parameter re-upload the reference's
+ * CUDA kernel does on a reorder.  Call it whenever the order changes. */
+GBX_API gbx_status gbx_set_atom_order(gbx_context* ctx, const int* atom_index);
 
 /* Same computation on host arrays (Reference-platform style): positions
  * double[3n]; forces double[3n] ADDED to; *energy set.  Copies inside.  Once

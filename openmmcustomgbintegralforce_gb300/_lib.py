@@ -18,13 +18,16 @@ STATUS_NAMES = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported",
     5: "non-finite result", 6: "lookup table too large", 7: "no result yet", 8: "device wait timed out",
     9: "more atoms than the static scratch of gbx_pair_noalloc holds",
+    10: "an earlier unchecked call lacked the volume terms (its lookup table outgrew its buffers)",
 }
 EXEC_FORCES, EXEC_ENERGY, EXEC_CHECK, EXEC_COUNT_WORK = 1, 2, 4, 8
+EXEC_POSQ_DOUBLE, EXEC_ENERGY_FLOAT = 16, 32
 
 # every symbol include/gbx.h declares
 EXPORTED = (
     "gbx_status_string", "gbx_version", "gbx_config_preset", "gbx_create", "gbx_destroy", "gbx_last_error",
-    "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_execute_host",
+    "gbx_set_particle_parameters", "gbx_set_global_parameters", "gbx_set_box", "gbx_execute", "gbx_set_atom_order",
+    "gbx_execute_host",
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
     "gbx_adjoint_host", "gbx_adjoint", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
@@ -124,6 +127,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_set_particle_parameters.argtypes = [vp, vp, vp]
     L.gbx_set_global_parameters.argtypes = [vp, cd, cd]
     L.gbx_set_box.argtypes = [vp, vp]
+    L.gbx_set_atom_order.argtypes = [vp, vp]
     L.gbx_execute.argtypes = [vp, vp, vp, ci, vp, ci, vp]
     L.gbx_execute_host.argtypes = [vp, vp, vp, vp, ci]
     L.gbx_get_born_radii.argtypes = [vp, vp]
@@ -209,6 +213,16 @@ class Context:
 
     def set_global_parameters(self, alpha0: float, alpha1: float):
         self._check(self.lib.gbx_set_global_parameters(self.h, float(alpha0), float(alpha1)))
+
+    def set_atom_order(self, atom_index):
+        """Slot k of the device positions / forces holds atom atom_index[k] (None: identity)."""
+        if atom_index is None:
+            self._check(self.lib.gbx_set_atom_order(self.h, None))
+            return
+        a = np.ascontiguousarray(atom_index, dtype=np.int32)
+        if a.shape != (self.n,):
+            raise GBXError(1, "atom_index must have one entry per particle")
+        self._check(self.lib.gbx_set_atom_order(self.h, a.ctypes.data_as(ctypes.c_void_p)))
 
     def set_box(self, box):
         b = np.ascontiguousarray(box, dtype=np.float64)

@@ -190,8 +190,14 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_energy_part, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_energy_fx, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_tile_box, 2 * (((size_t)n + 31) / 32)));
-  if (ctx->cfg.model != GBX_MODEL_GBSW)
+  if (ctx->cfg.model != GBX_MODEL_GBSW) {
     GBX_TRY(dalloc(ctx, &ctx->d_pstate, (size_t)n * Q * (ctx->cfg.model == GBX_MODEL_GBMV1 ? 1 : 5)));
+    GBX_TRY(dalloc(ctx, &ctx->d_pcell, (size_t)n * Q));
+    GBX_TRY(dalloc(ctx, &ctx->d_prank, (size_t)n * Q));
+    GBX_TRY(dalloc(ctx, &ctx->d_porder, (size_t)n * Q));
+    GBX_TRY(dalloc(ctx, &ctx->d_sval, (size_t)n * Q));
+    GBX_TRY(dalloc(ctx, &ctx->d_pgeom, 1));
+  }
   if (ctx->cfg.cutoff > 0) {
     GBX_TRY(dalloc(ctx, &ctx->d_perm, n));
     GBX_TRY(dalloc(ctx, &ctx->d_perm_tmp, n));
@@ -220,6 +226,11 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_status, sizeof(unsigned)));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_energy, sizeof(double)));
   GBX_CUDA(cudaEventCreateWithFlags(&ctx->srec_ev, cudaEventDisableTiming));
+  GBX_TRY(dalloc(ctx, &ctx->d_pub, 5));
+  GBX_CUDA(cudaMemset(ctx->d_pub, 0, sizeof(unsigned long long) * 5));
+  GBX_CUDA(cudaHostAlloc((void**)&ctx->h_pub, sizeof(gbx::StatusRecord), cudaHostAllocMapped));
+  memset(ctx->h_pub, 0, sizeof(gbx::StatusRecord));
+  GBX_CUDA(cudaHostGetDevicePointer((void**)&ctx->h_pub_dev, ctx->h_pub, 0));
   return GBX_OK;
 }
 
@@ -302,6 +313,11 @@ gbx_status grow_table(Context* ctx, long long cells, long long entries) {
     GBX_TRY(dalloc(ctx, &ctx->d_cell_cursor, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_cell2, cap));
     GBX_TRY(dalloc(ctx, &ctx->d_block_sums, cap / (1024 * 8) + 2));
+    if (ctx->cfg.model != GBX_MODEL_GBSW) {
+      GBX_TRY(dalloc(ctx, &ctx->d_pcount, cap));
+      GBX_TRY(dalloc(ctx, &ctx->d_pstart, cap + 1));
+      GBX_TRY(dalloc(ctx, &ctx->d_pblock_sums, cap / (1024 * 8) + 2));
+    }
     ctx->cell_cap = cap;
   }
   if (entries > ctx->entry_cap) {
@@ -455,6 +471,7 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_energy_reduce(ctx, energy, adjoint));
   GBX_TRY(mark());
+  GBX_TRY(gbx::launch_publish_status(ctx));
   ctx->have_result = true;
   if (check) {
     unsigned st = 0;
@@ -487,6 +504,37 @@ void set_model_params(Context* ctx, std::vector<float>& wpar, std::vector<float2
       par[i] = make_float2((float)(C - 100.0 * R * R), (float)R);
     }
   }
+}
+
+// Reads the status the device published for earlier unchecked calls (no
+// synchronisation).  A call whose lookup table outgrew its buffers ran
+// without the volume terms: *stale tells the caller to run this call checked
+// (which grows the buffers) and report it.  Buffers are also grown ahead of
+// need once the largest table seen reaches 90 % of them.
+gbx_status poll_status(Context* ctx, bool* stale, bool* nonfinite) {
+  *stale = *nonfinite = false;
+  if (!ctx->h_pub) return GBX_OK;
+  const volatile gbx::StatusRecord* r = ctx->h_pub;
+  const unsigned long long ov = r->overflows, nf = r->nonfinite, mc = r->max_cells, me = r->max_entries;
+  if (ov > ctx->pub_seen_overflows) {
+    ctx->pub_seen_overflows = ov;
+    *stale = true;
+  }
+  if (nf > ctx->pub_seen_nonfinite) {
+    ctx->pub_seen_nonfinite = nf;
+    *nonfinite = true;
+  }
+  if (!tables_sized(ctx)) return GBX_OK;
+  const long long cap = ctx->use_tight ? ctx->tcell_cap : ctx->cell_cap;
+  const long long ecap = ctx->use_tight ? ctx->tentry_cap : ctx->entry_cap;
+  const long long want_c = (long long)(mc + mc / 9 + 1), want_e = (long long)(me + me / 9 + 1);
+  if ((mc > 0 && want_c > cap) || (me > 0 && want_e > ecap)) {
+    if (want_c > ((long long)1 << 31) || want_e > 0x7fffffffLL) return GBX_OK;  // a checked call reports it
+    GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->use_tight) GBX_TRY(grow_tight(ctx, std::max(want_c, cap), std::max(want_e, ecap)));
+    else GBX_TRY(grow_table(ctx, std::max(want_c, cap), std::max(want_e, ecap)));
+  }
+  return GBX_OK;
 }
 
 }  // namespace
@@ -541,6 +589,7 @@ const char* gbx_status_string(gbx_status s) {
     case GBX_ERR_NOT_READY: return "no result yet";
     case GBX_ERR_TIMEOUT: return "device wait timed out";
     case GBX_ERR_EXCEEDS_STATIC_SCRATCH: return "more atoms than the static scratch of gbx_pair_noalloc holds (65536)";
+    case GBX_ERR_STALE_RESULT: return "an earlier unchecked call lacked the volume terms (its lookup table outgrew its buffers)";
   }
   return "unknown status";
 }
@@ -660,7 +709,9 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
                   ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
-                  ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate};
+                  ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate,
+                  ctx->d_pcell, ctx->d_prank, ctx->d_porder, ctx->d_sval, ctx->d_pcount, ctx->d_pstart,
+                  ctx->d_pblock_sums, ctx->d_pgeom, ctx->d_slot_of, ctx->d_pub};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k <= Context::kStages; ++k)
@@ -670,6 +721,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
   if (ctx->h_rmax) cudaFreeHost(ctx->h_rmax);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->h_energy) cudaFreeHost(ctx->h_energy);
+  if (ctx->h_pub) cudaFreeHost(ctx->h_pub);
   if (ctx->srec_ev) cudaEventDestroy(ctx->srec_ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -740,35 +792,59 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
   if ((flags & GBX_EXEC_FORCES) && (!force_fixed || force_stride < ctx->n)) return GBX_ERR_INVALID_ARGUMENT;
   if ((flags & GBX_EXEC_ENERGY) && !energy) return GBX_ERR_INVALID_ARGUMENT;
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
-  unsigned long long* f = force_fixed;
-  int stride = force_stride;
-  if (!(flags & GBX_EXEC_FORCES)) {  // forces not wanted: computed into (cleared) internal scratch
-    f = ctx->d_force_fx;
-    stride = ctx->n;
-  }
-  double* e = (flags & GBX_EXEC_ENERGY) ? energy : ctx->d_energy;
-  const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0, forces = (flags & GBX_EXEC_FORCES) != 0;
-  const bool check = (flags & GBX_EXEC_CHECK) || !tables_sized(ctx);
-  const float4* p4 = reinterpret_cast<const float4*>(posq);
-  if (check || count || ctx->timing) {
-    if (!forces) GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
-    return run_pipeline(ctx, p4, f, stride, e, check, false, count, forces);
-  }
+  const bool forces = (flags & GBX_EXEC_FORCES) != 0, want_e = (flags & GBX_EXEC_ENERGY) != 0;
+  const bool count = (flags & GBX_EXEC_COUNT_WORK) != 0;
+  const bool permuted = ctx->d_slot_of != nullptr;
+  const bool efloat = want_e && (flags & GBX_EXEC_ENERGY_FLOAT);
+  // the pipeline's own buffers where the caller's cannot take its output
+  // directly: forces not wanted or in another atom order, a float energy
+  const bool internal_f = !forces || permuted, internal_e = !want_e || efloat;
+  unsigned long long* f = internal_f ? ctx->d_force_fx : force_fixed;
+  const int stride = internal_f ? ctx->n : force_stride;
+  double* e = internal_e ? ctx->d_energy : energy;
+  bool stale = false, nonfinite = false;
+  GBX_TRY(poll_status(ctx, &stale, &nonfinite));
+  const bool check = (flags & GBX_EXEC_CHECK) || !tables_sized(ctx) || stale;
+  auto body = [&]() -> gbx_status {
+    ctx->in_double = (flags & GBX_EXEC_POSQ_DOUBLE) != 0;
+    ctx->in_permuted = permuted;
+    gbx_status st = GBX_OK;
+    if (internal_f && cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream))
+      st = GBX_ERR_CUDA;
+    if (st == GBX_OK && internal_e && cudaMemsetAsync(ctx->d_energy, 0, sizeof(double), ctx->stream))
+      st = GBX_ERR_CUDA;
+    if (st == GBX_OK) st = run_pipeline(ctx, static_cast<const float4*>(posq), f, stride, e, check, false, count, forces);
+    if (st == GBX_OK && ((forces && permuted) || efloat))
+      st = gbx::launch_finish_outputs(ctx, forces && permuted ? force_fixed : nullptr, force_stride,
+                                      efloat ? reinterpret_cast<float*>(energy) : nullptr);
+    ctx->in_double = ctx->in_permuted = false;
+    return st;
+  };
+  auto report = [&](gbx_status st) -> gbx_status {
+    if (st != GBX_OK) return st;
+    if (stale) {
+      ctx->last_error = "an earlier unchecked call's lookup table outgrew its buffers, so that call lacked the "
+                        "volume terms; the buffers were grown and this call ran checked";
+      return GBX_ERR_STALE_RESULT;
+    }
+    if (nonfinite) {
+      ctx->last_error = "an earlier unchecked call produced a non-finite Born radius";
+      return GBX_ERR_NONFINITE;
+    }
+    return GBX_OK;
+  };
+  if (check || count || ctx->timing) return report(body());
   // unchecked: one CUDA graph of the whole call, captured on first use
-  const Context::GraphKey key{posq, f, stride, e, flags & (GBX_EXEC_FORCES | GBX_EXEC_ENERGY), ctx->stream};
+  const Context::GraphKey key{posq, force_fixed, force_stride, energy, flags & ~GBX_EXEC_CHECK, ctx->stream};
   if (!ctx->graph || !(key == ctx->graph_key)) {
     drop_graph(ctx);
     GBX_TRY(fix_chain_records(ctx));
     if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       (void)cudaGetLastError();  // a stream that cannot be captured: launch directly
-      if (!forces) GBX_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream));
-      return run_pipeline(ctx, p4, f, stride, e, false, false, false, forces);
+      return report(body());
     }
     const long long before = ctx->launches;
-    gbx_status s = GBX_OK;
-    if (!forces && cudaMemsetAsync(f, 0, sizeof(unsigned long long) * 3 * ctx->n, ctx->stream) != cudaSuccess)
-      s = GBX_ERR_CUDA;
-    if (s == GBX_OK) s = run_pipeline(ctx, p4, f, stride, e, false, false, false, forces);
+    gbx_status s = body();
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
     ctx->graph_kernels = ctx->launches - before;  // captured, not yet run
@@ -789,6 +865,36 @@ gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long
   GBX_CUDA(cudaGraphLaunch(ctx->graph, ctx->stream));
   ctx->launches += ctx->graph_kernels;
   ctx->have_result = true;
+  return report(GBX_OK);
+}
+
+gbx_status gbx_set_atom_order(gbx_context* handle, const int* atom_index) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
+  const int n = ctx->n;
+  if (!atom_index) {
+    if (ctx->d_slot_of) {
+      drop_graph(ctx);
+      GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+      cudaFree(ctx->d_slot_of);
+      ctx->d_slot_of = nullptr;
+    }
+    return GBX_OK;
+  }
+  std::vector<int> slot_of(n, -1);
+  for (int k = 0; k < n; ++k) {
+    const int a = atom_index[k];
+    if (a < 0 || a >= n || slot_of[a] >= 0) {
+      ctx->last_error = "atom_index must be a permutation of 0..n-1";
+      return GBX_ERR_INVALID_ARGUMENT;
+    }
+    slot_of[a] = k;
+  }
+  if (!ctx->d_slot_of) GBX_TRY(dalloc(ctx, &ctx->d_slot_of, n));  // the captured graphs read the old layout
+  // the order is read by the kernels at run time: an update between calls
+  // needs no new graph, only the copy ordered after earlier work
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+  GBX_CUDA(cudaMemcpy(ctx->d_slot_of, slot_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
   return GBX_OK;
 }
 

@@ -25,6 +25,16 @@ enum : unsigned {
   kStatusTimeout = 16u,       // bounded device wait expired
 };
 
+// Status of the device calls, published by the last kernel of every call
+// into mapped host memory (monotone counters; seq written last).
+struct StatusRecord {
+  unsigned long long seq;          // calls published
+  unsigned long long overflows;    // calls whose lookup table outgrew its buffers
+  unsigned long long nonfinite;    // calls with a non-finite Born radius
+  unsigned long long max_cells;    // largest table geometry seen (cells)
+  unsigned long long max_entries;  // largest list-entry total seen
+};
+
 // Lookup-table geometry, computed on the device each step.
 struct TableGeom {
   double min[3];
@@ -155,6 +165,16 @@ struct Context {
   int* d_scursor = nullptr;
   int4* d_sgeom = nullptr;                    // cutoff: spatial grid geometry
   float* d_pstate = nullptr;                  // GBMV: per-point sums kept for the chain rule
+  // GBMV points binned by lookup-table cell (k_gbmv.cu)
+  int* d_pcell = nullptr;                     // [n Q] the point's cell or -1
+  int* d_prank = nullptr;                     // [n Q] slot within the cell
+  int* d_porder = nullptr;                    // [n Q] point id per slot
+  float* d_sval = nullptr;                    // [n Q] solvent fraction by point id
+  int* d_pcount = nullptr;                    // [cell_cap] points per cell
+  int* d_pstart = nullptr;                    // [cell_cap + 1] first slot per cell
+  int* d_pblock_sums = nullptr;               // scan scratch
+  TableGeom* d_pgeom = nullptr;               // the point scan's cell count and total
+  bool gbmv_cells = false;                    // this call's GBMV passes run by cell
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]
@@ -212,6 +232,17 @@ struct Context {
   static constexpr int kStages = 8;
   cudaEvent_t ev[kStages + 1] = {};
 
+  // caller-facing layout of the device call
+  int* d_slot_of = nullptr;       // internal atom i -> the caller's slot (gbx_set_atom_order)
+  bool in_permuted = false;       // this call reads and writes through d_slot_of
+  bool in_double = false;         // this call's positions are double4
+
+  // status of unchecked device calls, read without synchronising
+  unsigned long long* d_pub = nullptr;  // [5] device-side counters of StatusRecord
+  StatusRecord* h_pub = nullptr;        // mapped pinned record
+  StatusRecord* h_pub_dev = nullptr;    // its device address
+  unsigned long long pub_seen_overflows = 0, pub_seen_nonfinite = 0;
+
   // host staging
   float4* h_pos = nullptr;                 // pinned
   unsigned long long* h_force_fx = nullptr; // pinned
@@ -266,7 +297,9 @@ gbx_status pipeline(Context* ctx, const float4* posq, unsigned long long* force,
 gbx_status set_chunks(Context* ctx, int chunks);
 gbx_status fix_chain_records(Context* ctx);
 
-gbx_status launch_stage_positions(Context* ctx, const float4* posq);
+gbx_status launch_stage_positions(Context* ctx, const void* posq);
+gbx_status launch_finish_outputs(Context* ctx, unsigned long long* force, int stride, float* energy_float);
+gbx_status launch_publish_status(Context* ctx);
 gbx_status launch_table_build(Context* ctx, const float4* pos);
 gbx_status launch_tight_build(Context* ctx, const float4* pos);
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
@@ -277,6 +310,10 @@ int pair_segments(int n, int sms);
 ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
+bool gbmv_cells_apply(const Context* ctx);
+gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const ModelConst& m);
+gbx_status launch_gbmv_cells_chain(Context* ctx, const float4* pos, const ModelConst& m, unsigned long long* force,
+                                   int stride, bool adjoint);
 gbx_status launch_energy_reduce(Context* ctx, double* energy, bool adjoint);
 gbx_status launch_adjoint_out(Context* ctx, double* energy, double* forces, double* dEdq, double* dEdR,
                               double* dEdalpha);

@@ -39,13 +39,62 @@ namespace {
 // Internal positions: x, y, z and the model's main per-atom parameter in .w
 // (GBSW: R' = (R + 0.03) 0.952, CharmmReferenceGBSW.cpp:625; GBMV-I:
 // gamma_j = gamma0 ln(lambda) / R^4, GBMVIntegralTypeI.cpp:168; GBMV-II:
-// C_j = 10 P1 R + P2, GBMVIntegralTypeII.cpp:179).
-__global__ void stage_positions_kernel(const float4* __restrict__ in, int n, const float* __restrict__ wpar,
-                                       float4* __restrict__ out) {
+// C_j = 10 P1 R + P2, GBMVIntegralTypeII.cpp:179), from the caller's float4
+// or double4 positions (OpenMM's single / double precision posq).  With an
+// atom order set, internal atom i is read from the caller's slot slot_of[i].
+template <bool DBL>
+__global__ void stage_positions_kernel(const void* __restrict__ in, int n, const int* __restrict__ slot_of,
+                                       const float* __restrict__ wpar, float4* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float4 p = in[i];
-  out[i] = make_float4(p.x, p.y, p.z, wpar[i]);
+  const int k = slot_of ? slot_of[i] : i;
+  float x, y, z;
+  if (DBL) {
+    const double4 p = static_cast<const double4*>(in)[k];
+    x = (float)p.x;
+    y = (float)p.y;
+    z = (float)p.z;
+  } else {
+    const float4 p = static_cast<const float4*>(in)[k];
+    x = p.x;
+    y = p.y;
+    z = p.z;
+  }
+  out[i] = make_float4(x, y, z, wpar[i]);
+}
+
+// The caller's outputs of a call that ran on internal buffers: forces added
+// to the caller's slots (each slot written by one thread), the energy added
+// to a float.
+__global__ void finish_outputs_kernel(int n, const int* __restrict__ slot_of,
+                                      const unsigned long long* __restrict__ fint, unsigned long long* __restrict__ fout,
+                                      int stride, const double* __restrict__ e_int, float* __restrict__ e_float) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && e_float) *e_float += (float)*e_int;
+  if (i >= n || !fout) return;
+  const int k = slot_of ? slot_of[i] : i;
+  for (int c = 0; c < 3; ++c) fout[(size_t)c * stride + k] += fint[(size_t)c * n + i];
+}
+
+// The call's device status, published to mapped host memory so that a later
+// call can read it without synchronising: counts of table overflows and of
+// non-finite results, and the largest table seen (cells, list entries).
+__global__ void publish_status_kernel(const unsigned* __restrict__ status, const TableGeom* __restrict__ geom,
+                                      unsigned long long* __restrict__ dev, StatusRecord* host) {
+  const unsigned st = *status;
+  if (st & (kStatusTableCells | kStatusTableEntries | kStatusSegmentTooLong)) ++dev[1];
+  if (st & kStatusNonFinite) ++dev[2];
+  const unsigned long long c = (unsigned long long)geom->ncell, e = (unsigned long long)geom->total;
+  if (c > dev[3]) dev[3] = c;
+  if (e > dev[4]) dev[4] = e;
+  ++dev[0];
+  volatile StatusRecord* h = host;
+  h->overflows = dev[1];
+  h->nonfinite = dev[2];
+  h->max_cells = dev[3];
+  h->max_entries = dev[4];
+  __threadfence_system();
+  h->seq = dev[0];
 }
 
 __global__ void born_kernel(int n, int n_chunks, const float* __restrict__ J, double S4, double S7, double C4,
@@ -133,13 +182,42 @@ __global__ void __launch_bounds__(kRedThreads) energy_reduce_kernel(const double
 
 }  // namespace
 
-gbx_status launch_stage_positions(Context* ctx, const float4* posq) {
+gbx_status launch_stage_positions(Context* ctx, const void* posq) {
   const int n = ctx->n;
-  stage_positions_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(posq, n, ctx->d_wpar, ctx->d_pos);
+  const int* slot_of = ctx->in_permuted ? ctx->d_slot_of : nullptr;
+  if (ctx->in_double)
+    stage_positions_kernel<true><<<(n + 255) / 256, 256, 0, ctx->stream>>>(posq, n, slot_of, ctx->d_wpar, ctx->d_pos);
+  else
+    stage_positions_kernel<false><<<(n + 255) / 256, 256, 0, ctx->stream>>>(posq, n, slot_of, ctx->d_wpar, ctx->d_pos);
   ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx->last_error = std::string("stage launch: ") + cudaGetErrorString(e);
+    return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
+gbx_status launch_finish_outputs(Context* ctx, unsigned long long* force, int stride, float* energy_float) {
+  const int n = ctx->n;
+  finish_outputs_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+      n, ctx->in_permuted ? ctx->d_slot_of : nullptr, ctx->d_force_fx, force, stride, ctx->d_energy, energy_float);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ctx->last_error = std::string("output launch: ") + cudaGetErrorString(e);
+    return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
+gbx_status launch_publish_status(Context* ctx) {
+  publish_status_kernel<<<1, 1, 0, ctx->stream>>>(ctx->d_status, ctx->use_tight ? ctx->d_tgeom : ctx->d_geom,
+                                                  ctx->d_pub, ctx->h_pub_dev);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ctx->last_error = std::string("status launch: ") + cudaGetErrorString(e);
     return GBX_ERR_CUDA;
   }
   return GBX_OK;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __r
   for (int k = 0; k < kScanItems; ++k) {
     if (base + k < ncell) {
       start[base + k] = ex;
-      cursor[base + k] = 0;
+      if (cursor) cursor[base + k] = 0;
     }
     if (base + k == ncell - 1) {
       start[ncell] = ex + v[k];

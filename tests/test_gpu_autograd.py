@@ -52,7 +52,7 @@ def test_against_oracle_adjoint(case):
     assert abs(E / ref["energy"] - 1) < 2e-5
     assert rel_rms(grads["forces"], ref["forces"]) < 1e-4
     assert rel_rms(grads["dEdq"], ref["dEdq"]) < 1e-4
-    assert rel_rms(grads["dEdR"], ref["dEdR"]) < 1e-3
+    assert rel_rms(grads["dEdR"], ref["dEdR"]) < 1e-4
     assert np.abs(grads["dEdalpha"] / ref["dEdalpha"] - 1).max() < 1e-4
 
 

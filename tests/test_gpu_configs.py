@@ -91,3 +91,22 @@ def test_gbmv_adjoint_vs_oracle(itype):
     assert errs["dEdR"] < G_TOL
     assert errs["dEdalpha"] < G_TOL
     ctx.close()
+
+
+@pytest.mark.parametrize("itype", [1, 2])
+def test_gbmv_bitwise_deterministic(itype):
+    """The cell passes hand out slots by atomics; sorting each cell's points
+    makes every sum's order a function of the input: repeated calls and a
+    fresh context give the same bits."""
+    g = make_globule(3000, seed=53)
+    box = box_for(g.positions, margin=1.0)
+    m = (GBModel.gbmv2 if itype == 2 else GBModel.gbmv1)(box=box, lebedev=50)
+    runs = []
+    for _ in range(2):
+        ctx = Context(m, g.n)
+        ctx.set_particle_parameters(g.charge, g.radius)
+        for _ in range(2):
+            runs.append(ctx.execute_host(g.positions))
+        ctx.close()
+    for E, F in runs[1:]:
+        assert E == runs[0][0] and np.array_equal(F, runs[0][1])
