@@ -1,0 +1,258 @@
+// OpenMM kernels for CharmmGBSWForce / CharmmGBMVForce on the gbx C ABI.
+#include "GB300CharmmKernels.h"
+
+#include <algorithm>
+#include <cctype>
+
+#include "openmm/OpenMMException.h"
+
+using OpenMM::CharmmGBMVForce;
+using OpenMM::CharmmGBSWForce;
+using OpenMM::OpenMMException;
+
+namespace GB300 {
+
+namespace {
+
+std::string squeeze(const std::string& s) {
+  std::string out;
+  for (char c : s)
+    if (!std::isspace(static_cast<unsigned char>(c))) out += c;
+  return out;
+}
+
+// The canonical CHARMM GB expressions: the Born radius of
+// CharmmReferenceGBSW.cpp:591-593 and the pair and self terms of
+// CharmmReferenceGBSW.cpp:237-283 with ONE_4PI_EPS0 = 138.935456.
+const char* kBorn = "1/(alpha0*(1/0.05-I4)+alpha1*(1/(4*0.05^4)-I7)^(1/4))";
+const char* kSelf = "-0.5*138.935456*(1-1/80)*q^2/B";
+const char* kPair = "-138.935456*(1-1/80)*q1*q2/sqrt(r^2+B1*B2*exp(-r^2/(4*B1*B2)))";
+
+}  // namespace
+
+GbxForceState::~GbxForceState() {
+  if (handle) gbx_destroy(handle);
+}
+
+void GbxForceState::check(gbx_status status, const char* what) const {
+  if (status == GBX_OK) return;
+  std::string detail;
+  if (handle) {
+    char buf[512];
+    if (gbx_last_error(handle, buf, sizeof(buf)) == GBX_OK) detail = buf;
+  }
+  throw OpenMMException(std::string("GB300 ") + what + ": " + gbx_status_string(status) +
+                        (detail.empty() ? "" : " (" + detail + ")"));
+}
+
+void GbxForceState::create(const gbx_config& cfg, int n) {
+  cu.setAsCurrent();
+  numAtoms = n;
+  globals[0] = cfg.alpha0;
+  globals[1] = cfg.alpha1;
+  for (int k = 0; k < 3; ++k) box[k] = cfg.box[k];
+  check(gbx_create(&cfg, n, &handle), "gbx_create");
+}
+
+void GbxForceState::setParameters(const std::vector<double>& charge, const std::vector<double>& radius) {
+  cu.setAsCurrent();
+  check(gbx_set_particle_parameters(handle, charge.data(), radius.data()), "gbx_set_particle_parameters");
+}
+
+void GbxForceState::setGlobals(double alpha0, double alpha1) {
+  if (alpha0 == globals[0] && alpha1 == globals[1]) return;  // a change drops the captured call
+  check(gbx_set_global_parameters(handle, alpha0, alpha1), "gbx_set_global_parameters");
+  globals[0] = alpha0;
+  globals[1] = alpha1;
+}
+
+void GbxForceState::setBox(double a, double b, double c) {
+  if (a == box[0] && b == box[1] && c == box[2]) return;
+  const double edges[3] = {a, b, c};
+  check(gbx_set_box(handle, edges), "gbx_set_box");
+  box[0] = a;
+  box[1] = b;
+  box[2] = c;
+}
+
+double GbxForceState::execute(bool includeForces, bool includeEnergy) {
+  cu.setAsCurrent();
+  // OpenMM moves atoms between slots for locality; the library keeps atom
+  // order internally and reads and writes the slots through this map
+  if (!orderSet || cu.getAtomsWereReordered()) {
+    check(gbx_set_atom_order(handle, cu.getAtomIndex().data()), "gbx_set_atom_order");
+    orderSet = true;
+  }
+  int flags = (includeForces ? GBX_EXEC_FORCES : 0) | (includeEnergy ? GBX_EXEC_ENERGY : 0);
+  if (cu.getUseDoublePrecision()) flags |= GBX_EXEC_POSQ_DOUBLE;   // double4 posq, double energy
+  else if (!cu.getUseMixedPrecision()) flags |= GBX_EXEC_ENERGY_FLOAT;  // float4 posq, float energy
+  if (!flags) return 0.0;
+  const void* posq = reinterpret_cast<const void*>(cu.getPosq().getDevicePointer());
+  unsigned long long* force = reinterpret_cast<unsigned long long*>(cu.getForce().getDevicePointer());
+  double* energy = reinterpret_cast<double*>(cu.getEnergyBuffer().getDevicePointer());
+  check(gbx_execute(handle, posq, force, cu.getPaddedNumAtoms(), energy, flags, cu.getCurrentStream()),
+        "gbx_execute");
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// CharmmGBSWForce
+// ---------------------------------------------------------------------------
+
+void GB300CalcCharmmGBSWForceKernel::initialize(const OpenMM::System& system, const CharmmGBSWForce& force) {
+  if (force.getNumParticles() != system.getNumParticles())
+    throw OpenMMException("CharmmGBSWForce must have exactly as many particles as the System it belongs to.");
+  gbx_config cfg;
+  state.check(gbx_config_preset(GBX_PRESET_CHARMM_GBSW, &cfg), "gbx_config_preset");
+  if (force.getNonbondedMethod() != CharmmGBSWForce::NoCutoff) cfg.cutoff = force.getCutoffDistance();
+  if (force.getNonbondedMethod() == CharmmGBSWForce::CutoffPeriodic) {
+    // rectangular boxes: minimum-image distances (CharmmReferenceGBSW.cpp:147-159)
+    OpenMM::Vec3 a, b, c;
+    system.getDefaultPeriodicBoxVectors(a, b, c);
+    cfg.periodic = 1;
+    cfg.box[0] = a[0];
+    cfg.box[1] = b[1];
+    cfg.box[2] = c[2];
+    periodic = true;
+  }
+  state.create(cfg, system.getNumParticles());
+  copyParameters(force);
+}
+
+void GB300CalcCharmmGBSWForceKernel::copyParameters(const CharmmGBSWForce& force) {
+  const int n = force.getNumParticles();
+  std::vector<double> q(n), r(n);
+  for (int i = 0; i < n; ++i) {
+    double s;
+    force.getParticleParameters(i, q[i], r[i], s);
+  }
+  state.setParameters(q, r);
+}
+
+double GB300CalcCharmmGBSWForceKernel::execute(OpenMM::ContextImpl&, bool includeForces, bool includeEnergy) {
+  if (periodic) {  // a barostat may have rescaled the box
+    const auto b = state.cu.getPeriodicBoxSize();  // double4: x, y, z edges
+    state.setBox(b.x, b.y, b.z);
+  }
+  return state.execute(includeForces, includeEnergy);
+}
+
+void GB300CalcCharmmGBSWForceKernel::copyParametersToContext(OpenMM::ContextImpl&, const CharmmGBSWForce& force) {
+  if (force.getNumParticles() != state.numAtoms)
+    throw OpenMMException("updateParametersInContext: The number of particles has changed");
+  copyParameters(force);
+}
+
+// ---------------------------------------------------------------------------
+// CharmmGBMVForce
+// ---------------------------------------------------------------------------
+
+void checkCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int& radiusIndex) {
+  if (force.getGBIntegralType() == CharmmGBMVForce::CustomIntegral)
+    throw OpenMMException("GB300: CustomIntegral has no implementation");
+  chargeIndex = radiusIndex = -1;
+  for (int k = 0; k < force.getNumPerParticleParameters(); ++k) {
+    if (force.getPerParticleParameterName(k) == "q") chargeIndex = k;
+    if (force.getPerParticleParameterName(k) == "radius") radiusIndex = k;
+  }
+  // GBSWIntegral.cpp:79-80
+  if (radiusIndex < 0) throw OpenMMException("GBSWIntegral: the per perticle parameter 'radius' must be defined");
+  bool ok = chargeIndex >= 0 && force.getNumGBIntegrals() == 2 && force.getNumComputedValues() == 1 &&
+            force.getNumEnergyTerms() == 2 && force.getNumExclusions() == 0 &&
+            force.getNumTabulatedFunctions() == 0;
+  const char* integralNames[2] = {"I4", "I7"};
+  const int orders[2] = {4, 7};
+  for (int k = 0; ok && k < 2; ++k) {
+    std::string name;
+    std::vector<int> pi;
+    std::vector<double> pr;
+    force.getGBIntegralParameters(k, name, pi, pr);
+    if (pi.empty()) throw OpenMMException("GBSWIntegral: the order of integral must be given");
+    if (pi[0] < 2) throw OpenMMException("GBSWIntegral: the order of integral must be greater or equal to 2");
+    ok = name == integralNames[k] && pi[0] == orders[k];
+  }
+  if (ok) {
+    std::string name, expr;
+    CharmmGBMVForce::ComputationType type;
+    force.getComputedValueParameters(0, name, expr, type);
+    ok = name == "B" && squeeze(expr) == squeeze(kBorn) && type == CharmmGBMVForce::SingleParticle;
+  }
+  if (ok) {
+    std::string expr;
+    CharmmGBMVForce::ComputationType type;
+    force.getEnergyTermParameters(0, expr, type);
+    ok = squeeze(expr) == squeeze(kSelf) && type == CharmmGBMVForce::SingleParticle;
+    force.getEnergyTermParameters(1, expr, type);
+    ok = ok && squeeze(expr) == squeeze(kPair) && type == CharmmGBMVForce::ParticlePairNoExclusions;
+  }
+  if (!ok)
+    throw OpenMMException("GB300: the device path evaluates the canonical CHARMM GB expressions only; "
+                          "this CharmmGBMVForce needs the plugin's generic kernels");
+}
+
+void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, const CharmmGBMVForce& force) {
+  if (force.getNumParticles() != system.getNumParticles())
+    throw OpenMMException("CharmmGBMVForce must have exactly as many particles as the System it belongs to.");
+  for (int i = 0; i < force.getNumParticles(); ++i) {
+    std::vector<double> p;
+    force.getParticleParameters(i, p);
+    if ((int)p.size() != force.getNumPerParticleParameters())
+      throw OpenMMException("CharmmGBMVForce: Wrong number of parameters for particle " + std::to_string(i));
+  }
+  checkCanonicalGBMVForce(force, chargeIndex, radiusIndex);
+  int preset = GBX_PRESET_GBSW_INTEGRAL;
+  if (force.getGBIntegralType() == CharmmGBMVForce::GBMVIntegralTypeI) preset = GBX_PRESET_GBMV1;
+  if (force.getGBIntegralType() == CharmmGBMVForce::GBMVIntegralTypeII) preset = GBX_PRESET_GBMV2;
+  gbx_config cfg;
+  state.check(gbx_config_preset(preset, &cfg), "gbx_config_preset");
+  // the integral classes always build their table in the context's box
+  // (GBMVIntegralTypeI.cpp:102-105, GBMVIntegralTypeII.cpp:107-110)
+  OpenMM::Vec3 a, b, c;
+  system.getDefaultPeriodicBoxVectors(a, b, c);
+  cfg.box[0] = a[0];
+  cfg.box[1] = b[1];
+  cfg.box[2] = c[2];
+  if (force.getNonbondedMethod() != CharmmGBMVForce::NoCutoff) cfg.cutoff = force.getCutoffDistance();
+  if (force.getNonbondedMethod() == CharmmGBMVForce::CutoffPeriodic) {
+    // minimum-image integrals (GBSWIntegral on the box-sampled table,
+    // GBSWIntegral.cpp:63-68,109) and pair terms (CharmmReferenceGBMV.cpp:294-297)
+    cfg.periodic = 1;
+    cfg.table_mode = GBX_TABLE_PERIODIC;
+  }
+  for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
+    const std::string& name = force.getGlobalParameterName(k);
+    if (name == "alpha0") cfg.alpha0 = force.getGlobalParameterDefaultValue(k);
+    if (name == "alpha1") cfg.alpha1 = force.getGlobalParameterDefaultValue(k);
+  }
+  alphaNames[0] = "alpha0";
+  alphaNames[1] = "alpha1";
+  state.create(cfg, system.getNumParticles());
+  copyParameters(force);
+}
+
+void GB300CalcCharmmGBMVForceKernel::copyParameters(const CharmmGBMVForce& force) {
+  const int n = force.getNumParticles();
+  std::vector<double> q(n), r(n), p;
+  for (int i = 0; i < n; ++i) {
+    force.getParticleParameters(i, p);
+    q[i] = p[chargeIndex];
+    r[i] = p[radiusIndex];
+  }
+  state.setParameters(q, r);
+}
+
+double GB300CalcCharmmGBMVForceKernel::execute(OpenMM::ContextImpl& context, bool includeForces,
+                                              bool includeEnergy) {
+  state.setGlobals(context.getParameter(alphaNames[0]), context.getParameter(alphaNames[1]));
+  const auto b = state.cu.getPeriodicBoxSize();  // double4: x, y, z edges
+  state.setBox(b.x, b.y, b.z);
+  return state.execute(includeForces, includeEnergy);
+}
+
+void GB300CalcCharmmGBMVForceKernel::copyParametersToContext(OpenMM::ContextImpl&, const CharmmGBMVForce& force) {
+  if (force.getNumParticles() != state.numAtoms)
+    throw OpenMMException("updateParametersInContext: The number of particles has changed");
+  copyParameters(force);
+}
+
+}  // namespace GB300

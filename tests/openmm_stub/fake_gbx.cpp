@@ -1,0 +1,87 @@
+// A recording stand-in for the gbx C ABI (test infrastructure): lets the
+// OpenMM plugin adapter run without a GPU.  Every call appends a line to a
+// log the test driver reads; gbx_execute returns a status the driver sets.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbx.h"
+
+std::vector<std::string> g_log;
+gbx_status g_execute_status = GBX_OK;
+gbx_config g_last_config;
+
+struct gbx_context {
+  int n;
+};
+
+namespace {
+void log(const std::string& s) { g_log.push_back(s); }
+}  // namespace
+
+extern "C" {
+const char* gbx_status_string(gbx_status s) { return s == GBX_ERR_STALE_RESULT ? "stale result" : "status"; }
+gbx_status gbx_last_error(const gbx_context*, char* buf, size_t len) {
+  std::snprintf(buf, len, "an earlier unchecked call lacked the volume terms");
+  return GBX_OK;
+}
+gbx_status gbx_config_preset(int preset, gbx_config* cfg) {
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->model = preset == GBX_PRESET_GBMV1 ? GBX_MODEL_GBMV1 : preset == GBX_PRESET_GBMV2 ? GBX_MODEL_GBMV2 : 0;
+  cfg->table_mode = preset == GBX_PRESET_CHARMM_GBSW ? GBX_TABLE_STANDALONE
+                    : preset == GBX_PRESET_GBSW_INTEGRAL ? GBX_TABLE_GRID : GBX_TABLE_PERIODIC;
+  cfg->alpha0 = -0.180;
+  cfg->alpha1 = 1.817;
+  log("preset " + std::to_string(preset));
+  return GBX_OK;
+}
+gbx_status gbx_create(const gbx_config* cfg, int n, gbx_context** out) {
+  g_last_config = *cfg;
+  *out = new gbx_context{n};
+  char b[256];
+  std::snprintf(b, sizeof(b), "create n=%d model=%d table=%d periodic=%d cutoff=%g box=%g,%g,%g alpha=%g,%g", n,
+                cfg->model, cfg->table_mode, cfg->periodic, cfg->cutoff, cfg->box[0], cfg->box[1], cfg->box[2],
+                cfg->alpha0, cfg->alpha1);
+  log(b);
+  return GBX_OK;
+}
+gbx_status gbx_destroy(gbx_context* c) {
+  delete c;
+  log("destroy");
+  return GBX_OK;
+}
+gbx_status gbx_set_particle_parameters(gbx_context* c, const double* q, const double* r) {
+  char b[128];
+  std::snprintf(b, sizeof(b), "params q0=%g r0=%g q%d=%g", q[0], r[0], c->n - 1, q[c->n - 1]);
+  log(b);
+  return GBX_OK;
+}
+gbx_status gbx_set_global_parameters(gbx_context*, double a0, double a1) {
+  char b[128];
+  std::snprintf(b, sizeof(b), "globals %g %g", a0, a1);
+  log(b);
+  return GBX_OK;
+}
+gbx_status gbx_set_box(gbx_context*, const double box[3]) {
+  char b[128];
+  std::snprintf(b, sizeof(b), "box %g %g %g", box[0], box[1], box[2]);
+  log(b);
+  return GBX_OK;
+}
+gbx_status gbx_set_atom_order(gbx_context* c, const int* idx) {
+  std::string s = "order";
+  for (int k = 0; k < c->n; ++k) s += " " + std::to_string(idx[k]);
+  log(s);
+  return GBX_OK;
+}
+gbx_status gbx_execute(gbx_context*, const void* posq, unsigned long long* force, int stride, double* energy,
+                       int flags, void* stream) {
+  char b[160];
+  std::snprintf(b, sizeof(b), "execute posq=%lx force=%lx stride=%d energy=%lx flags=%d stream=%lx",
+                (unsigned long)(size_t)posq, (unsigned long)(size_t)force, stride, (unsigned long)(size_t)energy,
+                flags, (unsigned long)(size_t)stream);
+  log(b);
+  return g_execute_status;
+}
+}
