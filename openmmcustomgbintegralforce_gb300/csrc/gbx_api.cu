@@ -179,6 +179,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_par, n));
   GBX_TRY(dalloc(ctx, &ctx->d_wpar, n));
   GBX_TRY(dalloc(ctx, &ctx->d_pos, n));
+  GBX_TRY(dalloc(ctx, &ctx->d_reduce, gbx::table_geom_scratch_doubles(n)));
   GBX_TRY(dalloc(ctx, &ctx->d_J, 2 * (size_t)ctx->n_chunks * n));
   GBX_TRY(dalloc(ctx, &ctx->d_born, n));
   GBX_TRY(dalloc(ctx, &ctx->d_bornf, 2 * (size_t)n));

@@ -301,6 +301,7 @@ gbx_status launch_stage_positions(Context* ctx, const void* posq);
 gbx_status launch_finish_outputs(Context* ctx, unsigned long long* force, int stride, float* energy_float);
 gbx_status launch_publish_status(Context* ctx);
 gbx_status launch_table_build(Context* ctx, const float4* pos);
+size_t table_geom_scratch_doubles(int n);
 gbx_status launch_tight_build(Context* ctx, const float4* pos);
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);

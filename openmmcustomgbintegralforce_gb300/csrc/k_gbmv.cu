@@ -17,7 +17,9 @@
 //   fill     point ids into their cell's slots
 //   integral warp per cell: sorts the cell's point ids (the slots were
 //            handed out by atomics, in no fixed order) so that every later
-//            sum over the cell's points has an order fixed by the input;
+//            sum over the cell's points has an order fixed by the input
+//            (cells of more than kSortMax points keep the atomic order and
+//            the chain rule reduces each of their contributions on its own);
 //            per point the list sums in list order, the solvent fraction by
 //            point id, and the point's sums by slot for the chain rule
 //   reduce   warp per (atom, chunk): J4, J7 over the solvent fractions in
@@ -47,7 +49,7 @@ constexpr int kBinThreads = 128;
 constexpr int kCellWarps = 4;           // warps (cells) per block in the cell passes
 constexpr int kCellThreads = kCellWarps * kWarp;
 constexpr int kMaxList = 64;            // longest list the cell passes stage (the GBMV table cap)
-constexpr int kSortMax = 32 * kWarp;    // cells of up to 1024 points are sorted in registers
+constexpr int kSortMax = 16 * kWarp;    // cells of up to 512 points are sorted in registers
 constexpr int kChainPts = 4;            // points per chain sub-step
 constexpr int kChainEnt = kWarp / kChainPts;  // entry lanes per point
 constexpr int kEntPerLane = kMaxList / kChainEnt;
@@ -218,18 +220,7 @@ __device__ __noinline__ void sort_cell(int* order, int P, int lane) {
   else if (P <= 2 * kWarp) sort_slots<2>(order, P, lane);
   else if (P <= 4 * kWarp) sort_slots<4>(order, P, lane);
   else if (P <= 8 * kWarp) sort_slots<8>(order, P, lane);
-  else if (P <= 16 * kWarp) sort_slots<16>(order, P, lane);
-  else if (P <= kSortMax) sort_slots<32>(order, P, lane);
-}
-
-// Warp per cell: the cell's point ids into ascending order.
-__global__ void __launch_bounds__(kCellThreads) gbmv_sort_kernel(const TableGeom* __restrict__ geom, long long cell_cap,
-                                                                 CellPoints cp) {
-  const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
-  const long long cell = (long long)blockIdx.x * kCellWarps + w;
-  if (cell >= geom->ncell || cell >= cell_cap) return;
-  const int P = cp.count[cell];
-  if (P > 1) sort_cell(cp.order + cp.start[cell], P, lane);
+  else if (P <= kSortMax) sort_slots<16>(order, P, lane);
 }
 
 template <int MODEL, bool PER>
@@ -254,7 +245,8 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
     if (MODEL == GBX_MODEL_GBMV2) s_k[w][l] = __ldg(&tab.par[cs.y + l].x);
   }
   const int start = cp.start[cell];
-  const int* order = cp.order + start;
+  int* order = cp.order + start;
+  if (P > 1) sort_cell(order, P, lane);
   __syncwarp();
   const float4* E = s_e[w];
   const float* K = s_k[w];
@@ -355,10 +347,16 @@ __device__ __forceinline__ void add_dEdR(const CellChainOut& o, int k, bool sort
 }
 
 // One point's chain-rule factors (the point's own lanes read them from
-// shared memory): its position in the cell frame, c ds/dS and, for GBMV-II,
-// the factors of d s1, d s2 and d |v|^2 and the vector sum v.
+// shared memory): its position in the cell frame and the factors of the
+// gradient with c ds/dS folded in.  GBMV-II: with u_j = F_j / T_j and
+// vd = v . d_j, the pull on entry j is
+//   g_j = [-400 u_j (A + C vd) + B F_j (F_j - 400 u_j r_j^2)] d_j + F_j Cv
+// with A = c ds/dS s0 s2 / |v|^2, B = 2 c ds/dS s0 s1 / |v|^2,
+// C = -2 c ds/dS s0 s1 s2 / |v|^4 (the d s1, d s2 and d |v|^2 factors) and
+// Cv = C v.  GBMV-I: g_j = A e_j r_j^2 d_j with A = 4 c ds/dS gamma_j
+// folded per entry.
 struct PointChain {
-  float px, py, pz, cS, t1, t2, t3, vx, vy, vz;
+  float px, py, pz, cS, A, B, C, vx, vy, vz, cvx, cvy, cvz;
   int i;
 };
 
@@ -368,8 +366,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
                                                                        const float2* __restrict__ dEdJ,
                                                                        CellChainOut out) {
   __shared__ float4 s_e[kCellWarps][kMaxList];
-  __shared__ float2 s_par[kCellWarps][kMaxList];  // GBMV-II (K, R); GBMV-I (R, -)
-  __shared__ int s_idx[kCellWarps][kMaxList];
+  __shared__ float4 s_par[kCellWarps][kMaxList];  // (GBMV-II K | GBMV-I R, R, atom index, -)
   __shared__ PointChain s_pt[kCellWarps][kWarp];
   __shared__ float3 s_own[kCellWarps][kWarp];
   const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
@@ -386,8 +383,8 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
   for (int l = lane; l < cnt; l += kWarp) {
     const float4 a = __ldg(tab.e + cs.y + l);
     s_e[w][l] = make_float4(a.x - c0.x, a.y - c0.y, a.z - c0.z, a.w);
-    s_par[w][l] = __ldg(tab.par + cs.y + l);
-    s_idx[w][l] = __ldg(tab.index + cs.y + l);
+    const float2 pk = __ldg(tab.par + cs.y + l);
+    s_par[w][l] = make_float4(pk.x, pk.y, __int_as_float(__ldg(tab.index + cs.y + l)), 0.0f);
   }
   const int start = cp.start[cell];
   const int* order = cp.order + start;
@@ -411,7 +408,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
       PointChain pc;
       pc.cS = 0.0f;
       pc.i = -1;
-      pc.px = pc.py = pc.pz = pc.t1 = pc.t2 = pc.t3 = pc.vx = pc.vy = pc.vz = 0.0f;
+      pc.px = pc.py = pc.pz = pc.A = pc.B = pc.C = pc.vx = pc.vy = pc.vz = pc.cvx = pc.cvy = pc.cvz = 0.0f;
       if (k < P) {
         const int p = order[k];
         const int i = p / m.nq, q = p - i * m.nq;
@@ -427,6 +424,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
         if (MODEL == GBX_MODEL_GBMV1) {
           logistic_solvent(m.beta, m.lambda, state[k], pl);
           pc.cS = cq * __fdividef(m.beta * pl, (1.0f + pl) * (1.0f + pl));
+          pc.A = 4.0f * pc.cS;
         } else {
           const float s1 = state[k], s2 = state[k + cp.plane], vx = state[k + 2 * cp.plane],
                       vy = state[k + 3 * cp.plane], vz = state[k + 4 * cp.plane];
@@ -434,12 +432,15 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
           logistic_solvent(m.beta, m.lambda, m.s0 * s1 * s2 / s3sq, pl);
           pc.cS = cq * __fdividef(m.beta * pl, (1.0f + pl) * (1.0f + pl)) * m.s0;
           const float inv3 = 1.0f / s3sq;
-          pc.t1 = s2 * inv3;
-          pc.t2 = s1 * inv3;
-          pc.t3 = -s1 * s2 * inv3 * inv3;
+          pc.A = pc.cS * (s2 * inv3);
+          pc.B = 2.0f * pc.cS * (s1 * inv3);
+          pc.C = 2.0f * pc.cS * (-s1 * s2 * inv3 * inv3);
           pc.vx = vx;
           pc.vy = vy;
           pc.vz = vz;
+          pc.cvx = pc.C * vx;
+          pc.cvy = pc.C * vy;
+          pc.cvz = pc.C * vz;
         }
       }
       pts[lane] = pc;
@@ -457,8 +458,8 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
           const int l = es + e * kChainEnt;
           if (l < cnt) {
             const float4 a = s_e[w][l];
-            const float2 pk = s_par[w][l];
-            const int kj = s_idx[w][l];
+            const float4 pk = s_par[w][l];
+            const int kj = __float_as_int(pk.z);
             const float3 d = img.apply(make_float3(a.x - pc.px, a.y - pc.py, a.z - pc.pz));
             const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
             float gx, gy, gz;
@@ -466,27 +467,28 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
               const float r4 = r2 * r2;
               const float ex = __expf(a.w * r4);
               if (ADJ) add_dEdR(out, kj, sorted, accR[e], pc.cS * ex * r4 * (-4.0f * a.w / pk.x));
-              const float gs = pc.cS * 4.0f * a.w * ex * r2;  // dS/d(delta) = 4 gamma e r^2 delta
+              const float gs = pc.A * a.w * ex * r2;  // dS/d(delta) = 4 gamma e r^2 delta
               gx = gs * d.x;
               gy = gs * d.y;
               gz = gs * d.z;
             } else {
               const float T = fmaf(100.0f, r2, pk.x);
-              const float CT = __fdividef(a.w, T);
+              const float rT = __fdividef(1.0f, T);
+              const float CT = a.w * rT;
               const float F = CT * CT;
-              const float dFf = -400.0f * F * __fdividef(1.0f, T);  // dF/d(delta) = dFf delta
-              const float vd = pc.vx * d.x + pc.vy * d.y + pc.vz * d.z;
+              const float u = F * rT;  // dF/d(delta) = -400 u delta
+              const float vd = fmaf(pc.vx, d.x, fmaf(pc.vy, d.y, pc.vz * d.z));
               if (ADJ) {
                 const float R = pk.y;
                 const float Cp = 10.0f * m.p1, Tp = Cp - 200.0f * R;
                 const float dFdR = 2.0f * CT * __fdividef(Cp * T - a.w * Tp, T * T);
-                add_dEdR(out, kj, sorted, accR[e],
-                         pc.cS * (pc.t1 * dFdR + pc.t2 * (r2 * 2.0f * F * dFdR) + pc.t3 * (2.0f * vd * dFdR)));
+                // c ds/dS (s2 dF + s1 d(r^2 F^2) + d|v|^2) / |v|^2 terms, as pc.A, pc.B, pc.C carry them
+                add_dEdR(out, kj, sorted, accR[e], dFdR * (pc.A + pc.B * (r2 * F) + pc.C * vd));
               }
-              const float sc = pc.t1 * dFf + pc.t2 * 2.0f * F * fmaf(dFf, r2, F) + pc.t3 * 2.0f * vd * dFf;
-              gx = pc.cS * fmaf(sc, d.x, pc.t3 * 2.0f * F * pc.vx);
-              gy = pc.cS * fmaf(sc, d.y, pc.t3 * 2.0f * F * pc.vy);
-              gz = pc.cS * fmaf(sc, d.z, pc.t3 * 2.0f * F * pc.vz);
+              const float sc = -400.0f * u * fmaf(pc.C, vd, pc.A) + pc.B * F * fmaf(-400.0f * u, r2, F);
+              gx = fmaf(sc, d.x, F * pc.cvx);
+              gy = fmaf(sc, d.y, F * pc.cvy);
+              gz = fmaf(sc, d.z, F * pc.cvz);
             }
             if (kj != pc.i) {  // atom i's own entry moves with the point: no force
               if (sorted) {
@@ -551,7 +553,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
     }
     const int l = es + e * kChainEnt;
     if (ps == 0 && l < cnt) {
-      const int kj = s_idx[w][l];
+      const int kj = __float_as_int(s_par[w][l].z);
       if (sorted) add_fixed3(out, kj, -acc[e][0], -acc[e][1], -acc[e][2]);
       if (ADJ && sorted) {
         const long long r = float_to_fixed(accR[e]);
@@ -603,7 +605,6 @@ gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const Mod
   launch_scan<false>(ctx->d_pcount, ctx->d_pgeom, ctx->d_pblock_sums, ctx->d_pstart, nullptr, cells, 0x7fffffffffffLL,
                      ctx->d_status, st);
   gbmv_fill_kernel<<<(int)((npts + 255) / 256), 256, 0, st>>>(npts, cp);
-  gbmv_sort_kernel<<<cell_blocks, kCellThreads, 0, st>>>(ctx->d_geom, cells, cp);
   if (m.model == GBX_MODEL_GBMV1) {
     if (per) gbmv_cell_integral_kernel<GBX_MODEL_GBMV1, true><<<cell_blocks, kCellThreads, 0, st>>>(pos, t, qd, m, cp);
     else gbmv_cell_integral_kernel<GBX_MODEL_GBMV1, false><<<cell_blocks, kCellThreads, 0, st>>>(pos, t, qd, m, cp);
@@ -613,7 +614,7 @@ gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const Mod
   }
   gbmv_reduce_kernel<<<bin_blocks, kBinThreads, 0, st>>>(ctx->n, qd, m.nq, chunk, ctx->n_chunks, ctx->d_sval,
                                                          ctx->d_J);
-  ctx->launches += 9;  // bin, ncell copy, three scan phases, fill, sort, integral, reduce
+  ctx->launches += 8;  // bin, ncell copy, three scan phases, fill, integral, reduce
   return GBX_OK;
 }
 

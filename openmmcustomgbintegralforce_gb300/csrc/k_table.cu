@@ -35,72 +35,110 @@ __device__ __forceinline__ double half_sqrt3() { return ddiv(__dsqrt_rn(3.0), 2.
 // --------------------------------------------------------------------------
 // Geometry: CharmmReferenceGBSW.cpp:444-466, CustomGBIntegral.cpp:53-113,163-193
 // --------------------------------------------------------------------------
-__global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const float4* __restrict__ pos,
-                                                                  const double* __restrict__ radius, int n,
-                                                                  int mode, double h, double buffer, double sw,
-                                                                  double bx, double by, double bz,
+// Per-block partial extents and sums over a fixed range of atoms (FP64 on
+// every SM instead of one: the GPU's FP64 rate per SM is low), reduced by
+// a fixed-shape tree, so the centre of geometry is the same bits every call.
+constexpr int kPartThreads = 256;
+
+struct GeomPart {
+  double mn[3], mx[3], sum[3], rmax;
+};
+
+__global__ void __launch_bounds__(kPartThreads) table_geom_partial_kernel(const float4* __restrict__ pos,
+                                                                          const double* __restrict__ radius, int n,
+                                                                          GeomPart* __restrict__ parts) {
+  __shared__ double s[10][kPartThreads];
+  const int t = threadIdx.x, a = blockIdx.x * kPartThreads + t;
+  double v[10];
+  if (a < n) {
+    const float4 p = pos[a];
+    const double c[3] = {(double)p.x, (double)p.y, (double)p.z};
+    for (int k = 0; k < 3; ++k) {
+      v[k] = c[k];
+      v[3 + k] = c[k];
+      v[6 + k] = c[k];
+    }
+    v[9] = radius[a];
+  } else {
+    const float4 p = pos[blockIdx.x * kPartThreads];  // an atom of this block: neutral for min / max
+    for (int k = 0; k < 3; ++k) {
+      v[k] = v[3 + k] = (&p.x)[k];
+      v[6 + k] = 0.0;
+    }
+    v[9] = 0.0;
+  }
+  for (int k = 0; k < 10; ++k) s[k][t] = v[k];
+  __syncthreads();
+  for (int stride = kPartThreads / 2; stride > 0; stride >>= 1) {
+    if (t < stride) {
+      for (int k = 0; k < 3; ++k) {
+        s[k][t] = fmin(s[k][t], s[k][t + stride]);
+        s[3 + k][t] = fmax(s[3 + k][t], s[3 + k][t + stride]);
+        s[6 + k][t] = dadd(s[6 + k][t], s[6 + k][t + stride]);
+      }
+      s[9][t] = fmax(s[9][t], s[9][t + stride]);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    GeomPart g;
+    for (int k = 0; k < 3; ++k) {
+      g.mn[k] = s[k][0];
+      g.mx[k] = s[3 + k][0];
+      g.sum[k] = s[6 + k][0];
+    }
+    g.rmax = s[9][0];
+    parts[blockIdx.x] = g;
+  }
+}
+
+// CharmmReferenceGBSW.cpp:444-466, CustomGBIntegral.cpp:53-113,163-193: the
+// grid from the partial extents (combined in block order).
+__global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const GeomPart* __restrict__ parts, int nparts,
+                                                                  int n, int mode, double h, double buffer,
+                                                                  double sw, double bx, double by, double bz,
                                                                   TableGeom* __restrict__ g, long long cell_cap,
                                                                   unsigned* __restrict__ status) {
-  __shared__ double s_min[3][kGeomThreads / kWarp];
-  __shared__ double s_max[3][kGeomThreads / kWarp];
-  __shared__ double s_sum[3][kGeomThreads];
-  __shared__ double s_r[kGeomThreads / kWarp];
+  __shared__ double s[10][kGeomThreads];
   const int t = threadIdx.x;
-  double mn[3], mx[3], sm[3] = {0, 0, 0};
-  double rmax = 0.0;
-  if (n > 0) {
-    float4 p0 = pos[0];
-    mn[0] = mx[0] = p0.x;
-    mn[1] = mx[1] = p0.y;
-    mn[2] = mx[2] = p0.z;
+  double v[10];
+  const GeomPart p0 = parts[0];
+  for (int k = 0; k < 3; ++k) {
+    v[k] = p0.mn[k];
+    v[3 + k] = p0.mx[k];
+    v[6 + k] = 0.0;
   }
-  for (int a = t; a < n; a += blockDim.x) {
-    float4 p = pos[a];
-    double c[3] = {(double)p.x, (double)p.y, (double)p.z};
+  v[9] = 0.0;
+  for (int b = t; b < nparts; b += kGeomThreads) {  // each thread's parts in block order
+    const GeomPart p = parts[b];
     for (int k = 0; k < 3; ++k) {
-      mn[k] = fmin(mn[k], c[k]);
-      mx[k] = fmax(mx[k], c[k]);
-      sm[k] = dadd(sm[k], c[k]);
+      v[k] = fmin(v[k], p.mn[k]);
+      v[3 + k] = fmax(v[3 + k], p.mx[k]);
+      v[6 + k] = dadd(v[6 + k], p.sum[k]);
     }
-    rmax = fmax(rmax, radius[a]);
+    v[9] = fmax(v[9], p.rmax);
   }
-  // warp min/max (exact in any order)
-  for (int off = 16; off > 0; off >>= 1) {
-    for (int k = 0; k < 3; ++k) {
-      mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
-      mx[k] = fmax(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
-    }
-    rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
-  }
-  const int w = t / kWarp, l = t % kWarp;
-  if (l == 0) {
-    for (int k = 0; k < 3; ++k) {
-      s_min[k][w] = mn[k];
-      s_max[k][w] = mx[k];
-    }
-    s_r[w] = rmax;
-  }
-  for (int k = 0; k < 3; ++k) s_sum[k][t] = sm[k];
+  for (int k = 0; k < 10; ++k) s[k][t] = v[k];
   __syncthreads();
-  // fixed-shape tree for the centre-of-geometry sum (deterministic)
   for (int stride = kGeomThreads / 2; stride > 0; stride >>= 1) {
-    if (t < stride)
-      for (int k = 0; k < 3; ++k) s_sum[k][t] = dadd(s_sum[k][t], s_sum[k][t + stride]);
+    if (t < stride) {
+      for (int k = 0; k < 3; ++k) {
+        s[k][t] = fmin(s[k][t], s[k][t + stride]);
+        s[3 + k][t] = fmax(s[3 + k][t], s[3 + k][t + stride]);
+        s[6 + k][t] = dadd(s[6 + k][t], s[6 + k][t + stride]);
+      }
+      s[9][t] = fmax(s[9][t], s[9][t + stride]);
+    }
     __syncthreads();
   }
   if (t != 0) return;
-  for (int ww = 1; ww < kGeomThreads / kWarp; ++ww) {
-    for (int k = 0; k < 3; ++k) {
-      mn[k] = fmin(mn[k], s_min[k][ww]);
-      mx[k] = fmax(mx[k], s_max[k][ww]);
-    }
-    rmax = fmax(rmax, s_r[ww]);
-  }
+  double mn[3], mx[3], sm[3];
   for (int k = 0; k < 3; ++k) {
-    mn[k] = fmin(mn[k], s_min[k][0]);
-    mx[k] = fmax(mx[k], s_max[k][0]);
+    mn[k] = s[k][0];
+    mx[k] = s[3 + k][0];
+    sm[k] = s[6 + k][0];
   }
-  rmax = fmax(rmax, s_r[0]);
+  const double rmax = s[9][0];
   TableGeom G;
   G.mode = mode;
   G.total = 0;
@@ -131,7 +169,7 @@ __global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const float4* 
   } else {
     double box[3] = {bx, by, bz};
     double cog[3];
-    for (int k = 0; k < 3; ++k) cog[k] = ddiv(s_sum[k][0], (double)n);
+    for (int k = 0; k < 3; ++k) cog[k] = ddiv(sm[k], (double)n);
     double L = 0.0;
     for (int k = 0; k < 3; ++k) {
       double d = box[k];
@@ -370,6 +408,15 @@ __global__ void denormalize_kernel(const int* __restrict__ entries, const TableG
   }
 }
 
+}  // namespace
+
+// Scratch the geometry pass needs: one GeomPart per 256 atoms, in doubles.
+size_t table_geom_scratch_doubles(int n) {
+  return ((size_t)(n + kPartThreads - 1) / kPartThreads) * (sizeof(GeomPart) / sizeof(double));
+}
+
+namespace {
+
 int grid_for(long long work, int per_block) {
   long long b = (work + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -382,10 +429,13 @@ int grid_for(long long work, int per_block) {
 gbx_status launch_table_build(Context* ctx, const float4* pos) {
   const gbx_config& c = ctx->cfg;
   cudaStream_t st = ctx->stream;
-  table_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->d_radius, ctx->n, c.table_mode, c.grid_length,
-                                                c.table_buffer, c.switch_width, c.box[0], c.box[1], c.box[2],
-                                                ctx->d_geom, ctx->cell_cap, ctx->d_status);
-  ++ctx->launches;
+  const int nparts = (ctx->n + kPartThreads - 1) / kPartThreads;
+  GeomPart* parts = reinterpret_cast<GeomPart*>(ctx->d_reduce);
+  table_geom_partial_kernel<<<nparts, kPartThreads, 0, st>>>(pos, ctx->d_radius, ctx->n, parts);
+  table_geom_kernel<<<1, kGeomThreads, 0, st>>>(parts, nparts, ctx->n, c.table_mode, c.grid_length, c.table_buffer,
+                                                c.switch_width, c.box[0], c.box[1], c.box[2], ctx->d_geom,
+                                                ctx->cell_cap, ctx->d_status);
+  ctx->launches += 2;
   const long long cells = ctx->cell_cap;
   if (cells == 0) {
     // sizing call: geometry only; the caller reads it back and allocates

@@ -63,6 +63,7 @@ __device__ long long query_exact(const TableGeom& g, const float4 xi, const doub
 struct RefQuery {
   float rel[3];  // (x_i - min) / step, cell units
   float inv[3];
+  float invdims[3];  // periodic table: 1 / dims, the box in cell units being dims
   float eps;     // guard band in cell units
   bool off;      // the geometry has more cells than are allocated: no cell
   const TableGeom* g;
@@ -76,23 +77,34 @@ struct RefQuery {
     for (int k = 0; k < 3; ++k) {
       rel[k] = (float)((x[k] - geom.min[k]) / geom.step[k]);
       inv[k] = (float)(1.0 / geom.step[k]);
+      invdims[k] = 1.0f / (float)geom.dims[k];
     }
     eps = 1e-4f + 64.0f * (float)dmax * 5.96e-8f;
   }
   __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
     if (off) return -1;
     const TableGeom& G = *g;
-    const float t[3] = {fmaf(v.x, inv[0], rel[0]), fmaf(v.y, inv[1], rel[1]), fmaf(v.z, inv[2], rel[2])};
+    float t[3] = {fmaf(v.x, inv[0], rel[0]), fmaf(v.y, inv[1], rel[1]), fmaf(v.z, inv[2], rel[2])};
     int id[3];
     bool safe = true;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      if (G.mode == GBX_TABLE_PERIODIC) {
+        // the box-sampled grid spans the box (step = box / dims): moving the
+        // point by whole boxes (CustomGBIntegral.cpp:284-309) is a shift by
+        // whole multiples of dims in cell units; a point within the guard
+        // band of a box edge takes the exact path
+        const float W = (float)G.dims[k];
+        const float nb = floorf(t[k] * invdims[k]);
+        t[k] = fmaf(-nb, W, t[k]);
+        if (t[k] < eps || t[k] > W - eps) safe = false;
+      }
       const float f = floorf(t[k]);
       const float fr = t[k] - f;
       id[k] = (int)f;
       if (fr < eps || fr > 1.0f - eps) safe = false;
       if (G.mode == GBX_TABLE_PERIODIC) {
-        if (id[k] < 0 || id[k] >= G.dims[k]) safe = false;  // wrapping: exact path
+        if (id[k] < 0 || id[k] >= G.dims[k]) safe = false;
       } else {
         if (t[k] < -eps || t[k] > (float)(G.dims[k] - 1) + eps) return -1;
         if (t[k] < eps || t[k] > (float)(G.dims[k] - 1) - eps) safe = false;
