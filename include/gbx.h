@@ -104,7 +104,9 @@ typedef struct {
                            rectangular box[3] (edges >= 2 cutoff), the table query wrapped once per
                            axis (CharmmReferenceGBSW.cpp:242-243,287-288,522-535,620-621,647-648) */
   double tight_grid_length; /* cell edge of the exact GBSW table (nm); <= 0: 0.1 */
-  int reserved[4];
+  int integral_orders[2];   /* orders n of the two GB integrals (weights w / r^(n-2),
+                               GBSWIntegral.cpp:96,144); 0: 4 and 7 */
+  int reserved[2];
 } gbx_config;
 
 /* Which table the integrals read.  The reference's standalone GBSW table
@@ -136,6 +138,47 @@ GBX_API gbx_status gbx_last_error(const gbx_context* ctx, char* buf, size_t len)
 /* Per-particle charge (e) and input radius (nm).  Replaces
  * copyParametersToContext (charmmKernels.h:88,128; CharmmReferenceKernels.cpp:439-458). */
 GBX_API gbx_status gbx_set_particle_parameters(gbx_context* ctx, const double* charge, const double* radius);
+/* ------------------------------------------------------------------------
+ * A CharmmGBMVForce with expressions outside the canonical CHARMM set
+ * (CharmmGBMVForce.h:294-391: computed values and energy terms).  Replaces
+ * the reference's runtime-generated kernels (CharmmCudaKernels.cpp:228-827;
+ * CharmmReferenceGBMV.cpp:151-444 on the CPU): the expressions and their
+ * derivatives are compiled for the device when the context is created (NVRTC,
+ * loaded at run time).  Variables: per-particle parameters, globals, the GB
+ * integrals and earlier computed values by name; pair terms read r and every
+ * per-particle quantity with the suffix 1 or 2 (atom 1 is the lower index).
+ * One or two integrals; computed values are SingleParticle; pair terms run
+ * over every pair (no exclusions).  Per-particle parameters must include
+ * "radius" (GBSWIntegral.cpp:79-80).  gbx_adjoint is not available here.
+ * ------------------------------------------------------------------------ */
+enum { GBX_TERM_SINGLE = 0, GBX_TERM_PAIR = 1 };
+typedef struct {
+  int num_params;
+  const char* const* param_names;
+  int num_globals;
+  const char* const* global_names;
+  const double* global_values;
+  int num_integrals;
+  const char* const* integral_names;
+  const int* integral_orders;
+  int num_values;
+  const char* const* value_names;
+  const char* const* value_expressions;
+  int num_terms;
+  const char* const* term_expressions;
+  const int* term_types; /* GBX_TERM_* */
+} gbx_custom;
+
+GBX_API gbx_status gbx_create_custom(const gbx_config* cfg, int num_atoms, const gbx_custom* custom,
+                                     gbx_context** out);
+/* Per-particle parameters [num_atoms][num_params] (the radius among them). */
+GBX_API gbx_status gbx_set_custom_parameters(gbx_context* ctx, const double* params);
+GBX_API gbx_status gbx_set_custom_global(gbx_context* ctx, const char* name, double value);
+/* Checks an expression set without a device: parses it, checks every
+ * variable and compiles the generated code.  On failure `log` (may be NULL)
+ * receives the reason. */
+GBX_API gbx_status gbx_custom_check(const gbx_custom* custom, char* log, size_t len);
+
 /* Global parameters alpha0, alpha1 (the GBMV force's computed-value globals). */
 GBX_API gbx_status gbx_set_global_parameters(gbx_context* ctx, double alpha0, double alpha1);
 /* Periodic box edges (nm) for GBX_TABLE_PERIODIC. */

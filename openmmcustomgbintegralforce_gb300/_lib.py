@@ -31,6 +31,7 @@ EXPORTED = (
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
     "gbx_adjoint_host", "gbx_adjoint", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
+    "gbx_create_custom", "gbx_set_custom_parameters", "gbx_set_custom_global", "gbx_custom_check",
     "gbx_batch_create", "gbx_batch_destroy", "gbx_batch_molecule", "gbx_batch_buffers", "gbx_batch_execute",
     "gbx_batch_execute_host", "gbx_batch_tune", "gbx_batch_last_error",
 )
@@ -72,7 +73,8 @@ class GbxConfig(ctypes.Structure):
         ("table_policy", ctypes.c_int),
         ("periodic", ctypes.c_int),
         ("tight_grid_length", ctypes.c_double),
-        ("reserved", ctypes.c_int * 4),
+        ("integral_orders", ctypes.c_int * 2),
+        ("reserved", ctypes.c_int * 2),
     ]
 
     @staticmethod
@@ -99,6 +101,8 @@ class GbxConfig(ctypes.Structure):
         c.table_policy = 1 if m.reference_table else 0
         c.tight_grid_length = m.tight_h
         c.periodic = 1 if m.periodic else 0
+        c.integral_orders[0] = int(m.orders[0])
+        c.integral_orders[1] = int(m.orders[1] if len(m.orders) > 1 else m.orders[0])
         return c
 
 
@@ -128,6 +132,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_set_global_parameters.argtypes = [vp, cd, cd]
     L.gbx_set_box.argtypes = [vp, vp]
     L.gbx_set_atom_order.argtypes = [vp, vp]
+    L.gbx_create_custom.argtypes = [vp, ci, vp, vp]
+    L.gbx_set_custom_parameters.argtypes = [vp, vp]
+    L.gbx_set_custom_global.argtypes = [vp, ctypes.c_char_p, cd]
+    L.gbx_custom_check.argtypes = [vp, ctypes.c_char_p, sz]
     L.gbx_execute.argtypes = [vp, vp, vp, ci, vp, ci, vp]
     L.gbx_execute_host.argtypes = [vp, vp, vp, vp, ci]
     L.gbx_get_born_radii.argtypes = [vp, vp]
@@ -329,6 +337,98 @@ class Context:
         self._check(self.lib.gbx_get_lookup_table(self.h, _p(dims), _p(mn), _p(step), ctypes.byref(ncell),
                                                   _p(counts), ctypes.byref(total), _p(atoms)))
         return {"dims": dims, "min": mn, "step": step, "counts": counts, "atoms": atoms[: total.value]}
+
+
+class GbxCustom(ctypes.Structure):
+    _fields_ = [
+        ("num_params", ctypes.c_int), ("param_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("num_globals", ctypes.c_int), ("global_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("global_values", ctypes.POINTER(ctypes.c_double)),
+        ("num_integrals", ctypes.c_int), ("integral_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("integral_orders", ctypes.POINTER(ctypes.c_int)),
+        ("num_values", ctypes.c_int), ("value_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("value_expressions", ctypes.POINTER(ctypes.c_char_p)),
+        ("num_terms", ctypes.c_int), ("term_expressions", ctypes.POINTER(ctypes.c_char_p)),
+        ("term_types", ctypes.POINTER(ctypes.c_int)),
+    ]
+
+
+TERM_SINGLE, TERM_PAIR = 0, 1
+
+
+def custom_struct(custom: dict):
+    """A GbxCustom for ``custom`` (see CustomContext) and the buffers it points into."""
+    keep = []
+
+    def strs(xs):
+        arr = (ctypes.c_char_p * max(1, len(xs)))(*[x.encode() for x in xs])
+        keep.append(arr)
+        return arr
+
+    gl = list(custom.get("globals", {}).items())
+    integ = list(custom["integrals"])
+    vals = list(custom.get("values", []))
+    terms = list(custom["terms"])
+    c = GbxCustom()
+    c.num_params = len(custom["params"])
+    c.param_names = strs(custom["params"])
+    c.num_globals = len(gl)
+    c.global_names = strs([k for k, _ in gl])
+    gv = (ctypes.c_double * max(1, len(gl)))(*[float(v) for _, v in gl])
+    c.global_values = gv
+    c.num_integrals = len(integ)
+    c.integral_names = strs([k for k, _ in integ])
+    io = (ctypes.c_int * max(1, len(integ)))(*[int(o) for _, o in integ])
+    c.integral_orders = io
+    c.num_values = len(vals)
+    c.value_names = strs([k for k, _ in vals])
+    c.value_expressions = strs([e for _, e in vals])
+    c.num_terms = len(terms)
+    c.term_expressions = strs([e for e, _ in terms])
+    tt = (ctypes.c_int * max(1, len(terms)))(*[int(t) for _, t in terms])
+    c.term_types = tt
+    keep += [gv, io, tt]
+    return c, keep
+
+
+def check_custom(custom: dict):
+    """Parses and compiles an expression set without a device (gbx_custom_check):
+    (status, message)."""
+    lib = load()
+    c, _keep = custom_struct(custom)
+    buf = ctypes.create_string_buffer(4096)
+    st = lib.gbx_custom_check(ctypes.byref(c), buf, 4096)
+    return st, buf.value.decode(errors="replace")
+
+
+class CustomContext(Context):
+    """A context for CharmmGBMVForce expressions outside the canonical set
+    (gbx_create_custom): ``custom`` is a dict with ``params`` (names, one of
+    them "radius"), ``globals`` ({name: value}), ``integrals`` ([(name,
+    order)]), ``values`` ([(name, expression)]) and ``terms`` ([(expression,
+    TERM_SINGLE | TERM_PAIR)]).  The integral class, quadrature and table
+    come from ``model``."""
+
+    def __init__(self, model: GBModel, num_atoms: int, custom: dict):
+        self.lib = load()
+        self.model = model
+        self.n = int(num_atoms)
+        self.custom = custom
+        self.cfg = GbxConfig.from_model(model)
+        c, keep = custom_struct(custom)
+        h = ctypes.c_void_p()
+        self._check(self.lib.gbx_create_custom(ctypes.byref(self.cfg), self.n, ctypes.byref(c), ctypes.byref(h)),
+                    ctx=False)
+        self.h = h
+
+    def set_custom_parameters(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        if p.shape != (self.n, len(self.custom["params"])):
+            raise GBXError(1, "params must be [n, num_params]")
+        self._check(self.lib.gbx_set_custom_parameters(self.h, _p(p)))
+
+    def set_custom_global(self, name: str, value: float):
+        self._check(self.lib.gbx_set_custom_global(self.h, name.encode(), float(value)))
 
 
 class Batch:

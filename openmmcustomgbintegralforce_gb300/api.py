@@ -23,7 +23,7 @@ import re
 
 import numpy as np
 
-from ._lib import Context, GBXError
+from ._lib import Context, CustomContext, GBXError
 from .spec import TABLE_PERIODIC, GBModel
 
 # CharmmGBMVForce.h:87-104
@@ -359,6 +359,40 @@ def _check_canonical(force: CharmmGBMVForce):
     return names.index("q"), names.index("radius")
 
 
+def custom_spec(force: CharmmGBMVForce) -> dict:
+    """The force's expressions as a gbx_create_custom description (computed
+    values SingleParticle; energy terms SingleParticle or pair without
+    exclusions)."""
+    if force.getNumExclusions() or force.getNumTabulatedFunctions():
+        raise GBXError(4, "exclusions and tabulated functions are not supported by the compiled expressions")
+    if force.getGBIntegralType() == CustomIntegral:
+        raise GBXError(4, "CustomIntegral has no implementation")
+    names = [force.getPerParticleParameterName(i) for i in range(force.getNumPerParticleParameters())]
+    if "radius" not in names:
+        raise OpenMMException("GBSWIntegral: the per perticle parameter 'radius' must be defined")
+    integrals = []
+    for k in range(force.getNumGBIntegrals()):
+        name, pi, _ = force.getGBIntegralParameters(k)
+        if len(pi) == 0:
+            raise OpenMMException("GBSWIntegral: the order of integral must be given")
+        if pi[0] < 2:
+            raise OpenMMException("GBSWIntegral: the order of integral must be greater or equal to 2")
+        integrals.append((name, pi[0]))
+    values = []
+    for k in range(force.getNumComputedValues()):
+        name, expr, t = force.getComputedValueParameters(k)
+        if t != SingleParticle:
+            raise GBXError(4, "computed values must be SingleParticle")
+        values.append((name, expr))
+    terms = []
+    for k in range(force.getNumEnergyTerms()):
+        expr, t = force.getEnergyTermParameters(k)
+        terms.append((expr, 0 if t == SingleParticle else 1))
+    globals_ = {force.getGlobalParameterName(k): force.getGlobalParameterDefaultValue(k)
+                for k in range(force.getNumGlobalParameters())}
+    return {"params": names, "globals": globals_, "integrals": integrals, "values": values, "terms": terms}
+
+
 class CalcCharmmGBSWForceKernel:
     """Kernel for CharmmGBSWForce (charmmKernels.h:94-129) on the gbx C ABI.
 
@@ -424,7 +458,14 @@ class CalcCharmmGBMVForceKernel:
         for i in range(force.getNumParticles()):
             if len(force.getParticleParameters(i)) != force.getNumPerParticleParameters():
                 raise OpenMMException(f"CharmmGBMVForce: Wrong number of parameters for particle {i}")
-        self._iq, self._ir = _check_canonical(force)
+        try:
+            self._iq, self._ir = _check_canonical(force)
+            self.custom = None
+        except GBXError as e:
+            if e.status != 4:
+                raise
+            # outside the canonical set: the expressions are compiled for the device
+            self.custom = custom_spec(force)
         t = force.getGBIntegralType()
         box = tuple(self.box) if self.box is not None else (10.0, 10.0, 10.0)
         base = {GBSWIntegral: GBModel.gbsw_integral(), GBMVIntegralTypeI: GBModel.gbmv1(box=box),
@@ -444,18 +485,29 @@ class CalcCharmmGBMVForceKernel:
                     for k in range(force.getNumGlobalParameters())}
         m = m.replace(alpha0=globals_.get("alpha0", m.alpha0), alpha1=globals_.get("alpha1", m.alpha1),
                       pref=-ONE_4PI_EPS0 * (1 - 1 / 80))
+        if self.custom is not None:
+            m = m.replace(orders=tuple(o for _, o in self.custom["integrals"]))
         self.model = m
-        self.ctx = Context(m, numParticles)
+        self.ctx = Context(m, numParticles) if self.custom is None else CustomContext(m, numParticles, self.custom)
         self.copyParametersToContext(force)
 
     def copyParametersToContext(self, force: CharmmGBMVForce):
         if force.getNumParticles() != self.ctx.n:
             raise OpenMMException("updateParametersInContext: The number of particles has changed")
         p = np.array([force.getParticleParameters(i) for i in range(force.getNumParticles())], dtype=np.float64)
-        self.ctx.set_particle_parameters(p[:, self._iq], p[:, self._ir])
+        if self.custom is not None:
+            self.ctx.set_custom_parameters(p)
+        else:
+            self.ctx.set_particle_parameters(p[:, self._iq], p[:, self._ir])
 
     def setGlobalParameters(self, alpha0, alpha1):
         self.ctx.set_global_parameters(alpha0, alpha1)
+
+    def setGlobalParameter(self, name, value):
+        """A global parameter of a force outside the canonical set (Context.setParameter)."""
+        if self.custom is None:
+            raise GBXError(4, "the canonical set takes alpha0, alpha1 through setGlobalParameters")
+        self.ctx.set_custom_global(name, value)
 
     def setPeriodicBox(self, box):
         self.ctx.set_box(box)

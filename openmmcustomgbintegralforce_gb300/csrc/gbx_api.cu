@@ -2,6 +2,7 @@
 // execute pipeline and result queries.  No exception crosses this boundary.
 #include <math.h>
 #include <omp.h>
+#include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
@@ -110,6 +111,9 @@ gbx_status validate_config(const gbx_config& c, std::string& why) {
     for (int k = 0; k < 3; ++k)
       if (!(c.box[k] > 0)) return why = "periodic table needs a positive box", GBX_ERR_INVALID_ARGUMENT;
   if (c.table_cap > gbx::kMaxSortSegment) return why = "table_cap too large", GBX_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < 2; ++k)
+    if (c.integral_orders[k] != 0 && c.integral_orders[k] < 2)
+      return why = "integral orders must be >= 2", GBX_ERR_INVALID_ARGUMENT;
   if (c.periodic) {  // CutoffPeriodic (CharmmReferenceGBSW.cpp:147-159, CharmmReferenceGBMV.cpp:138-149)
     // the standalone GBSW table (wrapped query) or the box-sampled table of the integral classes
     if (c.table_mode == GBX_TABLE_GRID || (c.table_mode == GBX_TABLE_STANDALONE && c.model != GBX_MODEL_GBSW))
@@ -141,7 +145,14 @@ gbx_status upload_quadrature(Context* ctx) {
       for (int k = 0; k < 3; ++k) ctx->q_off[3 * q + k] = r * leb[4 * j + k];
       ctx->q_rad[q] = r;
       ctx->q_w[q] = wr[i] * leb[4 * j + 3];
-      const double w4 = ctx->q_w[q] / (r * r), w7 = ctx->q_w[q] / (r * r * r * r * r);
+      // weights of the two integrals, w / r^(n-2) (GBSWIntegral.cpp:96,144); orders 4 and 7 unless
+      // set (kept as the repeated products of the reference's 4 and 7: the same bits)
+      const double w4 = c.integral_orders[0] > 0 && c.integral_orders[0] != 4
+                            ? ctx->q_w[q] / std::pow(r, (double)(c.integral_orders[0] - 2))
+                            : ctx->q_w[q] / (r * r);
+      const double w7 = c.integral_orders[1] > 0 && c.integral_orders[1] != 7
+                            ? ctx->q_w[q] / std::pow(r, (double)(c.integral_orders[1] - 2))
+                            : ctx->q_w[q] / (r * r * r * r * r);
       S4 += w4;
       S7 += w7;
       qv[q] = make_float4((float)ctx->q_off[3 * q], (float)ctx->q_off[3 * q + 1], (float)ctx->q_off[3 * q + 2], (float)r);
@@ -453,6 +464,30 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   GBX_TRY(mark());
   GBX_TRY(gbx::launch_integrals(ctx, ctx->d_pos, count_work));
   GBX_TRY(mark());
+  if (ctx->custom) {
+    // expressions outside the canonical set: values, single and pair terms, dE/dJ
+    GBX_TRY(mark());
+    GBX_TRY(gbx::launch_custom_energy(ctx, ctx->d_pos, force, stride));
+    GBX_TRY(mark());
+    GBX_TRY(gbx::launch_custom_chain_prep(ctx));
+    GBX_TRY(mark());
+    if (chain) GBX_TRY(gbx::launch_chain(ctx, ctx->d_pos, force, stride, false));
+    GBX_TRY(mark());
+    GBX_TRY(gbx::launch_energy_reduce(ctx, energy, false));
+    GBX_TRY(mark());
+    GBX_TRY(gbx::launch_publish_status(ctx));
+    ctx->have_result = true;
+    if (check) {
+      unsigned st = 0;
+      GBX_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+      GBX_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (st & gbx::kStatusNonFinite) {
+        ctx->last_error = "non-finite computed value";
+        return GBX_ERR_NONFINITE;
+      }
+    }
+    return GBX_OK;
+  }
   GBX_TRY(gbx::launch_born(ctx));
   if (adjoint) {
     GBX_CUDA(cudaMemsetAsync(ctx->d_dEdq_fx, 0, sizeof(unsigned long long) * ctx->n, ctx->stream));
@@ -702,6 +737,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx) return GBX_ERR_INVALID_ARGUMENT;
   drop_graph(ctx);
+  gbx::custom_destroy(ctx);
   void* ptrs[] = {ctx->d_qv, ctx->d_qw, ctx->d_qoff, ctx->d_radius, ctx->d_charge, ctx->d_par, ctx->d_wpar,
                   ctx->d_geom, ctx->d_cell_count, ctx->d_cell_start, ctx->d_cell_cursor, ctx->d_entries,
                   ctx->d_block_sums, ctx->d_reduce, ctx->d_pos, ctx->d_J, ctx->d_born, ctx->d_bornf, ctx->d_dBdJ,
@@ -784,6 +820,102 @@ gbx_status gbx_set_box(gbx_context* handle, const double box[3]) {
     }
   for (int k = 0; k < 3; ++k) ctx->cfg.box[k] = box[k];
   return GBX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// A copy of a gbx_custom with owned strings, checked for what the device path supports.
+gbx_status custom_spec_of(const gbx_custom* cu, gbx::gbx_custom_spec& spec, std::string& why) {
+  if (!cu || cu->num_integrals < 1 || cu->num_integrals > 2 || cu->num_params < 1 || cu->num_values < 0 ||
+      cu->num_terms < 1 || cu->num_globals < 0)
+    return why = "need 1 or 2 integrals, parameters and energy terms", GBX_ERR_INVALID_ARGUMENT;
+  auto str = [](const char* s) { return std::string(s ? s : ""); };
+  for (int k = 0; k < cu->num_params; ++k) spec.params.push_back(str(cu->param_names[k]));
+  for (int k = 0; k < cu->num_globals; ++k) {
+    spec.globals.push_back(str(cu->global_names[k]));
+    spec.global_values.push_back(cu->global_values[k]);
+  }
+  for (int k = 0; k < cu->num_integrals; ++k) {
+    spec.integrals.push_back(str(cu->integral_names[k]));
+    spec.integral_orders.push_back(cu->integral_orders[k]);
+    if (cu->integral_orders[k] < 2)  // GBSWIntegral.cpp:85-88
+      return why = "the order of an integral must be greater or equal to 2", GBX_ERR_INVALID_ARGUMENT;
+  }
+  for (int k = 0; k < cu->num_values; ++k) {
+    spec.value_names.push_back(str(cu->value_names[k]));
+    spec.value_expressions.push_back(str(cu->value_expressions[k]));
+  }
+  for (int k = 0; k < cu->num_terms; ++k) {
+    spec.term_expressions.push_back(str(cu->term_expressions[k]));
+    if (cu->term_types[k] != GBX_TERM_SINGLE && cu->term_types[k] != GBX_TERM_PAIR)
+      return why = "unknown energy term type", GBX_ERR_INVALID_ARGUMENT;
+    spec.term_types.push_back(cu->term_types[k]);
+  }
+  if (std::find(spec.params.begin(), spec.params.end(), std::string("radius")) == spec.params.end())
+    return why = "the per-particle parameter 'radius' must be defined", GBX_ERR_INVALID_ARGUMENT;
+  return GBX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+gbx_status gbx_custom_check(const gbx_custom* cu, char* log, size_t len) {
+  gbx::gbx_custom_spec spec;
+  std::string why;
+  gbx_status s = custom_spec_of(cu, spec, why);
+  if (s == GBX_OK) s = gbx::custom_compile_only(spec, why);
+  if (log && len) {
+    strncpy(log, why.c_str(), len - 1);
+    log[len - 1] = 0;
+  }
+  return s;
+}
+
+gbx_status gbx_create_custom(const gbx_config* cfg, int num_atoms, const gbx_custom* cu, gbx_context** out) {
+  if (!cfg || !cu || !out || num_atoms < 1) return GBX_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  // the integral classes' tables (the standalone GBSW force has fixed expressions)
+  if (cfg->table_mode == GBX_TABLE_STANDALONE) return GBX_ERR_UNSUPPORTED;
+  gbx::gbx_custom_spec spec;
+  std::string why;
+  GBX_TRY(custom_spec_of(cu, spec, why));
+  gbx_config c = *cfg;
+  c.integral_orders[0] = spec.integral_orders[0];
+  c.integral_orders[1] = spec.integral_orders.size() > 1 ? spec.integral_orders[1] : spec.integral_orders[0];
+  gbx_context* h = nullptr;
+  GBX_TRY(gbx_create(&c, num_atoms, &h));
+  Context* ctx = reinterpret_cast<Context*>(h);
+  gbx_status s = gbx::custom_build(ctx, spec);
+  if (s == GBX_OK) {
+    ctx->energy_parts = gbx::custom_energy_parts(ctx);
+    s = dalloc(ctx, &ctx->d_energy_part, ctx->energy_parts);
+  }
+  if (s != GBX_OK) {
+    fprintf(stderr, "gbx_create_custom: %s\n", ctx->last_error.c_str());
+    gbx_destroy(h);
+    return s;
+  }
+  *out = h;
+  return GBX_OK;
+}
+
+gbx_status gbx_set_custom_parameters(gbx_context* handle, const double* params) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !params) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->custom) return GBX_ERR_UNSUPPORTED;
+  std::vector<double> radius;
+  GBX_TRY(gbx::custom_set_parameters(ctx, params, radius));
+  std::vector<double> q(ctx->n, 0.0);  // the custom terms read their own parameters
+  return gbx_set_particle_parameters(handle, q.data(), radius.data());
+}
+
+gbx_status gbx_set_custom_global(gbx_context* handle, const char* name, double value) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !name) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->custom) return GBX_ERR_UNSUPPORTED;
+  GBX_CUDA(cudaStreamSynchronize(ctx->stream));  // the copy must not race a call in flight
+  return gbx::custom_set_global(ctx, name, value);
 }
 
 gbx_status gbx_execute(gbx_context* handle, const void* posq, unsigned long long* force_fixed, int force_stride,
@@ -1061,6 +1193,10 @@ gbx_status gbx_adjoint_host(gbx_context* handle, const double* positions, double
                             double* dEdq, double* dEdR, double* dEdalpha) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !positions) return GBX_ERR_INVALID_ARGUMENT;
+  if (ctx->custom) {
+    ctx->last_error = "the adjoint covers the canonical expressions only";
+    return GBX_ERR_UNSUPPORTED;
+  }
   GBX_TRY(host_run(ctx, positions, true, false));
   const int n = ctx->n;
   std::vector<unsigned long long> q(n), r(n);
@@ -1086,6 +1222,10 @@ gbx_status gbx_adjoint(gbx_context* handle, const void* posq, double* energy, do
                        double* dEdR, double* dEdalpha, int flags, void* stream) {
   Context* ctx = reinterpret_cast<Context*>(handle);
   if (!ctx || !posq) return GBX_ERR_INVALID_ARGUMENT;
+  if (ctx->custom) {
+    ctx->last_error = "the adjoint covers the canonical expressions only";
+    return GBX_ERR_UNSUPPORTED;
+  }
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   const int n = ctx->n;
   GBX_CUDA(cudaMemsetAsync(ctx->d_force_fx, 0, sizeof(unsigned long long) * 3 * n, ctx->stream));

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gbx.h"
+#include "gbx_custom.h"
 
 namespace gbx {
 
@@ -175,6 +176,7 @@ struct Context {
   int* d_pblock_sums = nullptr;               // scan scratch
   TableGeom* d_pgeom = nullptr;               // the point scan's cell count and total
   bool gbmv_cells = false;                    // this call's GBMV passes run by cell
+  CustomPlan* custom = nullptr;               // expressions outside the canonical set (gbx_custom.cu)
   unsigned long long* d_force_fx = nullptr;  // internal force buffer [3n] (host path)
   double* d_energy = nullptr;     // internal energy (host path)
   unsigned long long* d_dEdR_fx = nullptr;  // adjoint [n]

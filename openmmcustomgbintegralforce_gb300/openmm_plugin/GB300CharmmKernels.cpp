@@ -66,6 +66,25 @@ void GbxForceState::setGlobals(double alpha0, double alpha1) {
   globals[1] = alpha1;
 }
 
+void GbxForceState::createCustom(const gbx_config& cfg, int n, const gbx_custom& custom) {
+  cu.setAsCurrent();
+  numAtoms = n;
+  customGlobals.assign(custom.global_values, custom.global_values + custom.num_globals);
+  for (int k = 0; k < 3; ++k) box[k] = cfg.box[k];
+  check(gbx_create_custom(&cfg, n, &custom, &handle), "gbx_create_custom (compiling the force's expressions)");
+}
+
+void GbxForceState::setCustomParameters(const std::vector<double>& params) {
+  cu.setAsCurrent();
+  check(gbx_set_custom_parameters(handle, params.data()), "gbx_set_custom_parameters");
+}
+
+void GbxForceState::setCustomGlobal(int index, const std::string& name, double value) {
+  if (customGlobals[index] == value) return;
+  check(gbx_set_custom_global(handle, name.c_str(), value), "gbx_set_custom_global");
+  customGlobals[index] = value;
+}
+
 void GbxForceState::setBox(double a, double b, double c) {
   if (a == box[0] && b == box[1] && c == box[2]) return;
   const double edges[3] = {a, b, c};
@@ -147,7 +166,7 @@ void GB300CalcCharmmGBSWForceKernel::copyParametersToContext(OpenMM::ContextImpl
 // CharmmGBMVForce
 // ---------------------------------------------------------------------------
 
-void checkCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int& radiusIndex) {
+bool isCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int& radiusIndex) {
   if (force.getGBIntegralType() == CharmmGBMVForce::CustomIntegral)
     throw OpenMMException("GB300: CustomIntegral has no implementation");
   chargeIndex = radiusIndex = -1;
@@ -157,6 +176,14 @@ void checkCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int
   }
   // GBSWIntegral.cpp:79-80
   if (radiusIndex < 0) throw OpenMMException("GBSWIntegral: the per perticle parameter 'radius' must be defined");
+  for (int k = 0; k < force.getNumGBIntegrals(); ++k) {
+    std::string name;
+    std::vector<int> pi;
+    std::vector<double> pr;
+    force.getGBIntegralParameters(k, name, pi, pr);
+    if (pi.empty()) throw OpenMMException("GBSWIntegral: the order of integral must be given");
+    if (pi[0] < 2) throw OpenMMException("GBSWIntegral: the order of integral must be greater or equal to 2");
+  }
   bool ok = chargeIndex >= 0 && force.getNumGBIntegrals() == 2 && force.getNumComputedValues() == 1 &&
             force.getNumEnergyTerms() == 2 && force.getNumExclusions() == 0 &&
             force.getNumTabulatedFunctions() == 0;
@@ -167,8 +194,6 @@ void checkCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int
     std::vector<int> pi;
     std::vector<double> pr;
     force.getGBIntegralParameters(k, name, pi, pr);
-    if (pi.empty()) throw OpenMMException("GBSWIntegral: the order of integral must be given");
-    if (pi[0] < 2) throw OpenMMException("GBSWIntegral: the order of integral must be greater or equal to 2");
     ok = name == integralNames[k] && pi[0] == orders[k];
   }
   if (ok) {
@@ -185,9 +210,7 @@ void checkCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int
     force.getEnergyTermParameters(1, expr, type);
     ok = ok && squeeze(expr) == squeeze(kPair) && type == CharmmGBMVForce::ParticlePairNoExclusions;
   }
-  if (!ok)
-    throw OpenMMException("GB300: the device path evaluates the canonical CHARMM GB expressions only; "
-                          "this CharmmGBMVForce needs the plugin's generic kernels");
+  return ok;
 }
 
 void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, const CharmmGBMVForce& force) {
@@ -199,7 +222,7 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     if ((int)p.size() != force.getNumPerParticleParameters())
       throw OpenMMException("CharmmGBMVForce: Wrong number of parameters for particle " + std::to_string(i));
   }
-  checkCanonicalGBMVForce(force, chargeIndex, radiusIndex);
+  custom = !isCanonicalGBMVForce(force, chargeIndex, radiusIndex);
   int preset = GBX_PRESET_GBSW_INTEGRAL;
   if (force.getGBIntegralType() == CharmmGBMVForce::GBMVIntegralTypeI) preset = GBX_PRESET_GBMV1;
   if (force.getGBIntegralType() == CharmmGBMVForce::GBMVIntegralTypeII) preset = GBX_PRESET_GBMV2;
@@ -219,20 +242,93 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     cfg.periodic = 1;
     cfg.table_mode = GBX_TABLE_PERIODIC;
   }
-  for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
-    const std::string& name = force.getGlobalParameterName(k);
-    if (name == "alpha0") cfg.alpha0 = force.getGlobalParameterDefaultValue(k);
-    if (name == "alpha1") cfg.alpha1 = force.getGlobalParameterDefaultValue(k);
+  if (!custom) {
+    for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
+      const std::string& name = force.getGlobalParameterName(k);
+      if (name == "alpha0") cfg.alpha0 = force.getGlobalParameterDefaultValue(k);
+      if (name == "alpha1") cfg.alpha1 = force.getGlobalParameterDefaultValue(k);
+    }
+    alphaNames[0] = "alpha0";
+    alphaNames[1] = "alpha1";
+    state.create(cfg, system.getNumParticles());
+  } else {
+    // the force's own expressions, compiled for the device
+    if (force.getNumExclusions() > 0 || force.getNumTabulatedFunctions() > 0)
+      throw OpenMMException("GB300: exclusions and tabulated functions are not supported");
+    std::vector<std::string> params, integrals, values, valueExprs, terms;
+    std::vector<double> globalValues;
+    std::vector<int> orders, types;
+    for (int k = 0; k < force.getNumPerParticleParameters(); ++k)
+      params.push_back(force.getPerParticleParameterName(k));
+    for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
+      globalNames.push_back(force.getGlobalParameterName(k));
+      globalValues.push_back(force.getGlobalParameterDefaultValue(k));
+    }
+    for (int k = 0; k < force.getNumGBIntegrals(); ++k) {
+      std::string name;
+      std::vector<int> pi;
+      std::vector<double> pr;
+      force.getGBIntegralParameters(k, name, pi, pr);
+      integrals.push_back(name);
+      orders.push_back(pi[0]);
+    }
+    for (int k = 0; k < force.getNumComputedValues(); ++k) {
+      std::string name, expr;
+      CharmmGBMVForce::ComputationType type;
+      force.getComputedValueParameters(k, name, expr, type);
+      if (type != CharmmGBMVForce::SingleParticle)
+        throw OpenMMException("GB300: computed values must be SingleParticle");
+      values.push_back(name);
+      valueExprs.push_back(expr);
+    }
+    for (int k = 0; k < force.getNumEnergyTerms(); ++k) {
+      std::string expr;
+      CharmmGBMVForce::ComputationType type;
+      force.getEnergyTermParameters(k, expr, type);
+      terms.push_back(expr);
+      types.push_back(type == CharmmGBMVForce::SingleParticle ? GBX_TERM_SINGLE : GBX_TERM_PAIR);
+    }
+    auto ptrs = [](const std::vector<std::string>& v) {
+      std::vector<const char*> p;
+      for (auto& x : v) p.push_back(x.c_str());
+      return p;
+    };
+    const auto pn = ptrs(params), gn = ptrs(globalNames), in = ptrs(integrals), vn = ptrs(values),
+               ve = ptrs(valueExprs), te = ptrs(terms);
+    gbx_custom cs;
+    cs.num_params = (int)params.size();
+    cs.param_names = pn.data();
+    cs.num_globals = (int)globalNames.size();
+    cs.global_names = gn.data();
+    cs.global_values = globalValues.data();
+    cs.num_integrals = (int)integrals.size();
+    cs.integral_names = in.data();
+    cs.integral_orders = orders.data();
+    cs.num_values = (int)values.size();
+    cs.value_names = vn.data();
+    cs.value_expressions = ve.data();
+    cs.num_terms = (int)terms.size();
+    cs.term_expressions = te.data();
+    cs.term_types = types.data();
+    state.createCustom(cfg, system.getNumParticles(), cs);
   }
-  alphaNames[0] = "alpha0";
-  alphaNames[1] = "alpha1";
-  state.create(cfg, system.getNumParticles());
   copyParameters(force);
 }
 
 void GB300CalcCharmmGBMVForceKernel::copyParameters(const CharmmGBMVForce& force) {
   const int n = force.getNumParticles();
-  std::vector<double> q(n), r(n), p;
+  std::vector<double> p;
+  if (custom) {
+    const int np = force.getNumPerParticleParameters();
+    std::vector<double> all((size_t)n * np);
+    for (int i = 0; i < n; ++i) {
+      force.getParticleParameters(i, p);
+      for (int k = 0; k < np; ++k) all[(size_t)i * np + k] = p[k];
+    }
+    state.setCustomParameters(all);
+    return;
+  }
+  std::vector<double> q(n), r(n);
   for (int i = 0; i < n; ++i) {
     force.getParticleParameters(i, p);
     q[i] = p[chargeIndex];
@@ -243,7 +339,12 @@ void GB300CalcCharmmGBMVForceKernel::copyParameters(const CharmmGBMVForce& force
 
 double GB300CalcCharmmGBMVForceKernel::execute(OpenMM::ContextImpl& context, bool includeForces,
                                               bool includeEnergy) {
-  state.setGlobals(context.getParameter(alphaNames[0]), context.getParameter(alphaNames[1]));
+  if (custom) {
+    for (size_t k = 0; k < globalNames.size(); ++k)
+      state.setCustomGlobal((int)k, globalNames[k], context.getParameter(globalNames[k]));
+  } else {
+    state.setGlobals(context.getParameter(alphaNames[0]), context.getParameter(alphaNames[1]));
+  }
   const auto b = state.cu.getPeriodicBoxSize();  // double4: x, y, z edges
   state.setBox(b.x, b.y, b.z);
   return state.execute(includeForces, includeEnergy);

@@ -34,6 +34,9 @@ class GbxForceState {
   void create(const gbx_config& cfg, int numAtoms);
   void setParameters(const std::vector<double>& charge, const std::vector<double>& radius);
   void setGlobals(double alpha0, double alpha1);
+  void createCustom(const gbx_config& cfg, int numAtoms, const gbx_custom& custom);
+  void setCustomParameters(const std::vector<double>& params);  // [n][num_params]
+  void setCustomGlobal(int index, const std::string& name, double value);
   void setBox(double a, double b, double c);
   // One evaluation on OpenMM's buffers; the energy is added to OpenMM's
   // energy buffer, so the kernel returns 0 as the reference CUDA kernel does.
@@ -47,6 +50,7 @@ class GbxForceState {
  private:
   bool orderSet = false;
   double globals[2] = {0.0, 0.0};
+  std::vector<double> customGlobals;
   double box[3] = {0.0, 0.0, 0.0};
 };
 
@@ -77,11 +81,16 @@ class GB300CalcCharmmGBMVForceKernel : public OpenMM::CalcCharmmGBMVForceKernel 
   GbxForceState state;
   int chargeIndex = -1, radiusIndex = -1;
   std::string alphaNames[2];
+  bool custom = false;                    // expressions outside the canonical set
+  std::vector<std::string> globalNames;   // the force's global parameters (custom)
 };
 
-// The expression set the device path evaluates for CharmmGBMVForce:
-// parameters q and radius, integrals I4 {4} and I7 {7}, the computed value
-// B and the self and pair energy terms.  Other expressions throw.
-void checkCanonicalGBMVForce(const OpenMM::CharmmGBMVForce& force, int& chargeIndex, int& radiusIndex);
+// Whether the force uses the canonical CHARMM expression set (parameters q
+// and radius, integrals I4 {4} and I7 {7}, the computed value B and the
+// self and pair energy terms), which the library's fixed kernels evaluate;
+// other sets are compiled for the device (gbx_create_custom).  Throws for
+// what neither path supports (CustomIntegral, a missing "radius", an
+// integral of order below 2).
+bool isCanonicalGBMVForce(const OpenMM::CharmmGBMVForce& force, int& chargeIndex, int& radiusIndex);
 
 }  // namespace GB300

@@ -181,18 +181,37 @@ int main() {
   {
     CharmmGBMVForce force;
     canonical(force, CharmmGBMVForce::GBMVIntegralTypeI);
-    force.addEnergyTerm("0.1*q", CharmmGBMVForce::SingleParticle);  // not the canonical set
+    force.addGlobalParameter("gamma", 0.5);
+    force.addEnergyTerm("gamma*radius^2", CharmmGBMVForce::SingleParticle);  // outside the canonical set
+    KernelFactory* gf = cuda.factories["CalcCharmmGBMVForce"];
+    std::unique_ptr<KernelImpl> k(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
+    auto& gbmv = dynamic_cast<CalcCharmmGBMVForceKernel&>(*k);
+    gbmv.initialize(system, force);
+    EXPECT(logged("create_custom n=4 model=1 params q radius integrals I4:4 I7:7 values B terms 0 1 0"));
+    EXPECT(logged("custom_params p00=0.2 p01=0.17"));
+    context.setParameter("gamma", 0.5);
+    gbmv.execute(context, true, true);
+    EXPECT(!logged("custom_global gamma"));
+    EXPECT(count("custom_global alpha0 -0.2") == 1);  // the context's value, changed by the scenario above
+    context.setParameter("gamma", 0.75);
+    gbmv.execute(context, true, true);
+    gbmv.execute(context, true, true);
+    EXPECT(count("custom_global gamma 0.75") == 1);
+    dump("gbmv expressions outside the canonical set: compiled");
+  }
+  {
+    CharmmGBMVForce force;
+    canonical(force, CharmmGBMVForce::CustomIntegral);
     KernelFactory* gf = cuda.factories["CalcCharmmGBMVForce"];
     std::unique_ptr<KernelImpl> k(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
     bool threw = false;
     try {
       dynamic_cast<CalcCharmmGBMVForceKernel&>(*k).initialize(system, force);
     } catch (const OpenMMException& e) {
-      threw = std::string(e.what()).find("canonical") != std::string::npos;
+      threw = std::string(e.what()).find("CustomIntegral") != std::string::npos;
     }
     EXPECT(threw);
-    EXPECT(!logged("create"));
-    dump("gbmv non-canonical expressions refused");
+    dump("custom integral refused");
   }
   {
     bool threw = false;

@@ -63,6 +63,33 @@ gbx_status gbx_set_global_parameters(gbx_context*, double a0, double a1) {
   log(b);
   return GBX_OK;
 }
+gbx_status gbx_create_custom(const gbx_config* cfg, int n, const gbx_custom* cs, gbx_context** out) {
+  g_last_config = *cfg;
+  *out = new gbx_context{n};
+  std::string s = "create_custom n=" + std::to_string(n) + " model=" + std::to_string(cfg->model) + " params";
+  for (int k = 0; k < cs->num_params; ++k) s += std::string(" ") + cs->param_names[k];
+  s += " integrals";
+  for (int k = 0; k < cs->num_integrals; ++k)
+    s += std::string(" ") + cs->integral_names[k] + ":" + std::to_string(cs->integral_orders[k]);
+  s += " values";
+  for (int k = 0; k < cs->num_values; ++k) s += std::string(" ") + cs->value_names[k];
+  s += " terms";
+  for (int k = 0; k < cs->num_terms; ++k) s += " " + std::to_string(cs->term_types[k]);
+  log(s);
+  return GBX_OK;
+}
+gbx_status gbx_set_custom_parameters(gbx_context*, const double* p) {
+  char b[128];
+  std::snprintf(b, sizeof(b), "custom_params p00=%g p01=%g p02=%g", p[0], p[1], p[2]);
+  log(b);
+  return GBX_OK;
+}
+gbx_status gbx_set_custom_global(gbx_context*, const char* name, double v) {
+  char b[128];
+  std::snprintf(b, sizeof(b), "custom_global %s %g", name, v);
+  log(b);
+  return GBX_OK;
+}
 gbx_status gbx_set_box(gbx_context*, const double box[3]) {
   char b[128];
   std::snprintf(b, sizeof(b), "box %g %g %g", box[0], box[1], box[2]);

@@ -1,0 +1,72 @@
+"""The custom-expression oracle (oracle/custom.py) pinned to the FP64 oracle:
+the canonical CHARMM set written as user expressions reproduces the
+canonical evaluation (CharmmReferenceGBSW's formulas) for the GBMV-II and
+GBSW-integral classes, and its forces are minus the gradient of its energy
+for an expression set outside the canonical one.  Also the library's own
+expression compiler on the CPU: every set compiles, and a wrong one is
+refused with a message (gbx_custom_check: no device needed)."""
+import copy
+
+import numpy as np
+import pytest
+
+from openmmcustomgbintegralforce_gb300.globule import make_globule
+from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
+from oracle import oracle as O
+from oracle.custom import CustomOracle
+from tests.custom_sets import CANONICAL, MODIFIED, modified_params
+
+
+@pytest.fixture(scope="module")
+def glob():
+    return make_globule(150, seed=71)
+
+
+@pytest.mark.parametrize("cls", ["gbmv2", "gbsw_integral"])
+def test_canonical_expressions_match_canonical_oracle(glob, cls):
+    g = glob
+    m = GBModel.gbmv2(box=box_for(g.positions, margin=1.0)) if cls == "gbmv2" else GBModel.gbsw_integral()
+    ref = O.Oracle(m).energy_forces(g.positions, g.charge, g.radius)
+    got = CustomOracle(m, CANONICAL).energy_forces(g.positions, np.stack([g.charge, g.radius], axis=1))
+    assert abs(got["energy"] / ref["energy"] - 1) < 1e-12
+    assert np.abs(got["forces"] - ref["forces"]).max() < 1e-10 * np.abs(ref["forces"]).max()
+    assert np.abs(got["values"][0] / ref["born"] - 1).max() < 1e-12
+
+
+def test_modified_expressions_forces_are_energy_gradient(glob):
+    g = glob
+    m = GBModel.gbmv2(box=box_for(g.positions, margin=1.0))
+    P = modified_params(g)
+    orc = CustomOracle(m, MODIFIED)
+    out = orc.energy_forces(g.positions, P)
+    rng = np.random.default_rng(4)
+    h = 1e-6
+    F = out["forces"]
+    for flat in rng.choice(3 * g.n, size=6, replace=False):
+        i, d = int(flat) // 3, int(flat) % 3
+        xp, xm = g.positions.copy(), g.positions.copy()
+        xp[i, d] += h
+        xm[i, d] -= h
+        fd = -(orc.energy_forces(xp, P)["energy"] - orc.energy_forces(xm, P)["energy"]) / (2 * h)
+        assert abs(fd - F[i, d]) <= 1e-6 * np.abs(F).max() + 1e-5 * abs(F[i, d]), (i, d, fd, F[i, d])
+
+
+def test_library_compiles_and_refuses_expression_sets():
+    from openmmcustomgbintegralforce_gb300._lib import check_custom
+
+    for s in (CANONICAL, MODIFIED):
+        st, msg = check_custom(s)
+        if st == 4 and "NVRTC" in msg:
+            pytest.skip("NVRTC not available")
+        assert st == 0, msg
+    bad = copy.deepcopy(MODIFIED)
+    bad["terms"] = [("q^2/Bx", 0)]
+    st, msg = check_custom(bad)
+    assert st != 0 and "Bx" in msg
+    bad["terms"] = [("q^2/(B", 0)]
+    st, msg = check_custom(bad)
+    assert st != 0 and "expected ')'" in msg
+    bad = copy.deepcopy(MODIFIED)
+    bad["params"] = ["q", "s"]
+    st, msg = check_custom(bad)
+    assert st != 0 and "radius" in msg

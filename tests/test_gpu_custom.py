@@ -1,0 +1,135 @@
+"""CharmmGBMVForce expressions compiled into device code (gbx_create_custom),
+through the C ABI, against the FP64 custom-expression oracle
+(oracle/custom.py, itself pinned to the canonical oracle):
+
+* the canonical set written as user expressions gives the canonical
+  context's results;
+* a set outside it (a second computed value, globals, a nonpolar
+  single-particle term, a Lepton definition) for the GBMV-II and
+  GBSW-integral classes, with and without a cutoff;
+* a global parameter update, bit-reproducible calls, and a refused
+  expression.
+
+Tolerances as the parity suite: energy 2e-5 relative, forces 1e-4 relative
+RMS, the first computed value (the Born radius) 1e-4 maximum relative.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from openmmcustomgbintegralforce_gb300._lib import Context, CustomContext, GBXError
+from openmmcustomgbintegralforce_gb300.globule import make_globule
+from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
+from oracle.custom import CustomOracle
+from tests.custom_sets import CANONICAL, MODIFIED, modified_params
+
+pytestmark = pytest.mark.gpu
+
+E_TOL, F_TOL, B_TOL = 2e-5, 1e-4, 1e-4
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+@pytest.fixture(scope="module")
+def glob():
+    return make_globule(1000, seed=73)
+
+
+def model_of(cls, g, **kw):
+    if cls == "gbmv2":
+        return GBModel.gbmv2(box=box_for(g.positions, margin=1.0), **kw)
+    return GBModel.gbsw_integral(**kw)
+
+
+def test_canonical_set_matches_canonical_context(glob):
+    g = glob
+    m = model_of("gbmv2", g)
+    ref = Context(m, g.n)
+    ref.set_particle_parameters(g.charge, g.radius)
+    E0, F0 = ref.execute_host(g.positions)
+    ctx = CustomContext(m, g.n, CANONICAL)
+    ctx.set_custom_parameters(np.stack([g.charge, g.radius], axis=1))
+    E1, F1 = ctx.execute_host(g.positions)
+    print(f"canonical as expressions: energy {abs(E1 / E0 - 1):.2e} forces {rel_rms(F1, F0):.2e}")
+    assert abs(E1 / E0 - 1) < E_TOL
+    assert rel_rms(F1, F0) < F_TOL
+    assert np.abs(ctx.born_radii() / ref.born_radii() - 1).max() < B_TOL
+    ctx.close()
+    ref.close()
+
+
+@pytest.mark.parametrize("cls,cutoff", [("gbmv2", 0.0), ("gbsw_integral", 0.0), ("gbmv2", 1.2)])
+def test_modified_set_vs_oracle(glob, cls, cutoff):
+    g = glob
+    m = model_of(cls, g, cutoff=cutoff)
+    P = modified_params(g)
+    ctx = CustomContext(m, g.n, MODIFIED)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(g.positions)
+    E2, F2 = ctx.execute_host(g.positions)
+    assert E2 == E and np.array_equal(F2, F)
+    ref = CustomOracle(m, MODIFIED).energy_forces(g.positions, P)
+    print(f"{cls} cutoff={cutoff}: energy {abs(E / ref['energy'] - 1):.2e} forces {rel_rms(F, ref['forces']):.2e}")
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    assert np.abs(ctx.born_radii() / ref["values"][0] - 1).max() < B_TOL
+    ctx.close()
+
+
+def test_global_update(glob):
+    g = glob
+    m = model_of("gbmv2", g)
+    P = modified_params(g)
+    ctx = CustomContext(m, g.n, MODIFIED)
+    ctx.set_custom_parameters(P)
+    ctx.execute_host(g.positions)
+    ctx.set_custom_global("eps", 4.0)
+    E, F = ctx.execute_host(g.positions)
+    mod = dict(MODIFIED, globals=dict(MODIFIED["globals"], eps=4.0))
+    ref = CustomOracle(m, mod).energy_forces(g.positions, P)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    with pytest.raises(GBXError):
+        ctx.set_custom_global("no_such", 1.0)
+    ctx.close()
+
+
+def test_refused_expression(glob):
+    g = glob
+    bad = copy.deepcopy(MODIFIED)
+    bad["terms"] = [("q^2/Bx", 0)]
+    with pytest.raises(GBXError):
+        CustomContext(model_of("gbmv2", g), g.n, bad)
+
+
+def test_kernel_mirror_compiles_a_non_canonical_force(glob):
+    """The Python mirror of the GBMV kernel takes a force outside the
+    canonical set through the compiled path."""
+    from openmmcustomgbintegralforce_gb300 import api
+
+    g = glob
+    f = api.CharmmGBMVForce()
+    for p in MODIFIED["params"]:
+        f.addPerParticleParameter(p)
+    for k, v in MODIFIED["globals"].items():
+        f.addGlobalParameter(k, v)
+    for name, order in MODIFIED["integrals"]:
+        f.addGBIntegral(name, [order], [])
+    for name, e in MODIFIED["values"]:
+        f.addComputedValue(name, e, api.SingleParticle)
+    for e, t in MODIFIED["terms"]:
+        f.addEnergyTerm(e, api.SingleParticle if t == 0 else api.ParticlePairNoExclusions)
+    f.setGBIntegralType(api.GBMVIntegralTypeII)
+    P = modified_params(g)
+    for row in P:
+        f.addParticle(list(row))
+    box = box_for(g.positions, margin=1.0)
+    k = api.CalcCharmmGBMVForceKernel(box=box)
+    k.initialize(g.n, f)
+    E, F = k.execute(g.positions)
+    ref = CustomOracle(GBModel.gbmv2(box=box), MODIFIED).energy_forces(g.positions, P)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL

@@ -9,8 +9,9 @@ initialize / execute / copyParametersToContext -- and checks the calls the
 adapter makes: the atom order handed over before the first step and after
 each reorder (parameters are not re-sent), the flags of each OpenMM
 precision mode, the box and global-parameter updates, an earlier step's
-overflowed table surfacing as an OpenMMException, and the refusal of
-non-canonical expressions.
+overflowed table surfacing as an OpenMMException, a force outside the
+canonical expression set handed to gbx_create_custom with its global
+parameters followed, and the refusal of CustomIntegral.
 """
 import os
 import shutil
