@@ -91,6 +91,11 @@ def workloads():
                                desc="GBSW 50,000-atom globule, 32x110 quadrature, 2.0 nm pair cutoff"),
         "gbsw10k": dict(n=10000, seed=2028, model=GBModel.charmm_gbsw(n_radial=32, lebedev=110),
                         desc="GBSW 10,000-atom globule, 32x110 quadrature (profiling case)"),
+        "gbsw10k_cutoff": dict(n=10000, seed=2028, model=GBModel.charmm_gbsw(n_radial=32, lebedev=110, cutoff=1.5),
+                               desc="GBSW 10,000-atom globule, 32x110 quadrature, 1.5 nm pair cutoff (profiling case)"),
+        "gbsw10k_periodic": dict(n=10000, seed=2028, model=None, periodic_cutoff=1.5,
+                                 desc="GBSW 10,000-atom globule in a box 0.5 nm wider than it on every side, "
+                                      "32x110 quadrature, CutoffPeriodic 1.5 nm (profiling case)"),
         "gbmv10k": dict(n=10000, seed=2027, model=None, gbmv=2,
                         desc="GBMV-II 10,000-atom globule, 24x50 quadrature"),
         "gbmv1_10k": dict(n=10000, seed=2027, model=None, gbmv=1,
@@ -113,6 +118,9 @@ def workload_config(name, w, model, world, jitter_A):
 def model_for(w, g):
     if w.get("model") is not None:
         return w["model"]
+    if w.get("periodic_cutoff"):
+        return GBModel.charmm_gbsw(n_radial=32, lebedev=110, cutoff=w["periodic_cutoff"], periodic=True,
+                                   box=box_for(g.positions, margin=0.5))
     box = box_for(g.positions, margin=1.0)
     if w["gbmv"] == 1:
         return GBModel.gbmv1(box=box, lebedev=50)
@@ -374,6 +382,75 @@ def rel_rms(a, b):
     return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
 
 
+def stage_roofline(ctx, model, g, n, step, flush, sptr, posq, force, stride, energy, sms, peaks, peak_src):
+    """Stage times (CUDA events the library records on its own stream, median
+    of 5 calls with L2 flushed before each), each stage's rate in TFLOP/s of
+    the reference algorithm's work on this input, and the dominant stage's
+    fraction of the FP32 peak."""
+    import torch
+
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_CHECK, EXEC_COUNT_WORK, EXEC_ENERGY, EXEC_FORCES, Context
+
+    ctx.set_timing(True)
+    stages = []
+    for k in range(5):
+        flush.fill_(1.0)
+        step(EXEC_FORCES | EXEC_ENERGY)
+        torch.cuda.synchronize()
+        stages.append(ctx.stage_times())
+    ctx.set_timing(False)
+    stage_ms = {k: float(np.median([s[k] for s in stages])) for k in stages[0]}
+
+    # executed work, and the reference algorithm's work on the same input:
+    # its own table, ascending lists, stop at the first burying atom (counted
+    # on the device by a reference-table context, outside the timed region)
+    step(EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK | EXEC_COUNT_WORK)
+    torch.cuda.synchronize()
+    executed = ctx.work()
+    if model.table_mode == 0 and not model.reference_table:
+        rctx = Context(model.replace(reference_table=True), n)
+        rctx.set_particle_parameters(g.charge, g.radius)
+        rctx.execute_device(posq.data_ptr(), force.data_ptr(), stride, energy.data_ptr(),
+                            EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK | EXEC_COUNT_WORK, sptr)
+        torch.cuda.synchronize()
+        work = rctx.work()
+        rctx.close()
+    else:
+        work = executed
+
+    fp32_peak = sms * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
+    points = float(n) * model.n_quad
+    if model.model == 0:
+        integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
+            FLOPS_POINT * points
+        chain_flops = FLOPS_CHAIN_EVAL * work["chain_list_evals"] + FLOPS_CHAIN_SHELL * work["chain_derivative_evals"] + \
+            FLOPS_POINT * points
+    else:
+        ev, ch = (FLOPS_GBMV1_EVAL, FLOPS_GBMV1_CHAIN) if model.model == 1 else (FLOPS_GBMV2_EVAL, FLOPS_GBMV2_CHAIN)
+        integral_flops = ev * work["volume_evals"] + (FLOPS_POINT + FLOPS_GBMV_POINT[model.model]) * points
+        chain_flops = ch * work["chain_list_evals"] + (FLOPS_POINT + FLOPS_GBMV_CHAIN_POINT) * points
+    pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
+    cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
+            "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12,
+            "chain_rule": chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12}
+    dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
+    achieved = cand.get(dominant)
+    return {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": (achieved / fp32_peak) if achieved else None,
+            "peak_source": f"nominal FP32 ({sms} SM x 128 lanes x 2 flop x max SM clock); "
+                           f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
+            "per_stage_tflops": cand, "per_stage_frac": {k: v / fp32_peak for k, v in cand.items()},
+            "stage_ms": stage_ms,
+            "work": {"volume_evals": work["volume_evals"], "shell_evals": work["shell_evals"],
+                     "points": points, "pairs": n * (n - 1) / 2.0,
+                     "chain_list_evals": work["chain_list_evals"],
+                     "chain_derivative_evals": work["chain_derivative_evals"],
+                     "executed_volume_evals": executed["volume_evals"],
+                     "executed_shell_evals": executed["shell_evals"],
+                     "note": "volume_evals/shell_evals: the reference algorithm's list work on this input "
+                             "(its table, ascending lists, first-burying-atom exit); executed_*: this run's"}}
+
+
 def measure_config(name, steps, jitter_A, dev, flush):
     """One configuration end to end on device-resident inputs: evals/s from
     CUDA events around each call (L2 flushed between calls; with jitter the
@@ -434,6 +511,13 @@ def measure_config(name, steps, jitter_A, dev, flush):
     res = {"workload": name, "desc": w["desc"], "atoms": n, "quadrature_points": model.n_quad, "steps": steps,
            "evals_per_s": 1000.0 / ms, "ms_per_step": ms, "gpu_launches_per_step": launches / steps,
            "jitter_A": jitter_A, "l2": "flushed (256 MiB write) between steps"}
+    if not adjoint:
+        peaks, peak_src = measured_peaks()
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        rl = stage_roofline(ctx, model, g, n, step, flush, sptr, posq, force, n, energy, sms, peaks, peak_src)
+        rl["traffic"] = TRAFFIC.get(name, {}).get(rl["kernel"])
+        rl["traffic_source"] = TRAFFIC_SOURCE.get(name)
+        res["roofline"] = rl
     if adjoint:
         # host arrays in, every gradient out
         ctx.adjoint(x)
@@ -553,70 +637,13 @@ def main():
     ms = allmax(world, float(np.mean(step_ms)))
     value = replica_value(world, ms)
 
-    # stage breakdown (events recorded by the library on its stream)
-    ctx.set_timing(True)
-    stages = []
-    for k in range(5):
-        flush.fill_(1.0)
-        step(EXEC_FORCES | EXEC_ENERGY)
-        torch.cuda.synchronize()
-        stages.append(ctx.stage_times())
-    ctx.set_timing(False)
-    stage_ms = {k: float(np.median([s[k] for s in stages])) for k in stages[0]}
-
-    # executed work, and the reference algorithm's work on the same input:
-    # its own table, ascending lists, stop at the first burying atom (counted
-    # on the device by a reference-table context, outside the timed region)
-    step(EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK | EXEC_COUNT_WORK)
-    torch.cuda.synchronize()
-    executed = ctx.work()
-    if model.table_mode == 0 and not model.reference_table:
-        rctx = Context(model.replace(reference_table=True), n)
-        rctx.set_particle_parameters(g.charge, g.radius)
-        rctx.execute_device(posq.data_ptr(), force.data_ptr(), stride, energy.data_ptr(),
-                            EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK | EXEC_COUNT_WORK, sptr)
-        torch.cuda.synchronize()
-        work = rctx.work()
-        rctx.close()
-    else:
-        work = executed
-
     peaks, peak_src = measured_peaks()
-    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    fp32_peak = sms * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
-    points = float(n) * model.n_quad
-    if model.model == 0:
-        integral_flops = FLOPS_GBSW_EVAL * work["volume_evals"] + FLOPS_GBSW_SHELL * work["shell_evals"] + \
-            FLOPS_POINT * points
-        chain_flops = FLOPS_CHAIN_EVAL * work["chain_list_evals"] + FLOPS_CHAIN_SHELL * work["chain_derivative_evals"] + \
-            FLOPS_POINT * points
-    else:
-        ev, ch = (FLOPS_GBMV1_EVAL, FLOPS_GBMV1_CHAIN) if model.model == 1 else (FLOPS_GBMV2_EVAL, FLOPS_GBMV2_CHAIN)
-        integral_flops = ev * work["volume_evals"] + (FLOPS_POINT + FLOPS_GBMV_POINT[model.model]) * points
-        chain_flops = ch * work["chain_list_evals"] + (FLOPS_POINT + FLOPS_GBMV_CHAIN_POINT) * points
-    pair_flops = FLOPS_PAIR * n * (n - 1) / 2.0
-    cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
-            "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12,
-            "chain_rule": chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12}
-    dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
-    achieved = cand.get(dominant)
-    roofline = {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": (achieved / fp32_peak) if achieved else None,
-                "traffic": TRAFFIC.get(args.workload, {}).get(dominant),
-                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                                   + TRAFFIC_SOURCE[args.workload]) if args.workload in TRAFFIC_SOURCE else None,
-                "peak_source": f"nominal FP32 ({sms} SM x 128 lanes x 2 flop x max SM clock); "
-                               f"MEASURED_PEAKS.json ({peak_src}) has no FP32 figure",
-                "per_stage_tflops": cand, "stage_ms": stage_ms,
-                "work": {"volume_evals": work["volume_evals"], "shell_evals": work["shell_evals"],
-                         "points": points, "pairs": n * (n - 1) / 2.0,
-                         "chain_list_evals": work["chain_list_evals"],
-                         "chain_derivative_evals": work["chain_derivative_evals"],
-                         "executed_volume_evals": executed["volume_evals"],
-                         "executed_shell_evals": executed["shell_evals"],
-                         "note": "volume_evals/shell_evals: the reference algorithm's list work on this input "
-                                 "(its table, ascending lists, first-burying-atom exit); executed_*: this run's"}}
+    roofline = stage_roofline(ctx, model, g, n, step, flush, sptr, posq, force, stride, energy, sms, peaks, peak_src)
+    dominant = roofline["kernel"]
+    roofline["traffic"] = TRAFFIC.get(args.workload, {}).get(dominant)
+    roofline["traffic_source"] = (("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                   + TRAFFIC_SOURCE[args.workload]) if args.workload in TRAFFIC_SOURCE else None)
 
     # e2e: host buffers through gbx_execute_host (copies inside the timed region)
     for _ in range(2):

@@ -229,6 +229,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_rmax, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_geom, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_tgeom, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_wgeom, 1));
   GBX_CUDA(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
   GBX_CUDA(cudaMemset(ctx->d_work, 0, sizeof(unsigned long long) * 4));
   GBX_CUDA(cudaMallocHost((void**)&ctx->h_pos, sizeof(float4) * n));
@@ -609,6 +610,27 @@ gbx_status fix_chain_records(Context* ctx) {
   if (ctx->srec_R >= want && ctx->srec_R > 0) return GBX_OK;
   return alloc_records(ctx, want);
 }
+
+void choose_table(Context* ctx) {
+  const gbx_config& c = ctx->cfg;
+  bool tight = ctx->tight_eligible;
+  if (tight && c.periodic) {
+    // the standalone grid lists atoms out to its pad from a cell's grid point
+    // (CharmmReferenceGBSW.cpp:454-455), so up to the pad plus a cell
+    // diagonal from a point; the exact table at the moved point equals the
+    // reference only while that is below half of every box edge, where the
+    // minimum image of every listed atom is the atom itself
+    double rmax = 0.0;
+    for (double r : ctx->radius) rmax = std::max(rmax, r);
+    const double reach = c.table_buffer + (rmax + 0.03) + c.switch_width + 1.5 * sqrt(3.0) * c.grid_length + 1e-3;
+    tight = reach < 0.5 * std::min(c.box[0], std::min(c.box[1], c.box[2]));
+  }
+  if (tight == ctx->use_tight) return;
+  drop_graph(ctx);
+  ctx->use_tight = tight;
+  ctx->tight_valid = false;
+  ctx->table_valid = false;
+}
 }  // namespace gbx
 
 extern "C" {
@@ -708,9 +730,11 @@ gbx_status gbx_create(const gbx_config* cfg, int num_atoms, gbx_context** out) {
     delete ctx;
     return GBX_ERR_CUDA;
   }
-  // the exact table assumes plain distances: a periodic system integrates on the reference table
-  ctx->use_tight = cfg->model == GBX_MODEL_GBSW && cfg->table_mode == GBX_TABLE_STANDALONE &&
-                   cfg->table_policy == GBX_TABLE_POLICY_AUTO && !cfg->periodic;
+  // the exact table serves GBSW on a standalone table; a periodic system
+  // only while the box is wide enough for its parameters (choose_table)
+  ctx->tight_eligible = cfg->model == GBX_MODEL_GBSW && cfg->table_mode == GBX_TABLE_STANDALONE &&
+                        cfg->table_policy == GBX_TABLE_POLICY_AUTO;
+  ctx->use_tight = ctx->tight_eligible && !cfg->periodic;
   ctx->tight_h = cfg->tight_grid_length > 0 ? cfg->tight_grid_length : 0.1;
   s = upload_quadrature(ctx);
   if (s == GBX_OK) s = alloc_atom_buffers(ctx);
@@ -743,7 +767,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_block_sums, ctx->d_reduce, ctx->d_pos, ctx->d_J, ctx->d_born, ctx->d_bornf, ctx->d_dBdJ,
                   ctx->d_integrals, ctx->d_dEdB_fx, ctx->d_dEdJ, ctx->d_energy_part, ctx->d_force_fx,
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
-                  ctx->d_tgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
+                  ctx->d_tgeom, ctx->d_wgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
                   ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
                   ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate,
@@ -794,6 +818,7 @@ gbx_status gbx_set_particle_parameters(gbx_context* handle, const double* charge
   GBX_CUDA(cudaMemcpy(ctx->d_charge, qf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemcpy(ctx->d_wpar, wpar.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemcpy(ctx->d_par, par.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  gbx::choose_table(ctx);
   return GBX_OK;
 }
 
@@ -819,6 +844,7 @@ gbx_status gbx_set_box(gbx_context* handle, const double box[3]) {
       return GBX_ERR_INVALID_ARGUMENT;
     }
   for (int k = 0; k < 3; ++k) ctx->cfg.box[k] = box[k];
+  gbx::choose_table(ctx);
   return GBX_OK;
 }
 

@@ -130,8 +130,10 @@ struct Context {
   // exact GBSW table (GBX_TABLE_POLICY_AUTO on a standalone table):
   // count[c] = -1 marks a cell every point of which is buried
   bool use_tight = false;
+  bool tight_eligible = false;   // GBSW on a standalone table with the AUTO policy
   double tight_h = 0.1;
   TableGeom* d_tgeom = nullptr;
+  TableGeom* d_wgeom = nullptr;  // periodic: the reference's standalone grid (its edges decide the move)
   long long tcell_cap = 0, tentry_cap = 0;
   int* d_tcount = nullptr;
   int* d_tstart = nullptr;
@@ -298,6 +300,10 @@ gbx_status pipeline(Context* ctx, const float4* posq, unsigned long long* force,
                     bool adjoint, bool count_work, bool forces);
 gbx_status set_chunks(Context* ctx, int chunks);
 gbx_status fix_chain_records(Context* ctx);
+// Whether the exact GBSW table serves this context's configuration and
+// parameters (a periodic one needs the standalone grid's reach below half
+// the shortest box edge); switching drops graphs and tables.
+void choose_table(Context* ctx);
 
 gbx_status launch_stage_positions(Context* ctx, const void* posq);
 gbx_status launch_finish_outputs(Context* ctx, unsigned long long* force, int stride, float* energy_float);
@@ -305,6 +311,8 @@ gbx_status launch_publish_status(Context* ctx);
 gbx_status launch_table_build(Context* ctx, const float4* pos);
 size_t table_geom_scratch_doubles(int n);
 gbx_status launch_tight_build(Context* ctx, const float4* pos);
+// The standalone (reference) table's grid geometry alone, into out.
+void launch_standalone_geom(Context* ctx, const float4* pos, TableGeom* out);
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);

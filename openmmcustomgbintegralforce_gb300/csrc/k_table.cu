@@ -426,6 +426,19 @@ int grid_for(long long work, int per_block) {
 
 }  // namespace
 
+void launch_standalone_geom(Context* ctx, const float4* pos, TableGeom* out) {
+  const gbx_config& c = ctx->cfg;
+  cudaStream_t st = ctx->stream;
+  const int nparts = (ctx->n + kPartThreads - 1) / kPartThreads;
+  GeomPart* parts = reinterpret_cast<GeomPart*>(ctx->d_reduce);
+  table_geom_partial_kernel<<<nparts, kPartThreads, 0, st>>>(pos, ctx->d_radius, ctx->n, parts);
+  // no cell of this grid is ever allocated or indexed: no capacity to check
+  table_geom_kernel<<<1, kGeomThreads, 0, st>>>(parts, nparts, ctx->n, GBX_TABLE_STANDALONE, c.grid_length,
+                                                c.table_buffer, c.switch_width, c.box[0], c.box[1], c.box[2], out,
+                                                0x7fffffffffffffffLL, ctx->d_status);
+  ctx->launches += 2;
+}
+
 gbx_status launch_table_build(Context* ctx, const float4* pos) {
   const gbx_config& c = ctx->cfg;
   cudaStream_t st = ctx->stream;

@@ -36,7 +36,7 @@ constexpr int kSortLanes = 8;                                   // lanes per sho
 constexpr int kSortSmall = kSortBuf / (kWarp / kSortLanes);     // longest short list (64)
 
 __global__ void __launch_bounds__(kGeomThreads) tight_geom_kernel(const float4* __restrict__ pos, int n, double h,
-                                                                  double w, TableGeom* __restrict__ g,
+                                                                  double w, double extent, TableGeom* __restrict__ g,
                                                                   long long cell_cap, unsigned* __restrict__ status) {
   __shared__ float s_min[3][kGeomThreads / kWarp], s_max[3][kGeomThreads / kWarp], s_r[kGeomThreads / kWarp];
   const int t = threadIdx.x;
@@ -94,7 +94,8 @@ __global__ void __launch_bounds__(kGeomThreads) tight_geom_kernel(const float4* 
   G.mode = -1;
   G.L = h;
   // membership margin: FP32 rounding of cell coordinates and distances
-  G.pad = 2e-5 + 4.0 * 1.1920929e-7 * (amax + 2.0 * margin);
+  // (extent: a periodic system's longest box edge, by which a point may be moved)
+  G.pad = 2e-5 + 4.0 * 1.1920929e-7 * (amax + 2.0 * margin + extent);
   G.total = 0;
   G.ncell = ncell;
   if (ncell > cell_cap) atomicOr(status, kStatusTableCells);
@@ -301,7 +302,10 @@ __global__ void __launch_bounds__(kSortWarps * kWarp) tight_sort_kernel(int* __r
 gbx_status launch_tight_build(Context* ctx, const float4* pos) {
   cudaStream_t st = ctx->stream;
   const double h = ctx->tight_h;
-  tight_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->n, h, ctx->cfg.switch_width, ctx->d_tgeom, ctx->tcell_cap,
+  const gbx_config& c = ctx->cfg;
+  const double extent = c.periodic ? fmax(c.box[0], fmax(c.box[1], c.box[2])) : 0.0;
+  if (c.periodic) launch_standalone_geom(ctx, pos, ctx->d_wgeom);
+  tight_geom_kernel<<<1, kGeomThreads, 0, st>>>(pos, ctx->n, h, c.switch_width, extent, ctx->d_tgeom, ctx->tcell_cap,
                                                 ctx->d_status);
   ++ctx->launches;
   const long long cells = ctx->tcell_cap;

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) integral_kernel(const float4* __rest
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   Work<COUNT> wk;
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) gbmv_integral_kernel(const float4* _
   const int g = lane / kGroup, r = lane % kGroup;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   float J4 = 0.0f, J7 = 0.0f;
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   __shared__ int s_long[kThreads / kWarp];  // a shaping entry beyond list position 63
   // the exact table: lists start at even entries and each cell's record sits
   // beside its first entry, so both are read 32 bytes at a time
-  constexpr bool kTight = std::is_same<Q, TightQuery>::value;
+  constexpr bool kTight = IsTight<Q>::value;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
   int4* region = EMIT ? sink.rec + (size_t)warp * sink.R : nullptr;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   float J4 = 0.0f, J7 = 0.0f;
   int head = 0, tail = 0;  // warp-uniform ring positions: taken, queued
@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(kThreads) chain_kernel(const float4* __restric
   // the record and the list-walk paths give the same bits
   long long fix = 0, fiy = 0, fiz = 0;
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int npts = rr.count ? rr.count[warp] : -1;
   if (MODEL == GBX_MODEL_GBSW && !ADJ && npts >= 0) {
     // recorded points, 32 at a time; lanes over their shaping entries
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(kThreads, 6) gbmv_chain_kernel(const float4* _
   const float4 xi = pos[i];
   const float2 de = dEdJ[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const size_t plane = (size_t)n * m.nq;
   long long fix = 0, fiy = 0, fiz = 0;
@@ -1048,8 +1048,9 @@ __global__ void __launch_bounds__(kThreads, 6) gbmv_chain_kernel(const float4* _
 
 Entries entries_of(const Context* ctx) {
   if (ctx->use_tight)
-    return Entries{ctx->d_tgeom, ctx->d_tcell,   ctx->d_tentry, nullptr, ctx->d_tindex, ctx->tcell_cap, ctx->d_tfirst,
-                   ctx->tentry_cap};
+    return Entries{ctx->d_tgeom,     ctx->d_tcell,   ctx->d_tentry,
+                   nullptr,          ctx->d_tindex,  ctx->tcell_cap,
+                   ctx->d_tfirst,    ctx->tentry_cap, ctx->cfg.periodic ? ctx->d_wgeom : nullptr};
   return Entries{ctx->d_geom,    ctx->d_cell2,    ctx->d_entry4, ctx->d_entry_par, ctx->d_entries, ctx->cell_cap,
                  nullptr,        ctx->entry_cap};
 }
@@ -1129,7 +1130,9 @@ gbx_status launch_status(Context* ctx, const char* what) {
 
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
   const ModelConst m = make_model_const(ctx);
-  if (ctx->use_tight) {
+  if (ctx->use_tight && ctx->cfg.periodic) {
+    launch_integrals_t<GBX_MODEL_GBSW, PeriodicTightQuery>(ctx, pos, m, count_work);
+  } else if (ctx->use_tight) {
     launch_integrals_t<GBX_MODEL_GBSW, TightQuery>(ctx, pos, m, count_work);
   } else if (ctx->cfg.periodic && ctx->cfg.table_mode == GBX_TABLE_STANDALONE) {
     launch_integrals_t<GBX_MODEL_GBSW, PeriodicQuery>(ctx, pos, m, count_work);
@@ -1151,7 +1154,10 @@ gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
 
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint) {
   const ModelConst m = make_model_const(ctx);
-  if (ctx->use_tight) {
+  if (ctx->use_tight && ctx->cfg.periodic) {
+    if (adjoint) launch_chain_t<GBX_MODEL_GBSW, PeriodicTightQuery, true>(ctx, pos, m, force, stride);
+    else launch_chain_t<GBX_MODEL_GBSW, PeriodicTightQuery, false>(ctx, pos, m, force, stride);
+  } else if (ctx->use_tight) {
     if (adjoint) launch_chain_t<GBX_MODEL_GBSW, TightQuery, true>(ctx, pos, m, force, stride);
     else launch_chain_t<GBX_MODEL_GBSW, TightQuery, false>(ctx, pos, m, force, stride);
   } else if (ctx->cfg.periodic && ctx->cfg.table_mode == GBX_TABLE_STANDALONE) {

@@ -28,6 +28,8 @@ struct Entries {
   const TightCell* first; // exact table: each cell's first list entry and record (else nullptr)
   long long entry_cap;    // entries allocated: a table with more was not sorted
                           // this step, its cell records are an earlier step's
+  const TableGeom* wrap;  // exact table of a periodic system: the reference's
+                          // standalone grid, whose edges decide a point's move
 };
 
 // Cells a query may index: none when the table outgrew either buffer this
@@ -81,6 +83,9 @@ struct RefQuery {
     }
     eps = 1e-4f + 64.0f * (float)dmax * 5.96e-8f;
   }
+  __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
+    init(*t.geom, xi, qo, usable_cells(t));
+  }
   __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
     if (off) return -1;
     const TableGeom& G = *g;
@@ -131,6 +136,9 @@ struct MinImageQuery : RefQuery {
       L[k] = (float)geom.box[k];
       iL[k] = (float)(1.0 / geom.box[k]);
     }
+  }
+  __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
+    init(*t.geom, xi, qo, usable_cells(t));
   }
   __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
     float d[3] = {(a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z};
@@ -185,6 +193,9 @@ struct PeriodicQuery {
     }
     eps = 1e-4f + 64.0f * (float)(dmax + wrap[0] + wrap[1] + wrap[2]) * 5.96e-8f;
   }
+  __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
+    init(*t.geom, xi, qo, usable_cells(t));
+  }
   __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
     if (off) return -1;
     const TableGeom& G = *g;
@@ -232,19 +243,127 @@ struct TightQuery {
     dims[1] = off ? 0 : g.dims[1];
     dims[2] = off ? 0 : g.dims[2];
   }
+  __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
+    init(*t.geom, xi, qo, usable_cells(t));
+  }
   // 32-bit arithmetic: the exact table holds fewer than 2^31 cells (checked
   // when it is sized); one unsigned compare per axis tests both bounds
-  __device__ __forceinline__ int cell(const float4, const float4 v, int) const {
-    const int cx = (int)floorf((xr[0] + v.x) * inv_h);
-    const int cy = (int)floorf((xr[1] + v.y) * inv_h);
-    const int cz = (int)floorf((xr[2] + v.z) * inv_h);
+  __device__ __forceinline__ int cell_at(float ox, float oy, float oz) const {
+    const int cx = (int)floorf((xr[0] + ox) * inv_h);
+    const int cy = (int)floorf((xr[1] + oy) * inv_h);
+    const int cz = (int)floorf((xr[2] + oz) * inv_h);
     if ((unsigned)cx >= (unsigned)dims[0] || (unsigned)cy >= (unsigned)dims[1] || (unsigned)cz >= (unsigned)dims[2])
       return -1;
     return (cx * dims[1] + cy) * dims[2] + cz;
   }
+  __device__ __forceinline__ int cell(const float4, const float4 v, int) const { return cell_at(v.x, v.y, v.z); }
   __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
     return make_float3((a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z);
   }
+};
+
+// The reference's move of a point off the standalone grid of a periodic
+// system (query_exact_wrap) in FP64, as shifts: false if the point misses.
+__device__ bool wrap_shift_exact(const TableGeom& g, const float4 xi, const double* qoff, int q, float sh[3]) {
+  const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
+  for (int k = 0; k < 3; ++k) {
+    double p = __dadd_rn(x[k], qoff[3 * q + k]);
+    double s = 0.0;
+    if (p < g.min[k]) {
+      p = __dadd_rn(p, g.box[k]);
+      s = g.box[k];
+    }
+    if (p > g.max[k]) {
+      p = __dsub_rn(p, g.box[k]);
+      s -= g.box[k];
+    }
+    if (p < g.min[k] || p > g.max[k]) return false;
+    sh[k] = (float)s;
+  }
+  return true;
+}
+
+// Exact GBSW table of a periodic system (CutoffPeriodic).  The reference
+// moves a point lying off its standalone grid by one box edge along each
+// axis, and reads the list of the cell the moved point p' falls in
+// (CharmmReferenceGBSW.cpp:522-535).  That list holds every atom within
+// reach of p', at distances below half a box edge (the table is only used
+// when the grid's pad plus a cell diagonal is below half the shortest edge),
+// so minimum-image distances are the distances to p' and V(p) is the exact
+// product at p'.  This query makes the reference's move (FP32 with the FP64
+// decision within a guard band of the grid's edges) and looks p' up in the
+// exact table; distances are by minimum image.
+struct PeriodicTightQuery : TightQuery {
+  float xw[3];    // x_i - the standalone grid's lower edge (nm)
+  float span[3];  // the standalone grid's extent (nm)
+  float L[3], iL[3];
+  float eps;
+  const TableGeom* wg;
+  const double* qoff;
+  __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
+    TightQuery::init(*t.geom, xi, qo, usable_cells(t));
+    const TableGeom& W = *t.wrap;
+    wg = t.wrap;
+    qoff = qo;
+    float ext = 0.0f;
+    const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
+    for (int k = 0; k < 3; ++k) {
+      xw[k] = (float)(x[k] - W.min[k]);
+      span[k] = (float)(W.max[k] - W.min[k]);
+      L[k] = (float)W.box[k];
+      iL[k] = (float)(1.0 / W.box[k]);
+      ext = fmaxf(ext, fabsf(xw[k]) + span[k] + L[k]);
+    }
+    // FP32 rounding of x_i - min + v (+- L), with room to spare
+    eps = 1e-5f + 16.0f * 1.1920929e-7f * (ext + 4.0f);
+  }
+  __device__ __forceinline__ int cell(const float4 xi, const float4 v, int q) const {
+    const float vv[3] = {v.x, v.y, v.z};
+    float sh[3];
+    bool safe = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float a = xw[k] + vv[k];
+      float s = 0.0f;
+      bool sk = fabsf(a) >= eps;
+      if (a < 0.0f) {
+        a += L[k];
+        s = L[k];
+      }
+      sk = sk && fabsf(a - span[k]) >= eps;
+      if (a > span[k]) {
+        a -= L[k];
+        s -= L[k];
+      }
+      sk = sk && fabsf(a) >= eps && fabsf(a - span[k]) >= eps;
+      if (sk && (a < 0.0f || a > span[k])) return -1;  // off the grid on this axis: a miss
+      safe = safe && sk;
+      sh[k] = s;
+    }
+    if (!safe && !wrap_shift_exact(*wg, xi, qoff, q, sh)) return -1;
+    return cell_at(v.x + sh[0], v.y + sh[1], v.z + sh[2]);
+  }
+  __device__ __forceinline__ float3 delta(const float4 a, const float4 xi, const float4 v) const {
+    float d[3] = {(a.x - xi.x) - v.x, (a.y - xi.y) - v.y, (a.z - xi.z) - v.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = fmaf(-L[k], floorf(fmaf(d[k], iL[k], 0.5f)), d[k]);
+    return make_float3(d[0], d[1], d[2]);
+  }
+};
+
+// The exact table's query types (cell records with the first entry, lists
+// in aligned pairs, buried cells).
+template <class Q>
+struct IsTight {
+  static constexpr bool value = false;
+};
+template <>
+struct IsTight<TightQuery> {
+  static constexpr bool value = true;
+};
+template <>
+struct IsTight<PeriodicTightQuery> {
+  static constexpr bool value = true;
 };
 
 // s = p / (1 + p) with p = exp(beta (S - lambda)): the solvent fraction

@@ -418,6 +418,52 @@ def test_cutoff_periodic_against_the_oracle_with_adjoint():
     ctx.close()
 
 
+def test_cutoff_periodic_exact_table_matches_reference_table():
+    """CutoffPeriodic GBSW on the exact table (points off the standalone grid
+    moved by a box edge as the reference moves them, then looked up in the
+    exact table) against the same system on the reference's standalone
+    table: the same volumes, hence energy, forces and Born radii to FP32
+    rounding, with a fraction of the list work.  A box too narrow for the
+    standalone grid's reach keeps the reference table (identical bits)."""
+    g = make_globule(1000, seed=17)
+    pos = g.positions - g.positions.min(axis=0)
+    m = GBModel.charmm_gbsw(n_radial=24, lebedev=50, cutoff=1.5, periodic=True, box=(3.2, 3.2, 3.3))
+    a = Context(m, g.n)
+    b = Context(m.replace(reference_table=True), g.n)
+    for c in (a, b):
+        c.set_particle_parameters(g.charge, g.radius)
+    Ea, Fa = a.execute_host(pos)
+    Eb, Fb = b.execute_host(pos)
+    assert abs(Ea / Eb - 1) < 1e-6
+    assert rel_rms(Fa, Fb) < 1e-5
+    assert np.abs(a.born_radii() / b.born_radii() - 1).max() < 1e-5
+    a.execute_host(pos, count_work=True)
+    b.execute_host(pos, count_work=True)
+    assert a.work()["volume_evals"] < 0.5 * b.work()["volume_evals"]
+    # the oracle (reference semantics) on the same input
+    ref = O.Oracle(m).energy_forces(pos, g.charge, g.radius)
+    assert abs(Ea / ref["energy"] - 1) < 2e-5 and rel_rms(Fa, ref["forces"]) < 1e-4
+    for c in (a, b):
+        c.close()
+
+    # half of a 1.6 nm edge is below the standalone grid's reach: the
+    # reference table serves the exact-table policy too
+    small = make_globule(120, seed=5)
+    sp = small.positions - small.positions.min(axis=0)
+    ms = GBModel.charmm_gbsw(cutoff=0.8, periodic=True, box=(1.6, 1.6, 1.6))
+    a = Context(ms, small.n)
+    b = Context(ms.replace(reference_table=True), small.n)
+    for c in (a, b):
+        c.set_particle_parameters(small.charge, small.radius)
+    Ea, Fa = a.execute_host(sp)
+    Eb, Fb = b.execute_host(sp)
+    assert Ea == Eb and np.array_equal(Fa, Fb)
+    ref = O.Oracle(ms).energy_forces(sp, small.charge, small.radius)
+    assert abs(Ea / ref["energy"] - 1) < 2e-5 and rel_rms(Fa, ref["forces"]) < 1e-4
+    for c in (a, b):
+        c.close()
+
+
 @pytest.mark.parametrize("itype", ["gbsw", "gbmv1", "gbmv2"])
 def test_gbmv_force_cutoff_periodic_against_the_oracle(itype):
     """A CharmmGBMVForce with CutoffPeriodic through the kernel mirror: the
@@ -447,3 +493,26 @@ def test_gbmv_force_cutoff_periodic_against_the_oracle(itype):
     flat = O.Oracle(m.replace(periodic=False, cutoff=0.0)).energy_forces(pos, g.charge, g.radius)
     assert abs(flat["energy"] / ref["energy"] - 1) > 1e-3
 
+
+
+def test_surface_area_energy_is_stored_and_unused(glob1000):
+    """CharmmGBSWForce's surface-area energy (CharmmGBSWForce.h:144-152,
+    default 2.25936 from CharmmGBSWForce.cpp:40) is a stored value that no
+    reference kernel reads: setting it changes neither energy nor forces."""
+    from openmmcustomgbintegralforce_gb300 import api
+
+    g = glob1000
+    out = []
+    for sa in (None, 0.0, 10.0):
+        f = api.CharmmGBSWForce()
+        assert f.getSurfaceAreaEnergy() == 2.25936
+        if sa is not None:
+            f.setSurfaceAreaEnergy(sa)
+            assert f.getSurfaceAreaEnergy() == sa
+        for i in range(g.n):
+            f.addParticle(g.charge[i], g.radius[i], 1.0)
+        k = api.CalcCharmmGBSWForceKernel()
+        k.initialize(g.n, f)
+        out.append(k.execute(g.positions))
+    for E, F in out[1:]:
+        assert E == out[0][0] and np.array_equal(F, out[0][1])
