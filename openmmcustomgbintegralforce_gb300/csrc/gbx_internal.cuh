@@ -42,6 +42,8 @@ struct TableGeom {
   double max[3];
   double step[3];
   double box[3];
+  double inv_step[3];  // 1 / step and 1 / box (0 without a box), for the FP32
+  double inv_box[3];   // queries: formed once here, not per lane in FP64
   double pad;       // standalone uniform pad
   double L;         // periodic: max(step)
   int dims[3];

@@ -80,8 +80,15 @@ struct Image {
     if (PER)
       for (int k = 0; k < 3; ++k) {
         L[k] = (float)g.box[k];
-        iL[k] = (float)(1.0 / g.box[k]);
+        iL[k] = (float)g.inv_box[k];
       }
+  }
+  __device__ __forceinline__ void apply2(float2& dx, float2& dy, float2& dz) const {
+    if (PER) {
+      dx = make_float2(fmaf(-L[0], floorf(fmaf(dx.x, iL[0], 0.5f)), dx.x), fmaf(-L[0], floorf(fmaf(dx.y, iL[0], 0.5f)), dx.y));
+      dy = make_float2(fmaf(-L[1], floorf(fmaf(dy.x, iL[1], 0.5f)), dy.x), fmaf(-L[1], floorf(fmaf(dy.y, iL[1], 0.5f)), dy.y));
+      dz = make_float2(fmaf(-L[2], floorf(fmaf(dz.x, iL[2], 0.5f)), dz.x), fmaf(-L[2], floorf(fmaf(dz.y, iL[2], 0.5f)), dz.y));
+    }
   }
   __device__ __forceinline__ float3 apply(float3 d) const {
     if (PER) {
@@ -114,39 +121,61 @@ template <int MODEL, class Q>
 __global__ void __launch_bounds__(kBinThreads) gbmv_bin_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                                Quad quad, ModelConst m, int chunk, int n_chunks,
                                                                CellPoints cp) {
+  // kBinBatch points per lane per step: their cell queries, list-count loads
+  // and slot atomics are issued back to back, so each warp keeps several
+  // atomics in flight instead of waiting out one round trip per point
+  constexpr int kBinBatch = 4;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   if (warp >= n * n_chunks) return;
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   Q query;
-  query.init(*tab.geom, xi, quad.qoff, usable_cells(tab));
+  query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
   const unsigned lt = (1u << lane) - 1u;
-  for (int base = q0; base < q1; base += kWarp) {
-    const int q = base + lane;
-    const bool valid = q < q1;
-    long long cell = -1;
-    int cnt = 0;
-    if (valid) {
-      cell = query.cell(xi, quad.qv[q], q);
-      if (cell >= 0) cnt = __ldg(&tab.cell[cell].x);
+  for (int base = q0; base < q1; base += kBinBatch * kWarp) {
+    long long cell[kBinBatch];
+    int cnt[kBinBatch];
+#pragma unroll
+    for (int u = 0; u < kBinBatch; ++u) {
+      const int q = base + u * kWarp + lane;
+      cell[u] = -1;
+      cnt[u] = 0;
+      if (q < q1) cell[u] = query.cell(xi, quad.qv[q], q);
     }
-    const bool listed = valid && cell >= 0 && cnt > 0;
-    const unsigned lm = __ballot_sync(0xffffffffu, listed);
-    const size_t p = (size_t)i * m.nq + q;
-    if (listed) {
-      // one atomic per distinct cell among the warp's points
-      const unsigned peers = __match_any_sync(lm, (int)cell);
-      const int leader = __ffs(peers) - 1;
-      int r0 = 0;
-      if (lane == leader) r0 = atomicAdd(&cp.count[cell], __popc(peers));
-      r0 = __shfl_sync(peers, r0, leader);
-      cp.cell[p] = (int)cell;
-      cp.rank[p] = r0 + __popc(peers & lt);
-    } else if (valid) {
-      cp.cell[p] = -1;
-      cp.sval[p] = empty_list_fraction<MODEL>(m);
+#pragma unroll
+    for (int u = 0; u < kBinBatch; ++u)
+      if (cell[u] >= 0) cnt[u] = __ldg(&tab.cell[cell[u]].x);
+    int r0[kBinBatch];
+    unsigned peers[kBinBatch];
+#pragma unroll
+    for (int u = 0; u < kBinBatch; ++u) {
+      const bool listed = cell[u] >= 0 && cnt[u] > 0;
+      const unsigned lm = __ballot_sync(0xffffffffu, listed);
+      r0[u] = 0;
+      peers[u] = 0u;
+      if (listed) {
+        // one atomic per distinct cell among the warp's points
+        peers[u] = __match_any_sync(lm, (int)cell[u]);
+        if (lane == __ffs(peers[u]) - 1) r0[u] = atomicAdd(&cp.count[cell[u]], __popc(peers[u]));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kBinBatch; ++u) {
+      const int q = base + u * kWarp + lane;
+      const bool listed = cell[u] >= 0 && cnt[u] > 0;
+      // every lane takes part in the shuffle; a lane without a cell reads its own value
+      const int src = listed ? __ffs(peers[u]) - 1 : lane;
+      const int rr = __shfl_sync(0xffffffffu, r0[u], src);
+      const size_t p = (size_t)i * m.nq + q;
+      if (listed) {
+        cp.cell[p] = (int)cell[u];
+        cp.rank[p] = rr + __popc(peers[u] & lt);
+      } else if (q < q1) {
+        cp.cell[p] = -1;
+        cp.sval[p] = empty_list_fraction<MODEL>(m);
+      }
     }
   }
 }
@@ -223,11 +252,61 @@ __device__ __noinline__ void sort_cell(int* order, int P, int lane) {
   else if (P <= kSortMax) sort_slots<16>(order, P, lane);
 }
 
+// Hardware reciprocal (PTX rcp.approx, relative error below 2^-22; the
+// denominators here are >= 1 in magnitude, never subnormal).
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 rcp2(float2 t) { return make_float2(rcp_ftz(t.x), rcp_ftz(t.y)); }
+
+// The cell's list staged in shared memory, one array per field, so that two
+// consecutive entries load as one float2 and feed packed FP32x2 arithmetic
+// (__ffma2_rn and friends: one instruction for two entries, each half
+// rounded as its scalar form).  A list of odd length is padded with one
+// entry whose every contribution is exactly zero (C = 0 for GBMV-II,
+// gamma = 0 for GBMV-I's chain; T = 100 r^2 + 1 >= 1), index -1.
+struct __align__(16) CellList {
+  float x[kMaxList], y[kMaxList], z[kMaxList];  // x_j - c0
+  float w[kMaxList];    // GBMV-II C_j | GBMV-I gamma_j
+  float k[kMaxList];    // GBMV-II C_j - 100 R_j^2 | GBMV-I R_j
+  float r[kMaxList];    // GBMV-II R_j
+  int idx[kMaxList];    // atom index
+};
+
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ int2 ld2i(const int* p) { return *reinterpret_cast<const int2*>(p); }
+
+template <bool PER>
+__device__ __forceinline__ void stage_list(CellList& L, const Entries& tab, int2 cs, int cnt, float3 c0, int lane) {
+  const int cnt2 = (cnt + 1) & ~1;
+  for (int l = lane; l < cnt2; l += kWarp) {
+    if (l < cnt) {
+      const float4 a = __ldg(tab.e + cs.y + l);
+      const float2 pk = __ldg(tab.par + cs.y + l);
+      L.x[l] = a.x - c0.x;
+      L.y[l] = a.y - c0.y;
+      L.z[l] = a.z - c0.z;
+      L.w[l] = a.w;
+      L.k[l] = pk.x;
+      L.r[l] = pk.y;
+      L.idx[l] = __ldg(tab.index + cs.y + l);
+    } else {
+      L.x[l] = L.y[l] = L.z[l] = 0.0f;
+      L.w[l] = 0.0f;
+      L.k[l] = 1.0f;
+      L.r[l] = 1.0f;
+      L.idx[l] = -1;
+    }
+  }
+}
+
 template <int MODEL, bool PER>
 __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const float4* __restrict__ pos, Entries tab,
                                                                           Quad quad, ModelConst m, CellPoints cp) {
-  __shared__ float4 s_e[kCellWarps][kMaxList];
-  __shared__ float s_k[kCellWarps][kMaxList];
+  __shared__ CellList s_list[kCellWarps];
   const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   const long long cell = (long long)blockIdx.x * kCellWarps + w;
   const TableGeom& G = *tab.geom;
@@ -239,17 +318,15 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
   const float3 c0 = cell_corner(G, (int)cell);
   Image<PER> img;
   img.init(G);
-  for (int l = lane; l < cnt; l += kWarp) {
-    const float4 a = __ldg(tab.e + cs.y + l);
-    s_e[w][l] = make_float4(a.x - c0.x, a.y - c0.y, a.z - c0.z, a.w);
-    if (MODEL == GBX_MODEL_GBMV2) s_k[w][l] = __ldg(&tab.par[cs.y + l].x);
-  }
+  CellList& L = s_list[w];
+  stage_list<PER>(L, tab, cs, cnt, c0, lane);
   const int start = cp.start[cell];
   int* order = cp.order + start;
   if (P > 1) sort_cell(order, P, lane);
   __syncwarp();
-  const float4* E = s_e[w];
-  const float* K = s_k[w];
+  // GBMV-II's padding entry adds exactly zero; GBMV-I's (e^0 = 1) does not,
+  // so its odd entry is taken on its own
+  const int npair = MODEL == GBX_MODEL_GBMV2 ? (cnt + 1) >> 1 : cnt >> 1;
   for (int base = 0; base < P; base += kWarp) {
     const int k = base + lane;
     const bool valid = k < P;
@@ -257,22 +334,34 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
     const int i = p / m.nq, q = p - i * m.nq;
     const float4 xi = __ldg(pos + i), v = __ldg(quad.qv + q);
     const float px = (xi.x - c0.x) + v.x, py = (xi.y - c0.y) + v.y, pz = (xi.z - c0.z) + v.z;
-    Sums s{0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int l = 0; l < cnt; ++l) {
-      const float4 a = E[l];
-      const float3 d = img.apply(make_float3(a.x - px, a.y - py, a.z - pz));
-      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+    const float2 npx = bc2(-px), npy = bc2(-py), npz = bc2(-pz);
+    float2 s1 = bc2(0.f), s2 = bc2(0.f), vx = bc2(0.f), vy = bc2(0.f), vz = bc2(0.f);
+    for (int j = 0; j < npair; ++j) {
+      const int l = 2 * j;
+      float2 dx = __fadd2_rn(ld2(L.x + l), npx), dy = __fadd2_rn(ld2(L.y + l), npy),
+             dz = __fadd2_rn(ld2(L.z + l), npz);
+      img.apply2(dx, dy, dz);
+      const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
       if (MODEL == GBX_MODEL_GBMV1) {
-        s.s1 += __expf(a.w * (r2 * r2));
+        const float2 g = __fmul2_rn(ld2(L.w + l), __fmul2_rn(r2, r2));
+        s1 = __fadd2_rn(s1, make_float2(__expf(g.x), __expf(g.y)));
       } else {
-        float F = __fdividef(a.w, fmaf(100.0f, r2, K[l]));
-        F = F * F;
-        s.s1 += F;
-        s.s2 = fmaf(r2, F * F, s.s2);
-        s.vx = fmaf(d.x, F, s.vx);
-        s.vy = fmaf(d.y, F, s.vy);
-        s.vz = fmaf(d.z, F, s.vz);
+        const float2 T = __ffma2_rn(bc2(100.0f), r2, ld2(L.k + l));
+        float2 F = __fmul2_rn(ld2(L.w + l), rcp2(T));
+        F = __fmul2_rn(F, F);
+        s1 = __fadd2_rn(s1, F);
+        s2 = __ffma2_rn(r2, __fmul2_rn(F, F), s2);
+        vx = __ffma2_rn(dx, F, vx);
+        vy = __ffma2_rn(dy, F, vy);
+        vz = __ffma2_rn(dz, F, vz);
       }
+    }
+    Sums s{s1.x + s1.y, s2.x + s2.y, vx.x + vx.y, vy.x + vy.y, vz.x + vz.y};
+    if (MODEL == GBX_MODEL_GBMV1 && (cnt & 1)) {
+      const int l = cnt - 1;
+      const float3 d = img.apply(make_float3(L.x[l] - px, L.y[l] - py, L.z[l] - pz));
+      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      s.s1 += __expf(L.w[l] * (r2 * r2));
     }
     if (valid) {
       float pl, S;
@@ -335,15 +424,10 @@ __device__ __forceinline__ void add_fixed3(const CellChainOut& o, int k, float g
   if (fz) atomicAdd(&o.force[k + 2 * o.stride], (unsigned long long)fz);
 }
 
-// dE/dR_k of one contribution: kept in the entry's register sum, or (cells
-// too dense to sort) reduced on its own.
-__device__ __forceinline__ void add_dEdR(const CellChainOut& o, int k, bool sorted, float& acc, float v) {
-  if (sorted) {
-    acc += v;
-  } else {
-    const long long r = float_to_fixed(v);
-    if (r) atomicAdd(&o.dEdR[k], (unsigned long long)r);
-  }
+// One fixed-point reduction (skipped when the value rounds to zero).
+__device__ __forceinline__ void add_fixed_one(unsigned long long* a, int k, float v) {
+  const long long r = float_to_fixed(v);
+  if (r) atomicAdd(&a[k], (unsigned long long)r);
 }
 
 // One point's chain-rule factors (the point's own lanes read them from
@@ -355,8 +439,11 @@ __device__ __forceinline__ void add_dEdR(const CellChainOut& o, int k, bool sort
 // C = -2 c ds/dS s0 s1 s2 / |v|^4 (the d s1, d s2 and d |v|^2 factors) and
 // Cv = C v.  GBMV-I: g_j = A e_j r_j^2 d_j with A = 4 c ds/dS gamma_j
 // folded per entry.
-struct PointChain {
-  float px, py, pz, cS, A, B, C, vx, vy, vz, cvx, cvy, cvz;
+struct __align__(16) PointChain {
+  float2 npx, npy, npz;  // minus the point's position in the cell frame, in both halves
+  float2 A, B, C;        // GBMV-I: A only
+  float2 vx, vy, vz, cvx, cvy, cvz;
+  float cS;
   int i;
 };
 
@@ -365,8 +452,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
                                                                        Quad quad, ModelConst m, CellPoints cp,
                                                                        const float2* __restrict__ dEdJ,
                                                                        CellChainOut out) {
-  __shared__ float4 s_e[kCellWarps][kMaxList];
-  __shared__ float4 s_par[kCellWarps][kMaxList];  // (GBMV-II K | GBMV-I R, R, atom index, -)
+  __shared__ CellList s_list[kCellWarps];
   __shared__ PointChain s_pt[kCellWarps][kWarp];
   __shared__ float3 s_own[kCellWarps][kWarp];
   const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
@@ -380,27 +466,27 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
   const float3 c0 = cell_corner(G, (int)cell);
   Image<PER> img;
   img.init(G);
-  for (int l = lane; l < cnt; l += kWarp) {
-    const float4 a = __ldg(tab.e + cs.y + l);
-    s_e[w][l] = make_float4(a.x - c0.x, a.y - c0.y, a.z - c0.z, a.w);
-    const float2 pk = __ldg(tab.par + cs.y + l);
-    s_par[w][l] = make_float4(pk.x, pk.y, __int_as_float(__ldg(tab.index + cs.y + l)), 0.0f);
-  }
+  CellList& L = s_list[w];
+  stage_list<PER>(L, tab, cs, cnt, c0, lane);
   const int start = cp.start[cell];
   const int* order = cp.order + start;
   const float* state = cp.state + start;
   // cells too dense to sort keep the atomic slot order: every contribution
   // is then reduced on its own (integer sums, independent of the order)
   const bool sorted = P <= kSortMax;
+  // lane (ps, es): point ps of each group of kChainPts, entry pairs es, es +
+  // kChainEnt, ... (entries 2 j and 2 j + 1 of pair j)
   const int ps = lane / kChainEnt, es = lane % kChainEnt;
-  float acc[kEntPerLane][3];
-  float accR[kEntPerLane];
+  constexpr int kPairsPerLane = kEntPerLane / 2;
+  float2 acc[kPairsPerLane][3];
+  float2 accR[kPairsPerLane];
 #pragma unroll
-  for (int e = 0; e < kEntPerLane; ++e) {
-    acc[e][0] = acc[e][1] = acc[e][2] = 0.0f;
-    accR[e] = 0.0f;
+  for (int e = 0; e < kPairsPerLane; ++e) {
+    acc[e][0] = acc[e][1] = acc[e][2] = bc2(0.f);
+    accR[e] = bc2(0.f);
   }
   PointChain* pts = s_pt[w];
+  const float Cp = 10.0f * m.p1;
   for (int base = 0; base < P; base += kWarp) {
     // lane t prepares point base + t
     {
@@ -408,7 +494,8 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
       PointChain pc;
       pc.cS = 0.0f;
       pc.i = -1;
-      pc.px = pc.py = pc.pz = pc.A = pc.B = pc.C = pc.vx = pc.vy = pc.vz = pc.cvx = pc.cvy = pc.cvz = 0.0f;
+      pc.npx = pc.npy = pc.npz = pc.A = pc.B = pc.C = bc2(0.f);
+      pc.vx = pc.vy = pc.vz = pc.cvx = pc.cvy = pc.cvz = bc2(0.f);
       if (k < P) {
         const int p = order[k];
         const int i = p / m.nq, q = p - i * m.nq;
@@ -417,14 +504,14 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
         const float2 de = __ldg(dEdJ + i);
         const float cq = fmaf(de.x, wq.x, de.y * wq.y);
         pc.i = i;
-        pc.px = (xi.x - c0.x) + v.x;
-        pc.py = (xi.y - c0.y) + v.y;
-        pc.pz = (xi.z - c0.z) + v.z;
+        pc.npx = bc2(-((xi.x - c0.x) + v.x));
+        pc.npy = bc2(-((xi.y - c0.y) + v.y));
+        pc.npz = bc2(-((xi.z - c0.z) + v.z));
         float pl;
         if (MODEL == GBX_MODEL_GBMV1) {
           logistic_solvent(m.beta, m.lambda, state[k], pl);
           pc.cS = cq * __fdividef(m.beta * pl, (1.0f + pl) * (1.0f + pl));
-          pc.A = 4.0f * pc.cS;
+          pc.A = bc2(4.0f * pc.cS);
         } else {
           const float s1 = state[k], s2 = state[k + cp.plane], vx = state[k + 2 * cp.plane],
                       vy = state[k + 3 * cp.plane], vz = state[k + 4 * cp.plane];
@@ -432,15 +519,17 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
           logistic_solvent(m.beta, m.lambda, m.s0 * s1 * s2 / s3sq, pl);
           pc.cS = cq * __fdividef(m.beta * pl, (1.0f + pl) * (1.0f + pl)) * m.s0;
           const float inv3 = 1.0f / s3sq;
-          pc.A = pc.cS * (s2 * inv3);
-          pc.B = 2.0f * pc.cS * (s1 * inv3);
-          pc.C = 2.0f * pc.cS * (-s1 * s2 * inv3 * inv3);
-          pc.vx = vx;
-          pc.vy = vy;
-          pc.vz = vz;
-          pc.cvx = pc.C * vx;
-          pc.cvy = pc.C * vy;
-          pc.cvz = pc.C * vz;
+          const float A = pc.cS * (s2 * inv3), B = 2.0f * pc.cS * (s1 * inv3),
+                      C = 2.0f * pc.cS * (-s1 * s2 * inv3 * inv3);
+          pc.A = bc2(A);
+          pc.B = bc2(B);
+          pc.C = bc2(C);
+          pc.vx = bc2(vx);
+          pc.vy = bc2(vy);
+          pc.vz = bc2(vz);
+          pc.cvx = bc2(C * vx);
+          pc.cvy = bc2(C * vy);
+          pc.cvz = bc2(C * vz);
         }
       }
       pts[lane] = pc;
@@ -449,70 +538,99 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
     const int np = min(kWarp, P - base);
     for (int sub = 0; sub < np; sub += kChainPts) {
       const int t = sub + ps;
-      const PointChain pc = pts[t < np ? t : 0];
+      const PointChain& pc = pts[t < np ? t : 0];
       const bool live = t < np && pc.cS != 0.0f;
-      float ox = 0.f, oy = 0.f, oz = 0.f;
+      float2 ox = bc2(0.f), oy = bc2(0.f), oz = bc2(0.f);
       if (live) {
+        const int pi = pc.i;
 #pragma unroll
-        for (int e = 0; e < kEntPerLane; ++e) {
-          const int l = es + e * kChainEnt;
+        for (int e = 0; e < kPairsPerLane; ++e) {
+          const int l = 2 * (es + e * kChainEnt);
           if (l < cnt) {
-            const float4 a = s_e[w][l];
-            const float4 pk = s_par[w][l];
-            const int kj = __float_as_int(pk.z);
-            const float3 d = img.apply(make_float3(a.x - pc.px, a.y - pc.py, a.z - pc.pz));
-            const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-            float gx, gy, gz;
+            float2 dx = __fadd2_rn(ld2(L.x + l), pc.npx), dy = __fadd2_rn(ld2(L.y + l), pc.npy),
+                   dz = __fadd2_rn(ld2(L.z + l), pc.npz);
+            img.apply2(dx, dy, dz);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            const float2 aw = ld2(L.w + l);
+            const int2 kj = ld2i(L.idx + l);
+            // atom i's own entry moves with the point: no force from it
+            const float2 own = make_float2(kj.x != pi ? 1.0f : 0.0f, kj.y != pi ? 1.0f : 0.0f);
+            float2 gx, gy, gz;
             if (MODEL == GBX_MODEL_GBMV1) {
-              const float r4 = r2 * r2;
-              const float ex = __expf(a.w * r4);
-              if (ADJ) add_dEdR(out, kj, sorted, accR[e], pc.cS * ex * r4 * (-4.0f * a.w / pk.x));
-              const float gs = pc.A * a.w * ex * r2;  // dS/d(delta) = 4 gamma e r^2 delta
-              gx = gs * d.x;
-              gy = gs * d.y;
-              gz = gs * d.z;
-            } else {
-              const float T = fmaf(100.0f, r2, pk.x);
-              const float rT = __fdividef(1.0f, T);
-              const float CT = a.w * rT;
-              const float F = CT * CT;
-              const float u = F * rT;  // dF/d(delta) = -400 u delta
-              const float vd = fmaf(pc.vx, d.x, fmaf(pc.vy, d.y, pc.vz * d.z));
+              const float2 r4 = __fmul2_rn(r2, r2);
+              const float2 g = __fmul2_rn(aw, r4);
+              const float2 ex = make_float2(__expf(g.x), __expf(g.y));
               if (ADJ) {
-                const float R = pk.y;
-                const float Cp = 10.0f * m.p1, Tp = Cp - 200.0f * R;
-                const float dFdR = 2.0f * CT * __fdividef(Cp * T - a.w * Tp, T * T);
-                // c ds/dS (s2 dF + s1 d(r^2 F^2) + d|v|^2) / |v|^2 terms, as pc.A, pc.B, pc.C carry them
-                add_dEdR(out, kj, sorted, accR[e], dFdR * (pc.A + pc.B * (r2 * F) + pc.C * vd));
+                // dS/dR_j = -4 gamma_j e_j r^4 / R_j (gamma ~ R^-4); padding: gamma = 0
+                const float2 R = ld2(L.k + l);
+                const float2 dr = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(pc.cS), ex), r4),
+                                             make_float2(-4.0f * aw.x / R.x, -4.0f * aw.y / R.y));
+                accR[e] = __fadd2_rn(accR[e], dr);
+                if (!sorted) {
+                  if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
+                  if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
+                }
               }
-              const float sc = -400.0f * u * fmaf(pc.C, vd, pc.A) + pc.B * F * fmaf(-400.0f * u, r2, F);
-              gx = fmaf(sc, d.x, F * pc.cvx);
-              gy = fmaf(sc, d.y, F * pc.cvy);
-              gz = fmaf(sc, d.z, F * pc.cvz);
-            }
-            if (kj != pc.i) {  // atom i's own entry moves with the point: no force
-              if (sorted) {
-                acc[e][0] += gx;
-                acc[e][1] += gy;
-                acc[e][2] += gz;
-              } else {
-                add_fixed3(out, kj, -gx, -gy, -gz);
+              // dS/d(delta) = 4 gamma e r^2 delta
+              const float2 gs = __fmul2_rn(__fmul2_rn(__fmul2_rn(__fmul2_rn(pc.A, aw), ex), r2), own);
+              gx = __fmul2_rn(gs, dx);
+              gy = __fmul2_rn(gs, dy);
+              gz = __fmul2_rn(gs, dz);
+            } else {
+              const float2 T = __ffma2_rn(bc2(100.0f), r2, ld2(L.k + l));
+              const float2 rT = rcp2(T);
+              const float2 CT = __fmul2_rn(aw, rT);
+              const float2 F = __fmul2_rn(CT, CT);
+              const float2 u = __fmul2_rn(F, rT);  // dF/d(delta) = -400 u delta
+              const float2 vd = __ffma2_rn(pc.vx, dx, __ffma2_rn(pc.vy, dy, __fmul2_rn(pc.vz, dz)));
+              if (ADJ) {
+                // dF/dR_j with T = C_j + 100 (r^2 - R_j^2), C_j = 10 p1 R_j + p2 (nm -> A):
+                // c ds/dS (s2 dF + s1 d(r^2 F^2) + d|v|^2) / |v|^2 as pc.A, pc.B, pc.C carry them
+                const float2 R = ld2(L.r + l);
+                const float2 Tp = __ffma2_rn(bc2(-200.0f), R, bc2(Cp));
+                const float2 num = __ffma2_rn(bc2(Cp), T, __fmul2_rn(make_float2(-aw.x, -aw.y), Tp));
+                const float2 dFdR = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(2.0f), CT), num), __fmul2_rn(rT, rT));
+                const float2 fac = __ffma2_rn(pc.C, vd, __ffma2_rn(pc.B, __fmul2_rn(r2, F), pc.A));
+                const float2 dr = __fmul2_rn(dFdR, fac);
+                accR[e] = __fadd2_rn(accR[e], dr);
+                if (!sorted) {
+                  if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
+                  if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
+                }
               }
-              ox += gx;
-              oy += gy;
-              oz += gz;
+              // g = [-400 u (A + C vd) + B F (F - 400 u r^2)] delta + F C v
+              const float2 m400u = __fmul2_rn(bc2(-400.0f), u);
+              const float2 sc = __fmul2_rn(
+                  __ffma2_rn(m400u, __ffma2_rn(pc.C, vd, pc.A), __fmul2_rn(__fmul2_rn(pc.B, F), __ffma2_rn(m400u, r2, F))),
+                  own);
+              const float2 Fo = __fmul2_rn(F, own);
+              gx = __ffma2_rn(sc, dx, __fmul2_rn(Fo, pc.cvx));
+              gy = __ffma2_rn(sc, dy, __fmul2_rn(Fo, pc.cvy));
+              gz = __ffma2_rn(sc, dz, __fmul2_rn(Fo, pc.cvz));
             }
+            if (sorted) {
+              acc[e][0] = __fadd2_rn(acc[e][0], gx);
+              acc[e][1] = __fadd2_rn(acc[e][1], gy);
+              acc[e][2] = __fadd2_rn(acc[e][2], gz);
+            } else {
+              if (l < cnt && kj.x != pi) add_fixed3(out, kj.x, -gx.x, -gy.x, -gz.x);
+              if (l + 1 < cnt && kj.y != pi) add_fixed3(out, kj.y, -gx.y, -gy.y, -gz.y);
+            }
+            ox = __fadd2_rn(ox, gx);
+            oy = __fadd2_rn(oy, gy);
+            oz = __fadd2_rn(oz, gz);
           }
         }
       }
       // the point's own pull, summed over its entry lanes
+      float px_ = ox.x + ox.y, py_ = oy.x + oy.y, pz_ = oz.x + oz.y;
 #pragma unroll
       for (int off = 1; off < kChainEnt; off <<= 1) {
-        ox += __shfl_xor_sync(0xffffffffu, ox, off);
-        oy += __shfl_xor_sync(0xffffffffu, oy, off);
-        oz += __shfl_xor_sync(0xffffffffu, oz, off);
+        px_ += __shfl_xor_sync(0xffffffffu, px_, off);
+        py_ += __shfl_xor_sync(0xffffffffu, py_, off);
+        pz_ += __shfl_xor_sync(0xffffffffu, pz_, off);
       }
-      if (es == 0 && t < np) s_own[w][t] = make_float3(ox, oy, oz);
+      if (es == 0 && t < np) s_own[w][t] = make_float3(px_, py_, pz_);
     }
     __syncwarp();
     // owner forces of these points: runs of one atom summed, one reduction per run
@@ -540,24 +658,31 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
     }
     __syncwarp();
   }
+  if (!sorted) return;
   // the entries' pull over all of the cell's points: summed over the point
   // lanes, one fixed-point reduction per entry
 #pragma unroll
-  for (int e = 0; e < kEntPerLane; ++e) {
+  for (int e = 0; e < kPairsPerLane; ++e) {
 #pragma unroll
     for (int off = kChainEnt; off < kWarp; off <<= 1) {
-      acc[e][0] += __shfl_xor_sync(0xffffffffu, acc[e][0], off);
-      acc[e][1] += __shfl_xor_sync(0xffffffffu, acc[e][1], off);
-      acc[e][2] += __shfl_xor_sync(0xffffffffu, acc[e][2], off);
-      if (ADJ) accR[e] += __shfl_xor_sync(0xffffffffu, accR[e], off);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        acc[e][c].x += __shfl_xor_sync(0xffffffffu, acc[e][c].x, off);
+        acc[e][c].y += __shfl_xor_sync(0xffffffffu, acc[e][c].y, off);
+      }
+      if (ADJ) {
+        accR[e].x += __shfl_xor_sync(0xffffffffu, accR[e].x, off);
+        accR[e].y += __shfl_xor_sync(0xffffffffu, accR[e].y, off);
+      }
     }
-    const int l = es + e * kChainEnt;
-    if (ps == 0 && l < cnt) {
-      const int kj = __float_as_int(s_par[w][l].z);
-      if (sorted) add_fixed3(out, kj, -acc[e][0], -acc[e][1], -acc[e][2]);
-      if (ADJ && sorted) {
-        const long long r = float_to_fixed(accR[e]);
-        if (r) atomicAdd(&out.dEdR[kj], (unsigned long long)r);
+    const int l = 2 * (es + e * kChainEnt);
+    if (ps == 0) {
+      for (int h = 0; h < 2; ++h) {
+        if (l + h >= cnt) break;
+        const int kj = L.idx[l + h];
+        add_fixed3(out, kj, h ? -acc[e][0].y : -acc[e][0].x, h ? -acc[e][1].y : -acc[e][1].x,
+                   h ? -acc[e][2].y : -acc[e][2].x);
+        if (ADJ) add_fixed_one(out.dEdR, kj, h ? accR[e].y : accR[e].x);
       }
     }
   }

@@ -184,6 +184,10 @@ __global__ void __launch_bounds__(kGeomThreads) table_geom_kernel(const GeomPart
     G.L = L;
     G.pad = 0.0;
   }
+  for (int k = 0; k < 3; ++k) {
+    G.inv_step[k] = 1.0 / G.step[k];
+    G.inv_box[k] = G.box[k] > 0.0 ? 1.0 / G.box[k] : 0.0;
+  }
   G.ncell = ncell;
   if (ncell > cell_cap) atomicOr(status, kStatusTableCells);
   *g = G;
@@ -261,16 +265,20 @@ __global__ void table_members_grid_kernel(const float4* __restrict__ pos, const 
 }
 
 // CustomGBIntegral.cpp:117-159 (PERIODIC): samples at the grid step, accumulated
-// by repeated addition exactly as the reference's for-loops do.
+// by repeated addition exactly as the reference's for-loops do.  The cell
+// index of a sample and the membership test are decided in FP32 wherever the
+// FP32 value is clear of the decision's boundary by a margin that covers its
+// rounding, and in the reference's FP64 operations otherwise (FP64 runs at a
+// small fraction of the FP32 rate on this part).
 template <bool FILL>
 __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, const double* __restrict__ radius,
                                               int n, const TableGeom* __restrict__ gp, double buffer, Emit em,
                                               long long cell_cap, unsigned* __restrict__ status) {
   // per warp and axis: the samples, their cell index (-1 outside) and the
-  // squared offset from the atom -- each depends on one axis only, so it is
-  // computed once per axis value, with the same FP64 operations
+  // squared offset from the atom in FP32 -- each depends on one axis only,
+  // so it is computed once per axis value
   __shared__ double s_samp[8][3][kMaxSamples];
-  __shared__ double s_sq[8][3][kMaxSamples];
+  __shared__ float s_sq[8][3][kMaxSamples];
   __shared__ int s_id[8][3][kMaxSamples];
   const int wib = threadIdx.x / kWarp;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
@@ -279,8 +287,9 @@ __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, co
   if (g.ncell > cell_cap) return;
   const long long ncell = g.ncell;
   double (*samp)[kMaxSamples] = s_samp[wib];
-  double (*sq)[kMaxSamples] = s_sq[wib];
+  float (*sq)[kMaxSamples] = s_sq[wib];
   int (*idx)[kMaxSamples] = s_id[wib];
+  constexpr float kEpsCell = 1e-4f;  // cell units: far above the FP32 rounding of a sample's position
   for (int a = warp; a < n; a += (gridDim.x * blockDim.x) / kWarp) {
     float4 p = pos[a];
     const double c[3] = {(double)p.x, (double)p.y, (double)p.z};
@@ -312,24 +321,43 @@ __global__ void table_members_periodic_kernel(const float4* __restrict__ pos, co
       const int k = t < cnt[0] ? 0 : (t < cnt[0] + cnt[1] ? 1 : 2);
       const int m = t - (k == 0 ? 0 : (k == 1 ? cnt[0] : cnt[0] + cnt[1]));
       const double xk = samp[k][m];
-      const double d = g.box[k];
-      const double x0 = dsub(xk, dmul(d, floor(ddiv(dsub(xk, g.min[k]), d))));
-      const int id = (int)floor(ddiv(dsub(x0, g.min[k]), g.step[k]));
+      // the sample moved into the box by whole box edges, then its cell
+      const float rel = (float)(xk - g.min[k]);
+      const float tb = rel * (float)g.inv_box[k];
+      const float nb = floorf(tb);
+      const float u = fmaf(-nb, (float)g.box[k], rel) * (float)g.inv_step[k];
+      const float fu = floorf(u);
+      int id;
+      if (tb - nb > kEpsCell && tb - nb < 1.0f - kEpsCell && u - fu > kEpsCell && u - fu < 1.0f - kEpsCell) {
+        id = (int)fu;
+      } else {
+        const double d = g.box[k];
+        const double x0 = dsub(xk, dmul(d, floor(ddiv(dsub(xk, g.min[k]), d))));
+        id = (int)floor(ddiv(dsub(x0, g.min[k]), g.step[k]));
+      }
       idx[k][m] = (id < 0 || id >= g.dims[k]) ? -1 : id;
-      const double e = dsub(xk, c[k]);
-      sq[k][m] = dmul(e, e);
+      const float e = (float)(xk - c[k]);
+      sq[k][m] = e * e;
     }
     __syncwarp();
     const int total = cnt[0] * cnt[1] * cnt[2];
     const long long sy = g.dims[2], sx = (long long)g.dims[1] * g.dims[2];
+    // FP32 squared distances carry a relative error below 4 2^-24
+    const float in2 = (float)(pad2 * (1.0 - 1e-6)), out2 = (float)(pad2 * (1.0 + 1e-6));
     for (int t = lane; t < total; t += kWarp) {
       const int kx = t / (cnt[1] * cnt[2]);
       const int ky = (t / cnt[2]) % cnt[1];
       const int kz = t % cnt[2];
       const int i0 = idx[0][kx], i1 = idx[1][ky], i2 = idx[2][kz];
-      const double s = dadd(dadd(sq[0][kx], sq[1][ky]), sq[2][kz]);
-      if (s < pad2 && i0 >= 0 && i1 >= 0 && i2 >= 0)
-        em.put<FILL>((long long)i0 * sx + (long long)i1 * sy + i2, a, ncell);
+      if (i0 < 0 || i1 < 0 || i2 < 0) continue;
+      const float sf = (sq[0][kx] + sq[1][ky]) + sq[2][kz];
+      bool member = sf < in2;
+      if (!member && sf <= out2) {
+        // the reference's FP64 test
+        const double e0 = dsub(samp[0][kx], c[0]), e1 = dsub(samp[1][ky], c[1]), e2 = dsub(samp[2][kz], c[2]);
+        member = dadd(dadd(dmul(e0, e0), dmul(e1, e1)), dmul(e2, e2)) < pad2;
+      }
+      if (member) em.put<FILL>((long long)i0 * sx + (long long)i1 * sy + i2, a, ncell);
     }
     __syncwarp();
   }

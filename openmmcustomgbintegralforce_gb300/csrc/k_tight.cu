@@ -97,6 +97,10 @@ __global__ void __launch_bounds__(kGeomThreads) tight_geom_kernel(const float4* 
   // (extent: a periodic system's longest box edge, by which a point may be moved)
   G.pad = 2e-5 + 4.0 * 1.1920929e-7 * (amax + 2.0 * margin + extent);
   G.total = 0;
+  for (int k = 0; k < 3; ++k) {
+    G.inv_step[k] = 1.0 / h;
+    G.inv_box[k] = 0.0;
+  }
   G.ncell = ncell;
   if (ncell > cell_cap) atomicOr(status, kStatusTableCells);
   *g = G;

@@ -77,8 +77,8 @@ struct RefQuery {
     const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
     const int dmax = max(geom.dims[0], max(geom.dims[1], geom.dims[2]));
     for (int k = 0; k < 3; ++k) {
-      rel[k] = (float)((x[k] - geom.min[k]) / geom.step[k]);
-      inv[k] = (float)(1.0 / geom.step[k]);
+      rel[k] = (float)((x[k] - geom.min[k]) * geom.inv_step[k]);
+      inv[k] = (float)geom.inv_step[k];
       invdims[k] = 1.0f / (float)geom.dims[k];
     }
     eps = 1e-4f + 64.0f * (float)dmax * 5.96e-8f;
@@ -134,7 +134,7 @@ struct MinImageQuery : RefQuery {
     RefQuery::init(geom, xi, qo, cap);
     for (int k = 0; k < 3; ++k) {
       L[k] = (float)geom.box[k];
-      iL[k] = (float)(1.0 / geom.box[k]);
+      iL[k] = (float)geom.inv_box[k];
     }
   }
   __device__ __forceinline__ void init(const Entries& t, const float4 xi, const double* qo) {
@@ -185,11 +185,11 @@ struct PeriodicQuery {
     const double x[3] = {(double)xi.x, (double)xi.y, (double)xi.z};
     const int dmax = max(geom.dims[0], max(geom.dims[1], geom.dims[2]));
     for (int k = 0; k < 3; ++k) {
-      rel[k] = (float)((x[k] - geom.min[k]) / geom.step[k]);
-      inv[k] = (float)(1.0 / geom.step[k]);
-      wrap[k] = (float)(geom.box[k] / geom.step[k]);
+      rel[k] = (float)((x[k] - geom.min[k]) * geom.inv_step[k]);
+      inv[k] = (float)geom.inv_step[k];
+      wrap[k] = (float)(geom.box[k] * geom.inv_step[k]);
       L[k] = (float)geom.box[k];
-      iL[k] = (float)(1.0 / geom.box[k]);
+      iL[k] = (float)geom.inv_box[k];
     }
     eps = 1e-4f + 64.0f * (float)(dmax + wrap[0] + wrap[1] + wrap[2]) * 5.96e-8f;
   }
@@ -237,7 +237,7 @@ struct TightQuery {
     xr[0] = (float)((double)xi.x - g.min[0]);
     xr[1] = (float)((double)xi.y - g.min[1]);
     xr[2] = (float)((double)xi.z - g.min[2]);
-    inv_h = (float)(1.0 / g.step[0]);
+    inv_h = (float)g.inv_step[0];
     const bool off = g.ncell > cap;  // more cells than allocated: no cell
     dims[0] = off ? 0 : g.dims[0];
     dims[1] = off ? 0 : g.dims[1];
@@ -311,7 +311,7 @@ struct PeriodicTightQuery : TightQuery {
       xw[k] = (float)(x[k] - W.min[k]);
       span[k] = (float)(W.max[k] - W.min[k]);
       L[k] = (float)W.box[k];
-      iL[k] = (float)(1.0 / W.box[k]);
+      iL[k] = (float)W.inv_box[k];
       ext = fmaxf(ext, fabsf(xw[k]) + span[k] + L[k]);
     }
     // FP32 rounding of x_i - min + v (+- L), with room to spare
