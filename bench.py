@@ -343,14 +343,58 @@ def measure_batched(gs, steps: int):
     batch_ms = timed(lambda: b.execute_device(0, sptr), steps)
     batch_host_ms = host_timed(lambda: b.execute_host(X), max(2, steps // 3))
     E, F = b.execute_host(X)
-    errs = []
+
+    # every molecule against its own single-molecule call (the same kernels:
+    # identical bits), and a stride-8 sample of them against the FP64 oracle
+    mism = 0
+    for k, (c, g) in enumerate(zip(b.molecules, gs)):
+        Ek, Fk = c.execute_host(g.positions)
+        o = b.offsets[k]
+        mism += int(not (Ek == E[k] and np.array_equal(Fk, F[o:o + sizes[k]])))
     from oracle import oracle as O
 
-    for k in (0, 1, 2, 3):
-        r = O.Oracle(models[k]).energy_forces(gs[k].positions, gs[k].charge, gs[k].radius)
+    sample = [k + (k // 8) % 2 for k in range(0, len(gs), 8)]  # every 8th, GBSW and GBMV-II alternating
+    errs = []
+    for k in sample:
+        r = O.Oracle(models[k], nthreads=os.cpu_count() or 1).energy_forces(gs[k].positions, gs[k].charge,
+                                                                            gs[k].radius)
         Fk = F[b.offsets[k]:b.offsets[k] + sizes[k]]
         errs.append((abs(E[k] / r["energy"] - 1.0),
                      float(np.sqrt(((Fk - r["forces"]) ** 2).sum() / (r["forces"] ** 2).sum()))))
+
+    # the batched differentiable form: every molecule's energy, dE/dx, dE/dq,
+    # dE/dR and dE/dalpha per call, against a loop of gbx_adjoint per molecule
+    dev = torch.device("cuda", torch.cuda.current_device())
+    M, T = len(gs), b.total
+    adj = {k: torch.zeros(n_, dtype=torch.float64, device=dev)
+           for k, n_ in (("E", M), ("F", 3 * T), ("q", T), ("R", T), ("a", 2 * M))}
+
+    def batch_adjoint():
+        b.adjoint_device(adj["E"].data_ptr(), adj["F"].data_ptr(), adj["q"].data_ptr(), adj["R"].data_ptr(),
+                         adj["a"].data_ptr(), 0, sptr)
+
+    def plain_adjoint():
+        for m, c in enumerate(b.molecules):
+            o = b.offsets[m]
+            c.adjoint_device(p + 16 * o, adj["E"].data_ptr() + 8 * m, adj["F"].data_ptr() + 24 * o,
+                             adj["q"].data_ptr() + 8 * o, adj["R"].data_ptr() + 8 * o,
+                             adj["a"].data_ptr() + 16 * m, 0, sptr)
+
+    batch_adjoint()
+    plain_adjoint()
+    plain_adj_ms = timed(plain_adjoint, max(2, steps // 3))
+    batch_adj_ms = timed(batch_adjoint, max(2, steps // 3))
+    A = b.adjoint_host(X)
+    adj_err = []
+    for k in (0, 1):
+        r = O.Oracle(models[k], nthreads=os.cpu_count() or 1).energy_forces(gs[k].positions, gs[k].charge,
+                                                                            gs[k].radius, adjoint=True)
+        o, n_ = b.offsets[k], sizes[k]
+        adj_err.append({"molecule": k, "energy_rel": abs(A["energies"][k] / r["energy"] - 1.0),
+                        "force_rel_rms": rel_rms(A["forces"][o:o + n_], r["forces"]),
+                        "dEdq_rel_rms": rel_rms(A["dEdq"][o:o + n_], r["dEdq"]),
+                        "dEdR_rel_rms": rel_rms(A["dEdR"][o:o + n_], r["dEdR"]),
+                        "dEdalpha_rel_max": float(np.abs(A["dEdalpha"][k] / r["dEdalpha"] - 1).max())})
     b.close()
     n = len(gs)
     return {"workload": f"{n} globules, atoms log-uniform in [500, 8000] (total {sum(sizes)}), "
@@ -363,7 +407,12 @@ def measure_batched(gs, steps: int):
                      "speedup_vs_plain": plain_host_ms / batch_host_ms,
                      "plain": "gbx_execute_host per molecule (host positions in, forces and energy out)",
                      "batched": "gbx_batch_execute_host (all positions in, all forces and energies out)"},
-            "err_vs_fp64_sample": {"molecules": [0, 1, 2, 3], "energy_rel_max": max(a for a, _ in errs),
+            "adjoint": {"confs_per_s": n * 1000.0 / batch_adj_ms, "plain_confs_per_s": n * 1000.0 / plain_adj_ms,
+                        "speedup_vs_plain": plain_adj_ms / batch_adj_ms,
+                        "batched": "gbx_batch_adjoint (device outputs: energies, forces, dE/dq, dE/dR, dE/dalpha)",
+                        "plain": "gbx_adjoint per molecule on one stream", "err_vs_fp64": adj_err},
+            "molecules_differing_from_single_calls": mism,
+            "err_vs_fp64_sample": {"molecules": sample, "energy_rel_max": max(a for a, _ in errs),
                                    "force_rel_rms_max": max(b_ for _, b_ in errs)}}
 
 

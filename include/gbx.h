@@ -44,7 +44,9 @@ typedef enum {
   GBX_ERR_NONFINITE = 5,      /* a Born radius or the energy came out NaN/Inf */
   GBX_ERR_TABLE_TOO_LARGE = 6, /* lookup grid would exceed its limits (reference: length > 1000 nm) */
   GBX_ERR_NOT_READY = 7,      /* result queried before an execute */
-  GBX_ERR_TIMEOUT = 8,        /* a device-side wait gave up (batched persistent kernel) */
+  GBX_ERR_TIMEOUT = 8,        /* reserved for a device-side wait that gives up; no kernel of this
+                                 library waits on another (no spin, no grid barrier), so no
+                                 entry point returns it */
   GBX_ERR_EXCEEDS_STATIC_SCRATCH = 9, /* gbx_pair_noalloc: more atoms than its static scratch holds */
   GBX_ERR_STALE_RESULT = 10   /* gbx_execute: an earlier unchecked call's lookup table outgrew its
                                  buffers, so that call's results lacked the volume terms; the
@@ -277,6 +279,19 @@ GBX_API gbx_status gbx_batch_execute(gbx_batch* batch, int flags, void* stream);
 /* Host arrays: positions / forces [total][3] (nm, kJ/mol/nm), energies [molecules]. */
 GBX_API gbx_status gbx_batch_execute_host(gbx_batch* batch, const double* positions, double* forces,
                                           double* energies);
+/* Batched adjoint (the differentiable form over many molecules): gbx_adjoint
+ * of every molecule on the batch's positions (posq buffer), fanned out over
+ * the batch's streams.  Device FP64 outputs laid out by the atom offsets,
+ * any may be NULL: energies [molecules], forces [total][3] (-dE/dx),
+ * dEdq [total], dEdR [total], dEdalpha [molecules][2].  Unchecked calls
+ * re-run checked when a table outgrew its buffers; flags may hold
+ * GBX_EXEC_CHECK.  Molecules built on compiled expressions are refused
+ * (GBX_ERR_UNSUPPORTED), as by gbx_adjoint. */
+GBX_API gbx_status gbx_batch_adjoint(gbx_batch* batch, double* energies, double* forces, double* dEdq, double* dEdR,
+                                     double* dEdalpha, int flags, void* stream);
+/* Host arrays: positions [total][3] in, the same outputs on the host. */
+GBX_API gbx_status gbx_batch_adjoint_host(gbx_batch* batch, const double* positions, double* energies,
+                                          double* forces, double* dEdq, double* dEdR, double* dEdalpha);
 /* Autotuner: times the captured batch over stream counts {4, 8, 16, 32} and
  * quadrature chunkings (default chunks per atom / {1, 2, 4}) and keeps the
  * fastest.  Outputs may be NULL. */

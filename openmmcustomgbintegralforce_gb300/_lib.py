@@ -33,7 +33,8 @@ EXPORTED = (
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
     "gbx_create_custom", "gbx_set_custom_parameters", "gbx_set_custom_global", "gbx_custom_check",
     "gbx_batch_create", "gbx_batch_destroy", "gbx_batch_molecule", "gbx_batch_buffers", "gbx_batch_execute",
-    "gbx_batch_execute_host", "gbx_batch_tune", "gbx_batch_last_error",
+    "gbx_batch_execute_host", "gbx_batch_adjoint", "gbx_batch_adjoint_host", "gbx_batch_tune",
+    "gbx_batch_last_error",
 )
 STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
@@ -156,6 +157,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_batch_buffers.argtypes = [vp, vp, vp, vp, vp]
     L.gbx_batch_execute.argtypes = [vp, ci, vp]
     L.gbx_batch_execute_host.argtypes = [vp, vp, vp, vp]
+    L.gbx_batch_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, ci, vp]
+    L.gbx_batch_adjoint_host.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.gbx_batch_tune.argtypes = [vp, vp, vp, vp]
     L.gbx_batch_last_error.argtypes = [vp, ctypes.c_char_p, sz]
     L.gbx_set_timing.argtypes = [vp, ci]
@@ -484,6 +487,25 @@ class Batch:
 
     def execute_device(self, flags: int = 0, stream: int = 0):
         self._check(self.lib.gbx_batch_execute(self.h, int(flags), ctypes.c_void_p(stream or None)))
+
+    def adjoint_device(self, energies: int, forces: int, dEdq: int, dEdR: int, dEdalpha: int, flags: int = 0,
+                       stream: int = 0):
+        """gbx_batch_adjoint on device FP64 arrays (addresses; 0 for none)."""
+        v = lambda a: ctypes.c_void_p(a or None)  # noqa: E731
+        self._check(self.lib.gbx_batch_adjoint(self.h, v(energies), v(forces), v(dEdq), v(dEdR), v(dEdalpha),
+                                               int(flags), ctypes.c_void_p(stream or None)))
+
+    def adjoint_host(self, positions):
+        """Energies [molecules], forces [total, 3], dEdq [total], dEdR [total], dEdalpha [molecules, 2]."""
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        if x.shape != (self.total, 3):
+            raise GBXError(1, "positions must be [total atoms, 3]")
+        M = len(self.sizes)
+        out = {"energies": np.zeros(M), "forces": np.zeros((self.total, 3)), "dEdq": np.zeros(self.total),
+               "dEdR": np.zeros(self.total), "dEdalpha": np.zeros((M, 2))}
+        self._check(self.lib.gbx_batch_adjoint_host(self.h, _p(x), _p(out["energies"]), _p(out["forces"]),
+                                                    _p(out["dEdq"]), _p(out["dEdR"]), _p(out["dEdalpha"])))
+        return out
 
     def execute_host(self, positions):
         x = np.ascontiguousarray(positions, dtype=np.float64)

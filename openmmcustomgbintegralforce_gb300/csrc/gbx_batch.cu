@@ -50,6 +50,8 @@ struct gbx_batch {
   cudaStream_t graph_stream = nullptr;     // stream the graph was captured for
   std::vector<unsigned long long> epochs;  // each molecule's epoch at capture
   bool sized = false;                      // one checked call has run
+  double* d_adj = nullptr;                 // host-form adjoint outputs (allocated on first use)
+  double* h_adj = nullptr;                 // pinned copy of them
   std::string last_error;
 };
 
@@ -183,6 +185,64 @@ gbx_status run(gbx_batch* b, cudaStream_t main, bool force_check) {
   return GBX_OK;
 }
 
+// Device outputs of the batched adjoint, laid out by the batch's atom
+// offsets (any may be null).
+struct AdjOut {
+  double* energies;  // [molecules]
+  double* forces;    // [total][3]
+  double* dEdq;      // [total]
+  double* dEdR;      // [total]
+  double* dEdalpha;  // [molecules][2]
+};
+
+// The adjoint fan-out: every molecule's gbx_adjoint on its stream, joined
+// back and the status words ORed (as fan_out).  Not captured: each call
+// launches the pipelines afresh.
+gbx_status adjoint_fan_out(gbx_batch* b, cudaStream_t main, bool check, const AdjOut& o) {
+  BCUDA(b, cudaEventRecord(b->fork, main));
+  for (auto s : b->streams) BCUDA(b, cudaStreamWaitEvent(s, b->fork, 0));
+  for (size_t k = 0; k < b->order.size(); ++k) {
+    const int m = b->order[k];
+    Context* c = b->mols[m];
+    const long long a = b->off[m];
+    const gbx_status s =
+        gbx_adjoint(reinterpret_cast<gbx_context*>(c), b->d_pos + a, o.energies ? o.energies + m : nullptr,
+                    o.forces ? o.forces + 3 * a : nullptr, o.dEdq ? o.dEdq + a : nullptr, o.dEdR ? o.dEdR + a : nullptr,
+                    o.dEdalpha ? o.dEdalpha + 2 * m : nullptr, check ? GBX_EXEC_CHECK : 0,
+                    b->streams[k % b->streams.size()]);
+    if (s != GBX_OK) {
+      b->last_error = "molecule " + std::to_string(m) + ": " + c->last_error;
+      return s;
+    }
+  }
+  for (size_t k = 0; k < b->streams.size(); ++k) {
+    BCUDA(b, cudaEventRecord(b->joins[k], b->streams[k]));
+    BCUDA(b, cudaStreamWaitEvent(main, b->joins[k], 0));
+  }
+  or_status_kernel<<<1, 256, 0, main>>>(b->d_status_ptr, (int)b->mols.size(), b->d_status);
+  BCUDA(b, cudaGetLastError());
+  return GBX_OK;
+}
+
+// Unchecked fan-out, re-run checked when a table outgrew its buffers.
+gbx_status run_adjoint(gbx_batch* b, cudaStream_t main, bool force_check, const AdjOut& o) {
+  BTRY(adjoint_fan_out(b, main, force_check, o));
+  BCUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, main));
+  BCUDA(b, cudaStreamSynchronize(main));
+  unsigned st = *b->h_status;
+  if (!force_check && (st & (kStatusTableCells | kStatusTableEntries | kStatusSegmentTooLong))) {
+    BTRY(adjoint_fan_out(b, main, true, o));
+    BCUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, main));
+    BCUDA(b, cudaStreamSynchronize(main));
+    st = *b->h_status;
+  }
+  if (st & kStatusNonFinite) {
+    b->last_error = "non-finite Born radius in the batch";
+    return GBX_ERR_NONFINITE;
+  }
+  return GBX_OK;
+}
+
 }  // namespace
 }  // namespace gbx
 
@@ -244,9 +304,10 @@ gbx_status gbx_batch_destroy(gbx_batch* b) {
   for (auto e : b->joins) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->own) cudaStreamDestroy(b->own);
-  for (void* p : {(void*)b->d_pos, (void*)b->d_force, (void*)b->d_energy, (void*)b->d_status_ptr, (void*)b->d_status})
+  for (void* p : {(void*)b->d_pos, (void*)b->d_force, (void*)b->d_energy, (void*)b->d_status_ptr, (void*)b->d_status,
+                  (void*)b->d_adj})
     if (p) cudaFree(p);
-  for (void* p : {(void*)b->h_status, (void*)b->h_pos, (void*)b->h_force, (void*)b->h_energy})
+  for (void* p : {(void*)b->h_status, (void*)b->h_pos, (void*)b->h_force, (void*)b->h_energy, (void*)b->h_adj})
     if (p) cudaFreeHost(p);
   delete b;
   return GBX_OK;
@@ -308,6 +369,50 @@ gbx_status gbx_batch_execute_host(gbx_batch* b, const double* positions, double*
         for (int k = 0; k < 3; ++k) forces[3 * (b->off[m] + i) + k] = gbx::fixed_to_double(f[(size_t)k * n + i]);
     if (energies) energies[m] = b->h_energy[m];
   }
+  return GBX_OK;
+}
+
+gbx_status gbx_batch_adjoint(gbx_batch* b, double* energies, double* forces, double* dEdq, double* dEdR,
+                             double* dEdalpha, int flags, void* stream) {
+  if (!b) return GBX_ERR_INVALID_ARGUMENT;
+  return gbx::run_adjoint(b, stream ? (cudaStream_t)stream : b->own, (flags & GBX_EXEC_CHECK) != 0,
+                          gbx::AdjOut{energies, forces, dEdq, dEdR, dEdalpha});
+}
+
+gbx_status gbx_batch_adjoint_host(gbx_batch* b, const double* positions, double* energies, double* forces,
+                                  double* dEdq, double* dEdR, double* dEdalpha) {
+  if (!b || !positions) return GBX_ERR_INVALID_ARGUMENT;
+  const long long T = b->total, M = (long long)b->mols.size();
+  const size_t len = (size_t)(M + 3 * T + T + T + 2 * M);
+  if (!b->d_adj) {
+    BCUDA(b, cudaMalloc((void**)&b->d_adj, sizeof(double) * len));
+    BCUDA(b, cudaMallocHost((void**)&b->h_adj, sizeof(double) * len));
+  }
+  const int threads = std::max(1, std::min(8, omp_get_num_procs()));
+  bool finite = true;
+  float4* hp = b->h_pos;
+#pragma omp parallel for reduction(&& : finite) num_threads(threads)
+  for (long long k = 0; k < T; ++k) {
+    const double x = positions[3 * k], y = positions[3 * k + 1], z = positions[3 * k + 2];
+    hp[k] = make_float4((float)x, (float)y, (float)z, 0.f);
+    finite = std::isfinite(x) && std::isfinite(y) && std::isfinite(z) && finite;
+  }
+  if (!finite) {
+    b->last_error = "non-finite position";
+    return GBX_ERR_INVALID_ARGUMENT;
+  }
+  double* d = b->d_adj;
+  const gbx::AdjOut o{d, d + M, d + M + 3 * T, d + M + 4 * T, d + M + 5 * T};
+  BCUDA(b, cudaMemcpyAsync(b->d_pos, b->h_pos, sizeof(float4) * T, cudaMemcpyHostToDevice, b->own));
+  BTRY(gbx::run_adjoint(b, b->own, false, o));
+  BCUDA(b, cudaMemcpyAsync(b->h_adj, b->d_adj, sizeof(double) * len, cudaMemcpyDeviceToHost, b->own));
+  BCUDA(b, cudaStreamSynchronize(b->own));
+  const double* h = b->h_adj;
+  if (energies) std::memcpy(energies, h, sizeof(double) * M);
+  if (forces) std::memcpy(forces, h + M, sizeof(double) * 3 * T);
+  if (dEdq) std::memcpy(dEdq, h + M + 3 * T, sizeof(double) * T);
+  if (dEdR) std::memcpy(dEdR, h + M + 4 * T, sizeof(double) * T);
+  if (dEdalpha) std::memcpy(dEdalpha, h + M + 5 * T, sizeof(double) * 2 * M);
   return GBX_OK;
 }
 

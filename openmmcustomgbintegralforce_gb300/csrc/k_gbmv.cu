@@ -11,8 +11,9 @@
 //
 //   bin      warp per (atom, quadrature chunk), lanes over points: the
 //            point's cell (the reference query, exact near cell faces),
-//            a slot in the cell by one atomic per distinct cell per warp;
-//            points whose cell has no list get their solvent fraction here
+//            a slot in the cell by one atomic per point, four points per
+//            lane in flight; points whose cell has no list get their
+//            solvent fraction here
 //   scan     points per cell -> each cell's first slot
 //   fill     point ids into their cell's slots
 //   integral warp per cell: sorts the cell's point ids (the slots were
@@ -25,7 +26,9 @@
 //   reduce   warp per (atom, chunk): J4, J7 over the solvent fractions in
 //            quadrature order (the integral pass's partition, so the Born
 //            radii are assembled as before)
-//   chain    warp per cell, lanes as 4 points x 8 list entries: each lane
+//   chain    warp per cell, lanes as 4 points x 8 lanes of entry pairs
+//            (packed FP32x2, two entries per instruction; the integral pass
+//            likewise evaluates two entries per instruction): each lane
 //            keeps the pull of its entries in registers over all of the
 //            cell's points (one fixed-point reduction per cell and entry
 //            instead of one per point and entry); the point's own pull is
@@ -133,7 +136,6 @@ __global__ void __launch_bounds__(kBinThreads) gbmv_bin_kernel(const float4* __r
   Q query;
   query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
-  const unsigned lt = (1u << lane) - 1u;
   for (int base = q0; base < q1; base += kBinBatch * kWarp) {
     long long cell[kBinBatch];
     int cnt[kBinBatch];
@@ -147,31 +149,21 @@ __global__ void __launch_bounds__(kBinThreads) gbmv_bin_kernel(const float4* __r
 #pragma unroll
     for (int u = 0; u < kBinBatch; ++u)
       if (cell[u] >= 0) cnt[u] = __ldg(&tab.cell[cell[u]].x);
-    int r0[kBinBatch];
-    unsigned peers[kBinBatch];
+    // one slot atomic per listed point (the warp's points mostly fall in
+    // distinct cells: aggregating them by __match_any_sync measured slower)
+    int slot[kBinBatch];
 #pragma unroll
     for (int u = 0; u < kBinBatch; ++u) {
-      const bool listed = cell[u] >= 0 && cnt[u] > 0;
-      const unsigned lm = __ballot_sync(0xffffffffu, listed);
-      r0[u] = 0;
-      peers[u] = 0u;
-      if (listed) {
-        // one atomic per distinct cell among the warp's points
-        peers[u] = __match_any_sync(lm, (int)cell[u]);
-        if (lane == __ffs(peers[u]) - 1) r0[u] = atomicAdd(&cp.count[cell[u]], __popc(peers[u]));
-      }
+      slot[u] = 0;
+      if (cell[u] >= 0 && cnt[u] > 0) slot[u] = atomicAdd(&cp.count[cell[u]], 1);
     }
 #pragma unroll
     for (int u = 0; u < kBinBatch; ++u) {
       const int q = base + u * kWarp + lane;
-      const bool listed = cell[u] >= 0 && cnt[u] > 0;
-      // every lane takes part in the shuffle; a lane without a cell reads its own value
-      const int src = listed ? __ffs(peers[u]) - 1 : lane;
-      const int rr = __shfl_sync(0xffffffffu, r0[u], src);
       const size_t p = (size_t)i * m.nq + q;
-      if (listed) {
+      if (cell[u] >= 0 && cnt[u] > 0) {
         cp.cell[p] = (int)cell[u];
-        cp.rank[p] = rr + __popc(peers[u] & lt);
+        cp.rank[p] = slot[u];
       } else if (q < q1) {
         cp.cell[p] = -1;
         cp.sval[p] = empty_list_fraction<MODEL>(m);
@@ -262,12 +254,13 @@ __device__ __forceinline__ float rcp_ftz(float x) {
 __device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 rcp2(float2 t) { return make_float2(rcp_ftz(t.x), rcp_ftz(t.y)); }
 
-// The cell's list staged in shared memory, one array per field, so that two
-// consecutive entries load as one float2 and feed packed FP32x2 arithmetic
-// (__ffma2_rn and friends: one instruction for two entries, each half
-// rounded as its scalar form).  A list of odd length is padded with one
-// entry whose every contribution is exactly zero (C = 0 for GBMV-II,
-// gamma = 0 for GBMV-I's chain; T = 100 r^2 + 1 >= 1), index -1.
+// The cell's list staged in shared memory, one array per field, so that four
+// consecutive entries load as one float4 (two pairs) and each pair feeds
+// packed FP32x2 arithmetic (__ffma2_rn and friends: one instruction for two
+// entries, each half rounded as its scalar form).  A list whose length is
+// not a multiple of four is padded with entries whose every contribution is
+// exactly zero (C = 0 for GBMV-II, gamma = 0 for GBMV-I's chain;
+// T = 100 r^2 + 1 >= 1), index -1.
 struct __align__(16) CellList {
   float x[kMaxList], y[kMaxList], z[kMaxList];  // x_j - c0
   float w[kMaxList];    // GBMV-II C_j | GBMV-I gamma_j
@@ -277,12 +270,14 @@ struct __align__(16) CellList {
 };
 
 __device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
-__device__ __forceinline__ int2 ld2i(const int* p) { return *reinterpret_cast<const int2*>(p); }
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
 template <bool PER>
 __device__ __forceinline__ void stage_list(CellList& L, const Entries& tab, int2 cs, int cnt, float3 c0, int lane) {
-  const int cnt2 = (cnt + 1) & ~1;
-  for (int l = lane; l < cnt2; l += kWarp) {
+  const int cnt4 = (cnt + 3) & ~3;
+  for (int l = lane; l < cnt4; l += kWarp) {
     if (l < cnt) {
       const float4 a = __ldg(tab.e + cs.y + l);
       const float2 pk = __ldg(tab.par + cs.y + l);
@@ -324,9 +319,9 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
   int* order = cp.order + start;
   if (P > 1) sort_cell(order, P, lane);
   __syncwarp();
-  // GBMV-II's padding entry adds exactly zero; GBMV-I's (e^0 = 1) does not,
-  // so its odd entry is taken on its own
-  const int npair = MODEL == GBX_MODEL_GBMV2 ? (cnt + 1) >> 1 : cnt >> 1;
+  // GBMV-II's padding entries add exactly zero; GBMV-I's (e^0 = 1) do not,
+  // so its last (cnt mod 4) entries are taken one at a time
+  const int nquad = MODEL == GBX_MODEL_GBMV2 ? (cnt + 3) >> 2 : cnt >> 2;
   for (int base = 0; base < P; base += kWarp) {
     const int k = base + lane;
     const bool valid = k < P;
@@ -336,18 +331,16 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
     const float px = (xi.x - c0.x) + v.x, py = (xi.y - c0.y) + v.y, pz = (xi.z - c0.z) + v.z;
     const float2 npx = bc2(-px), npy = bc2(-py), npz = bc2(-pz);
     float2 s1 = bc2(0.f), s2 = bc2(0.f), vx = bc2(0.f), vy = bc2(0.f), vz = bc2(0.f);
-    for (int j = 0; j < npair; ++j) {
-      const int l = 2 * j;
-      float2 dx = __fadd2_rn(ld2(L.x + l), npx), dy = __fadd2_rn(ld2(L.y + l), npy),
-             dz = __fadd2_rn(ld2(L.z + l), npz);
+    auto pair = [&](float2 ex, float2 ey, float2 ez, float2 ew, float2 ek) {
+      float2 dx = __fadd2_rn(ex, npx), dy = __fadd2_rn(ey, npy), dz = __fadd2_rn(ez, npz);
       img.apply2(dx, dy, dz);
       const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
       if (MODEL == GBX_MODEL_GBMV1) {
-        const float2 g = __fmul2_rn(ld2(L.w + l), __fmul2_rn(r2, r2));
+        const float2 g = __fmul2_rn(ew, __fmul2_rn(r2, r2));
         s1 = __fadd2_rn(s1, make_float2(__expf(g.x), __expf(g.y)));
       } else {
-        const float2 T = __ffma2_rn(bc2(100.0f), r2, ld2(L.k + l));
-        float2 F = __fmul2_rn(ld2(L.w + l), rcp2(T));
+        const float2 T = __ffma2_rn(bc2(100.0f), r2, ek);
+        float2 F = __fmul2_rn(ew, rcp2(T));
         F = __fmul2_rn(F, F);
         s1 = __fadd2_rn(s1, F);
         s2 = __ffma2_rn(r2, __fmul2_rn(F, F), s2);
@@ -355,13 +348,21 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_integral_kernel(const 
         vy = __ffma2_rn(dy, F, vy);
         vz = __ffma2_rn(dz, F, vz);
       }
+    };
+    for (int j = 0; j < nquad; ++j) {
+      const int l = 4 * j;
+      const float4 X = ld4(L.x + l), Y = ld4(L.y + l), Z = ld4(L.z + l), W = ld4(L.w + l);
+      const float4 K4 = MODEL == GBX_MODEL_GBMV2 ? ld4(L.k + l) : make_float4(0.f, 0.f, 0.f, 0.f);
+      pair(lo2(X), lo2(Y), lo2(Z), lo2(W), lo2(K4));
+      pair(hi2(X), hi2(Y), hi2(Z), hi2(W), hi2(K4));
     }
     Sums s{s1.x + s1.y, s2.x + s2.y, vx.x + vx.y, vy.x + vy.y, vz.x + vz.y};
-    if (MODEL == GBX_MODEL_GBMV1 && (cnt & 1)) {
-      const int l = cnt - 1;
-      const float3 d = img.apply(make_float3(L.x[l] - px, L.y[l] - py, L.z[l] - pz));
-      const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-      s.s1 += __expf(L.w[l] * (r2 * r2));
+    if (MODEL == GBX_MODEL_GBMV1) {
+      for (int l = 4 * nquad; l < cnt; ++l) {
+        const float3 d = img.apply(make_float3(L.x[l] - px, L.y[l] - py, L.z[l] - pz));
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        s.s1 += __expf(L.w[l] * (r2 * r2));
+      }
     }
     if (valid) {
       float pl, S;
@@ -434,15 +435,15 @@ __device__ __forceinline__ void add_fixed_one(unsigned long long* a, int k, floa
 // shared memory): its position in the cell frame and the factors of the
 // gradient with c ds/dS folded in.  GBMV-II: with u_j = F_j / T_j and
 // vd = v . d_j, the pull on entry j is
-//   g_j = [-400 u_j (A + C vd) + B F_j (F_j - 400 u_j r_j^2)] d_j + F_j Cv
+//   g_j = [-400 u_j (A + C vd) + B F_j (F_j - 400 u_j r_j^2)] d_j + F_j C v
 // with A = c ds/dS s0 s2 / |v|^2, B = 2 c ds/dS s0 s1 / |v|^2,
-// C = -2 c ds/dS s0 s1 s2 / |v|^4 (the d s1, d s2 and d |v|^2 factors) and
-// Cv = C v.  GBMV-I: g_j = A e_j r_j^2 d_j with A = 4 c ds/dS gamma_j
+// C = -2 c ds/dS s0 s1 s2 / |v|^4 (the d s1, d s2 and d |v|^2 factors).
+// GBMV-I: g_j = A e_j r_j^2 d_j with A = 4 c ds/dS gamma_j
 // folded per entry.
 struct __align__(16) PointChain {
   float2 npx, npy, npz;  // minus the point's position in the cell frame, in both halves
   float2 A, B, C;        // GBMV-I: A only
-  float2 vx, vy, vz, cvx, cvy, cvz;
+  float2 vx, vy, vz;
   float cS;
   int i;
 };
@@ -495,7 +496,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
       pc.cS = 0.0f;
       pc.i = -1;
       pc.npx = pc.npy = pc.npz = pc.A = pc.B = pc.C = bc2(0.f);
-      pc.vx = pc.vy = pc.vz = pc.cvx = pc.cvy = pc.cvz = bc2(0.f);
+      pc.vx = pc.vy = pc.vz = bc2(0.f);
       if (k < P) {
         const int p = order[k];
         const int i = p / m.nq, q = p - i * m.nq;
@@ -527,9 +528,6 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
           pc.vx = bc2(vx);
           pc.vy = bc2(vy);
           pc.vz = bc2(vz);
-          pc.cvx = bc2(C * vx);
-          pc.cvy = bc2(C * vy);
-          pc.cvz = bc2(C * vz);
         }
       }
       pts[lane] = pc;
@@ -543,82 +541,83 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
       float2 ox = bc2(0.f), oy = bc2(0.f), oz = bc2(0.f);
       if (live) {
         const int pi = pc.i;
+        // entries l and l + 1 as one pair, accumulated into acc[e]
+        auto pair = [&](int e, int l, float2 ex, float2 ey, float2 ez, float2 aw, float2 ek, float2 er, int2 kj) {
+          float2 dx = __fadd2_rn(ex, pc.npx), dy = __fadd2_rn(ey, pc.npy), dz = __fadd2_rn(ez, pc.npz);
+          img.apply2(dx, dy, dz);
+          const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+          // atom i's own entry moves with the point: no force from it
+          const float2 own = make_float2(kj.x != pi ? 1.0f : 0.0f, kj.y != pi ? 1.0f : 0.0f);
+          float2 gx, gy, gz;
+          if (MODEL == GBX_MODEL_GBMV1) {
+            const float2 r4 = __fmul2_rn(r2, r2);
+            const float2 g = __fmul2_rn(aw, r4);
+            const float2 ex2 = make_float2(__expf(g.x), __expf(g.y));
+            if (ADJ) {
+              // dS/dR_j = -4 gamma_j e_j r^4 / R_j (gamma ~ R^-4); padding: gamma = 0
+              const float2 dr = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(pc.cS), ex2), r4),
+                                           make_float2(-4.0f * aw.x / ek.x, -4.0f * aw.y / ek.y));
+              accR[e] = __fadd2_rn(accR[e], dr);
+              if (!sorted) {
+                if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
+                if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
+              }
+            }
+            // dS/d(delta) = 4 gamma e r^2 delta
+            const float2 gs = __fmul2_rn(__fmul2_rn(__fmul2_rn(__fmul2_rn(pc.A, aw), ex2), r2), own);
+            gx = __fmul2_rn(gs, dx);
+            gy = __fmul2_rn(gs, dy);
+            gz = __fmul2_rn(gs, dz);
+          } else {
+            const float2 T = __ffma2_rn(bc2(100.0f), r2, ek);
+            const float2 rT = rcp2(T);
+            const float2 CT = __fmul2_rn(aw, rT);
+            const float2 F = __fmul2_rn(CT, CT);
+            const float2 u = __fmul2_rn(F, rT);  // dF/d(delta) = -400 u delta
+            const float2 vd = __ffma2_rn(pc.vx, dx, __ffma2_rn(pc.vy, dy, __fmul2_rn(pc.vz, dz)));
+            if (ADJ) {
+              // dF/dR_j with T = C_j + 100 (r^2 - R_j^2), C_j = 10 p1 R_j + p2 (nm -> A):
+              // c ds/dS (s2 dF + s1 d(r^2 F^2) + d|v|^2) / |v|^2 as pc.A, pc.B, pc.C carry them
+              const float2 Tp = __ffma2_rn(bc2(-200.0f), er, bc2(Cp));
+              const float2 num = __ffma2_rn(bc2(Cp), T, __fmul2_rn(make_float2(-aw.x, -aw.y), Tp));
+              const float2 dFdR = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(2.0f), CT), num), __fmul2_rn(rT, rT));
+              const float2 fac = __ffma2_rn(pc.C, vd, __ffma2_rn(pc.B, __fmul2_rn(r2, F), pc.A));
+              const float2 dr = __fmul2_rn(dFdR, fac);
+              accR[e] = __fadd2_rn(accR[e], dr);
+              if (!sorted) {
+                if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
+                if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
+              }
+            }
+            // g = [-400 u (A + C vd) + B F (F - 400 u r^2)] delta + F C v
+            const float2 m400u = __fmul2_rn(bc2(-400.0f), u);
+            const float2 sc = __fmul2_rn(
+                __ffma2_rn(m400u, __ffma2_rn(pc.C, vd, pc.A), __fmul2_rn(__fmul2_rn(pc.B, F), __ffma2_rn(m400u, r2, F))),
+                own);
+            const float2 FC = __fmul2_rn(__fmul2_rn(F, own), pc.C);
+            gx = __ffma2_rn(sc, dx, __fmul2_rn(FC, pc.vx));
+            gy = __ffma2_rn(sc, dy, __fmul2_rn(FC, pc.vy));
+            gz = __ffma2_rn(sc, dz, __fmul2_rn(FC, pc.vz));
+          }
+          if (sorted) {
+            acc[e][0] = __fadd2_rn(acc[e][0], gx);
+            acc[e][1] = __fadd2_rn(acc[e][1], gy);
+            acc[e][2] = __fadd2_rn(acc[e][2], gz);
+          } else {
+            if (l < cnt && kj.x != pi) add_fixed3(out, kj.x, -gx.x, -gy.x, -gz.x);
+            if (l + 1 < cnt && kj.y != pi) add_fixed3(out, kj.y, -gx.y, -gy.y, -gz.y);
+          }
+          ox = __fadd2_rn(ox, gx);
+          oy = __fadd2_rn(oy, gy);
+          oz = __fadd2_rn(oz, gz);
+        };
 #pragma unroll
         for (int e = 0; e < kPairsPerLane; ++e) {
           const int l = 2 * (es + e * kChainEnt);
           if (l < cnt) {
-            float2 dx = __fadd2_rn(ld2(L.x + l), pc.npx), dy = __fadd2_rn(ld2(L.y + l), pc.npy),
-                   dz = __fadd2_rn(ld2(L.z + l), pc.npz);
-            img.apply2(dx, dy, dz);
-            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            const float2 aw = ld2(L.w + l);
-            const int2 kj = ld2i(L.idx + l);
-            // atom i's own entry moves with the point: no force from it
-            const float2 own = make_float2(kj.x != pi ? 1.0f : 0.0f, kj.y != pi ? 1.0f : 0.0f);
-            float2 gx, gy, gz;
-            if (MODEL == GBX_MODEL_GBMV1) {
-              const float2 r4 = __fmul2_rn(r2, r2);
-              const float2 g = __fmul2_rn(aw, r4);
-              const float2 ex = make_float2(__expf(g.x), __expf(g.y));
-              if (ADJ) {
-                // dS/dR_j = -4 gamma_j e_j r^4 / R_j (gamma ~ R^-4); padding: gamma = 0
-                const float2 R = ld2(L.k + l);
-                const float2 dr = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(pc.cS), ex), r4),
-                                             make_float2(-4.0f * aw.x / R.x, -4.0f * aw.y / R.y));
-                accR[e] = __fadd2_rn(accR[e], dr);
-                if (!sorted) {
-                  if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
-                  if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
-                }
-              }
-              // dS/d(delta) = 4 gamma e r^2 delta
-              const float2 gs = __fmul2_rn(__fmul2_rn(__fmul2_rn(__fmul2_rn(pc.A, aw), ex), r2), own);
-              gx = __fmul2_rn(gs, dx);
-              gy = __fmul2_rn(gs, dy);
-              gz = __fmul2_rn(gs, dz);
-            } else {
-              const float2 T = __ffma2_rn(bc2(100.0f), r2, ld2(L.k + l));
-              const float2 rT = rcp2(T);
-              const float2 CT = __fmul2_rn(aw, rT);
-              const float2 F = __fmul2_rn(CT, CT);
-              const float2 u = __fmul2_rn(F, rT);  // dF/d(delta) = -400 u delta
-              const float2 vd = __ffma2_rn(pc.vx, dx, __ffma2_rn(pc.vy, dy, __fmul2_rn(pc.vz, dz)));
-              if (ADJ) {
-                // dF/dR_j with T = C_j + 100 (r^2 - R_j^2), C_j = 10 p1 R_j + p2 (nm -> A):
-                // c ds/dS (s2 dF + s1 d(r^2 F^2) + d|v|^2) / |v|^2 as pc.A, pc.B, pc.C carry them
-                const float2 R = ld2(L.r + l);
-                const float2 Tp = __ffma2_rn(bc2(-200.0f), R, bc2(Cp));
-                const float2 num = __ffma2_rn(bc2(Cp), T, __fmul2_rn(make_float2(-aw.x, -aw.y), Tp));
-                const float2 dFdR = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(2.0f), CT), num), __fmul2_rn(rT, rT));
-                const float2 fac = __ffma2_rn(pc.C, vd, __ffma2_rn(pc.B, __fmul2_rn(r2, F), pc.A));
-                const float2 dr = __fmul2_rn(dFdR, fac);
-                accR[e] = __fadd2_rn(accR[e], dr);
-                if (!sorted) {
-                  if (l < cnt) add_fixed_one(out.dEdR, kj.x, dr.x);
-                  if (l + 1 < cnt) add_fixed_one(out.dEdR, kj.y, dr.y);
-                }
-              }
-              // g = [-400 u (A + C vd) + B F (F - 400 u r^2)] delta + F C v
-              const float2 m400u = __fmul2_rn(bc2(-400.0f), u);
-              const float2 sc = __fmul2_rn(
-                  __ffma2_rn(m400u, __ffma2_rn(pc.C, vd, pc.A), __fmul2_rn(__fmul2_rn(pc.B, F), __ffma2_rn(m400u, r2, F))),
-                  own);
-              const float2 Fo = __fmul2_rn(F, own);
-              gx = __ffma2_rn(sc, dx, __fmul2_rn(Fo, pc.cvx));
-              gy = __ffma2_rn(sc, dy, __fmul2_rn(Fo, pc.cvy));
-              gz = __ffma2_rn(sc, dz, __fmul2_rn(Fo, pc.cvz));
-            }
-            if (sorted) {
-              acc[e][0] = __fadd2_rn(acc[e][0], gx);
-              acc[e][1] = __fadd2_rn(acc[e][1], gy);
-              acc[e][2] = __fadd2_rn(acc[e][2], gz);
-            } else {
-              if (l < cnt && kj.x != pi) add_fixed3(out, kj.x, -gx.x, -gy.x, -gz.x);
-              if (l + 1 < cnt && kj.y != pi) add_fixed3(out, kj.y, -gx.y, -gy.y, -gz.y);
-            }
-            ox = __fadd2_rn(ox, gx);
-            oy = __fadd2_rn(oy, gy);
-            oz = __fadd2_rn(oz, gz);
+            const float2 R2 = ADJ && MODEL == GBX_MODEL_GBMV2 ? ld2(L.r + l) : bc2(0.f);
+            pair(e, l, ld2(L.x + l), ld2(L.y + l), ld2(L.z + l), ld2(L.w + l), ld2(L.k + l), R2,
+                 *reinterpret_cast<const int2*>(L.idx + l));
           }
         }
       }

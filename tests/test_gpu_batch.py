@@ -73,6 +73,32 @@ def test_batch_against_oracle(setup):
         assert rel_rms(split(b, F)[k], r["forces"]) < 1e-4
 
 
+def test_batch_adjoint_matches_single_contexts_and_oracle(setup):
+    """gbx_batch_adjoint (every molecule's energy, dE/dx, dE/dq, dE/dR and
+    dE/dalpha in one fanned-out call) equals each molecule's own
+    gbx_adjoint_host bit for bit, on the first (checked) call and on a
+    repeat; GBSW and GBMV-II molecules also against the oracle's adjoint."""
+    gs, ms, b, X = setup
+    for call in range(2):
+        out = b.adjoint_host(X)
+        for k, (c, g) in enumerate(zip(b.molecules, gs)):
+            o, n = b.offsets[k], b.sizes[k]
+            ref = c.adjoint(X[o:o + n])
+            assert out["energies"][k] == ref["energy"], (call, k)
+            assert np.array_equal(out["forces"][o:o + n], ref["forces"]), (call, k)
+            assert np.array_equal(out["dEdq"][o:o + n], ref["dEdq"]), (call, k)
+            assert np.array_equal(out["dEdR"][o:o + n], ref["dEdR"]), (call, k)
+            assert np.array_equal(out["dEdalpha"][k], ref["dEdalpha"]), (call, k)
+    for k in (0, 1):
+        o, n = b.offsets[k], b.sizes[k]
+        r = O.Oracle(ms[k]).energy_forces(gs[k].positions, gs[k].charge, gs[k].radius, adjoint=True)
+        assert abs(out["energies"][k] / r["energy"] - 1) < 2e-5
+        assert rel_rms(out["forces"][o:o + n], r["forces"]) < 1e-4
+        assert rel_rms(out["dEdq"][o:o + n], r["dEdq"]) < 1e-4
+        assert rel_rms(out["dEdR"][o:o + n], r["dEdR"]) < 1e-4
+        assert np.abs(out["dEdalpha"][k] / r["dEdalpha"] - 1).max() < 1e-4
+
+
 def test_replay_that_outgrows_a_table_reruns_checked(setup):
     gs, ms, b, X = setup
     b.execute_host(X)
