@@ -482,7 +482,7 @@ def stage_roofline(ctx, model, g, n, step, flush, sptr, posq, force, stride, ene
     cand = {"integrals": integral_flops / (stage_ms["integrals"] * 1e-3) / 1e12,
             "pair": pair_flops / (stage_ms["pair"] * 1e-3) / 1e12,
             "chain_rule": chain_flops / (stage_ms["chain_rule"] * 1e-3) / 1e12}
-    dominant = max(("integrals", "pair", "chain_rule", "lookup_table"), key=lambda k: stage_ms[k])
+    dominant = max(("integrals", "pair", "chain_rule", "lookup_table", "point_binning"), key=lambda k: stage_ms[k])
     achieved = cand.get(dominant)
     return {"bound": "fp32", "kernel": dominant, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": (achieved / fp32_peak) if achieved else None,

@@ -36,7 +36,7 @@ EXPORTED = (
     "gbx_batch_execute_host", "gbx_batch_adjoint", "gbx_batch_adjoint_host", "gbx_batch_tune",
     "gbx_batch_last_error",
 )
-STAGES = ("stage_positions", "lookup_table", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
+STAGES = ("stage_positions", "lookup_table", "point_binning", "integrals", "born_radii", "pair", "chain_prep", "chain_rule",
           "energy_reduce")
 
 

@@ -463,6 +463,8 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
   const bool chain = forces || adjoint;
   GBX_TRY(prepare_records(ctx, chain && !adjoint && !count_work));
   GBX_TRY(mark());
+  GBX_TRY(gbx::launch_binning(ctx, ctx->d_pos, count_work));
+  GBX_TRY(mark());
   GBX_TRY(gbx::launch_integrals(ctx, ctx->d_pos, count_work));
   GBX_TRY(mark());
   if (ctx->custom) {

@@ -235,7 +235,7 @@ struct Context {
 
   // optional per-stage timing (CUDA events on the execute stream)
   bool timing = false;
-  static constexpr int kStages = 8;
+  static constexpr int kStages = 9;
   cudaEvent_t ev[kStages + 1] = {};
 
   // caller-facing layout of the device call
@@ -315,6 +315,9 @@ size_t table_geom_scratch_doubles(int n);
 gbx_status launch_tight_build(Context* ctx, const float4* pos);
 // The standalone (reference) table's grid geometry alone, into out.
 void launch_standalone_geom(Context* ctx, const float4* pos, TableGeom* out);
+// GBMV on a table the cell passes serve: bins the quadrature points by
+// cell (the cell passes' data layout); nothing otherwise.
+gbx_status launch_binning(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work);
 gbx_status launch_born(Context* ctx);
 gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
@@ -324,6 +327,7 @@ ModelConst make_model_const(const Context* ctx);
 gbx_status launch_chain_prep(Context* ctx, bool adjoint);
 gbx_status launch_chain(Context* ctx, const float4* pos, unsigned long long* force, int stride, bool adjoint);
 bool gbmv_cells_apply(const Context* ctx);
+gbx_status launch_gbmv_cells_bin(Context* ctx, const float4* pos, const ModelConst& m);
 gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const ModelConst& m);
 gbx_status launch_gbmv_cells_chain(Context* ctx, const float4* pos, const ModelConst& m, unsigned long long* force,
                                    int stride, bool adjoint);

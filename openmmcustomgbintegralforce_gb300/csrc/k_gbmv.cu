@@ -704,7 +704,7 @@ Entries gbmv_entries(const Context* ctx) {
 }
 }  // namespace
 
-gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const ModelConst& m) {
+gbx_status launch_gbmv_cells_bin(Context* ctx, const float4* pos, const ModelConst& m) {
   cudaStream_t st = ctx->stream;
   const Entries t = gbmv_entries(ctx);
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
@@ -715,7 +715,6 @@ gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const Mod
   const long long warps = (long long)ctx->n * ctx->n_chunks;
   const int bin_blocks = (int)((warps * kWarp + kBinThreads - 1) / kBinThreads);
   const long long cells = ctx->cell_cap;
-  const int cell_blocks = (int)((cells + kCellWarps - 1) / kCellWarps);
   cudaMemsetAsync(ctx->d_pcount, 0, sizeof(int) * cells, st);
   const bool per = ctx->cfg.periodic != 0;
   if (m.model == GBX_MODEL_GBMV1) {
@@ -729,6 +728,22 @@ gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const Mod
   launch_scan<false>(ctx->d_pcount, ctx->d_pgeom, ctx->d_pblock_sums, ctx->d_pstart, nullptr, cells, 0x7fffffffffffLL,
                      ctx->d_status, st);
   gbmv_fill_kernel<<<(int)((npts + 255) / 256), 256, 0, st>>>(npts, cp);
+  ctx->launches += 6;  // bin, ncell copy, three scan phases, fill
+  return GBX_OK;
+}
+
+gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const ModelConst& m) {
+  cudaStream_t st = ctx->stream;
+  const Entries t = gbmv_entries(ctx);
+  const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
+  const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
+  const long long npts = (long long)ctx->n * m.nq;
+  const CellPoints cp{ctx->d_pcount, ctx->d_pstart, ctx->d_porder, ctx->d_pcell, ctx->d_prank,
+                      ctx->d_sval,   ctx->d_pstate, (size_t)npts};
+  const long long warps = (long long)ctx->n * ctx->n_chunks;
+  const int bin_blocks = (int)((warps * kWarp + kBinThreads - 1) / kBinThreads);
+  const int cell_blocks = (int)((ctx->cell_cap + kCellWarps - 1) / kCellWarps);
+  const bool per = ctx->cfg.periodic != 0;
   if (m.model == GBX_MODEL_GBMV1) {
     if (per) gbmv_cell_integral_kernel<GBX_MODEL_GBMV1, true><<<cell_blocks, kCellThreads, 0, st>>>(pos, t, qd, m, cp);
     else gbmv_cell_integral_kernel<GBX_MODEL_GBMV1, false><<<cell_blocks, kCellThreads, 0, st>>>(pos, t, qd, m, cp);
@@ -738,7 +753,7 @@ gbx_status launch_gbmv_cells_integral(Context* ctx, const float4* pos, const Mod
   }
   gbmv_reduce_kernel<<<bin_blocks, kBinThreads, 0, st>>>(ctx->n, qd, m.nq, chunk, ctx->n_chunks, ctx->d_sval,
                                                          ctx->d_J);
-  ctx->launches += 8;  // bin, ncell copy, three scan phases, fill, integral, reduce
+  ctx->launches += 2;  // integral, reduce
   return GBX_OK;
 }
 

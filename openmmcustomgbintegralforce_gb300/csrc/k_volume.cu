@@ -1062,9 +1062,7 @@ int volume_blocks(const Context* ctx) {
 
 template <int MODEL, class Q>
 void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bool count_work) {
-  ctx->gbmv_cells = false;
-  if (MODEL != GBX_MODEL_GBSW && !count_work && gbmv_cells_apply(ctx)) {
-    ctx->gbmv_cells = true;
+  if (MODEL != GBX_MODEL_GBSW && !count_work && ctx->gbmv_cells) {
     launch_gbmv_cells_integral(ctx, pos, m);
     return;
   }
@@ -1127,6 +1125,13 @@ gbx_status launch_status(Context* ctx, const char* what) {
 }
 
 }  // namespace
+
+gbx_status launch_binning(Context* ctx, const float4* pos, bool count_work) {
+  ctx->gbmv_cells = ctx->cfg.model != GBX_MODEL_GBSW && !count_work && gbmv_cells_apply(ctx);
+  if (!ctx->gbmv_cells) return GBX_OK;
+  launch_gbmv_cells_bin(ctx, pos, make_model_const(ctx));
+  return launch_status(ctx, "point binning launch");
+}
 
 gbx_status launch_integrals(Context* ctx, const float4* pos, bool count_work) {
   const ModelConst m = make_model_const(ctx);
