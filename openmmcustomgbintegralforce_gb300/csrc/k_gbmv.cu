@@ -120,31 +120,69 @@ __device__ __forceinline__ float empty_list_fraction(const ModelConst& m) {
   return logistic_solvent(m.beta, m.lambda, 0.0f, p);
 }
 
+// One binned point: its slot in its cell, or (no list) its solvent fraction.
+template <int MODEL>
+__device__ __forceinline__ void bin_point(const CellPoints& cp, const Entries& tab, const ModelConst& m, size_t p,
+                                          long long cell) {
+  const int cnt = cell >= 0 ? __ldg(&tab.cell[cell].x) : 0;
+  if (cnt > 0) {
+    cp.cell[p] = (int)cell;
+    cp.rank[p] = atomicAdd(&cp.count[cell], 1);
+  } else {
+    cp.cell[p] = -1;
+    cp.sval[p] = empty_list_fraction<MODEL>(m);
+  }
+}
+
 template <int MODEL, class Q>
 __global__ void __launch_bounds__(kBinThreads) gbmv_bin_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                                Quad quad, ModelConst m, int chunk, int n_chunks,
                                                                CellPoints cp) {
   // kBinBatch points per lane per step: their cell queries, list-count loads
-  // and slot atomics are issued back to back, so each warp keeps several
-  // atomics in flight instead of waiting out one round trip per point
+  // and slot atomics are issued back to back.  A point within the FP32
+  // query's guard band (about one in 500) needs the FP64 query; those are
+  // queued per warp and resolved kBinDefer at a time with every lane busy,
+  // instead of stalling the warp for each one (FP64 runs at a small fraction
+  // of the FP32 rate on this part, whatever the number of active lanes).
   constexpr int kBinBatch = 4;
+  constexpr int kBinDefer = 256;
+  static_assert(kBinDefer >= 2 * kBinBatch * kWarp, "deferred queue");
+  __shared__ int s_defer[kBinThreads / kWarp][kBinDefer];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
+  const int wib = threadIdx.x / kWarp;
   if (warp >= n * n_chunks) return;
   const int i = warp % n, c = warp / n;
   const float4 xi = pos[i];
   Q query;
   query.init(tab, xi, quad.qoff);
   const int q0 = c * chunk, q1 = min(m.nq, q0 + chunk);
+  const unsigned lt = (1u << lane) - 1u;
+  int* defer = s_defer[wib];
+  int ndef = 0;  // warp-uniform
+  auto flush = [&]() {
+    __syncwarp();
+    for (int k = lane; k < ndef; k += kWarp) {
+      const int q = defer[k];
+      bin_point<MODEL>(cp, tab, m, (size_t)i * m.nq + q, query.cell(xi, quad.qv[q], q));
+    }
+    __syncwarp();
+    ndef = 0;
+  };
   for (int base = q0; base < q1; base += kBinBatch * kWarp) {
     long long cell[kBinBatch];
     int cnt[kBinBatch];
+    bool late[kBinBatch];
 #pragma unroll
     for (int u = 0; u < kBinBatch; ++u) {
       const int q = base + u * kWarp + lane;
       cell[u] = -1;
       cnt[u] = 0;
-      if (q < q1) cell[u] = query.cell(xi, quad.qv[q], q);
+      late[u] = false;
+      if (q < q1) cell[u] = query.cell_fast(quad.qv[q], late[u]);
+      const unsigned dm = __ballot_sync(0xffffffffu, late[u]);
+      if (late[u]) defer[ndef + __popc(dm & lt)] = q;
+      ndef += __popc(dm);
     }
 #pragma unroll
     for (int u = 0; u < kBinBatch; ++u)
@@ -164,12 +202,14 @@ __global__ void __launch_bounds__(kBinThreads) gbmv_bin_kernel(const float4* __r
       if (cell[u] >= 0 && cnt[u] > 0) {
         cp.cell[p] = (int)cell[u];
         cp.rank[p] = slot[u];
-      } else if (q < q1) {
+      } else if (q < q1 && !late[u]) {
         cp.cell[p] = -1;
         cp.sval[p] = empty_list_fraction<MODEL>(m);
       }
     }
+    if (ndef > kBinDefer - kBinBatch * kWarp) flush();
   }
+  if (ndef > 0) flush();
 }
 
 __global__ void gbmv_fill_kernel(long long npts, CellPoints cp) {

@@ -87,6 +87,14 @@ struct RefQuery {
     init(*t.geom, xi, qo, usable_cells(t));
   }
   __device__ __forceinline__ long long cell(const float4 xi, const float4 v, int q) const {
+    bool unsafe;
+    const long long c = cell_fast(v, unsafe);
+    return unsafe ? query_exact(*g, xi, qoff, q) : c;
+  }
+  // The FP32 query alone; unsafe: the point lies within the guard band of a
+  // cell face or grid edge and needs the exact query (the result is then -1).
+  __device__ __forceinline__ long long cell_fast(const float4 v, bool& unsafe) const {
+    unsafe = false;
     if (off) return -1;
     const TableGeom& G = *g;
     float t[3] = {fmaf(v.x, inv[0], rel[0]), fmaf(v.y, inv[1], rel[1]), fmaf(v.z, inv[2], rel[2])};
@@ -115,7 +123,10 @@ struct RefQuery {
         if (t[k] < eps || t[k] > (float)(G.dims[k] - 1) - eps) safe = false;
       }
     }
-    if (!safe) return query_exact(G, xi, qoff, q);
+    if (!safe) {
+      unsafe = true;
+      return -1;
+    }
     return (long long)id[0] * ((long long)G.dims[1] * G.dims[2]) + (long long)id[1] * G.dims[2] + id[2];
   }
   // x_j - p formed as (x_j - x_i) - v: the FP32 difference of nearby atoms is exact
