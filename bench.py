@@ -76,11 +76,16 @@ FLOPS_GBMV_CHAIN_POINT = 5.0
 FLOPS_PAIR = 39.0
 
 
-# DRAM bytes (read + write) per launch of each stage's main kernel, from one ncu
-# capture of the same workload (the files named in TRAFFIC_SOURCE).
-TRAFFIC = {"gbsw50k": {"integrals": 1641.7e6 + 715.4e6, "pair": 3.04e6 + 0.04e6, "chain_rule": 1089.6e6 + 0.07e6},
-           "gbmv10k": {"integrals": 129.6e6 + 213.7e6, "chain_rule": 317.1e6 + 5.6e6}}
-TRAFFIC_SOURCE = {"gbsw50k": "profiles/kernels_gbsw50k.md", "gbmv10k": "profiles/gbmv_kernels_gbmv10k.md"}
+# DRAM bytes (read + write) per step of each stage's kernels, from one ncu
+# capture of the same workload and build (the files named in TRAFFIC_SOURCE).
+TRAFFIC = {"gbsw50k": {"integrals": 2353.1e6, "pair": 3.09e6 + 3.03e6, "chain_rule": 1089.3e6,
+                       "lookup_table": 180.0e6 + 146.6e6 + 5.5e6 + 9.6e6},
+           "gbmv10k": {"integrals": 405.2e6 + 48.0e6, "chain_rule": 291.7e6, "point_binning": 89.0e6 + 145.2e6,
+                       "pair": 0.63e6 + 0.63e6},
+           "gbmv1_10k": {"integrals": 211.4e6 + 48.0e6, "chain_rule": 127.4e6, "point_binning": 85.8e6 + 144.0e6,
+                         "pair": 0.63e6 + 0.62e6}}
+TRAFFIC_SOURCE = {"gbsw50k": "profiles/launches_gbsw50k.md", "gbmv10k": "profiles/launches_gbmv10k.md",
+                  "gbmv1_10k": "profiles/launches_gbmv1_10k.md"}
 
 
 def workloads():

@@ -128,14 +128,17 @@ __global__ void tight_members_kernel(TightArgs a) {
   const TableGeom& g = *a.geom;
   if (g.ncell > a.cell_cap) return;
   const float h = (float)g.step[0];
-  const float inv_h = (float)(1.0 / g.step[0]);
+  const float inv_h = (float)g.inv_step[0];
   const float eps = (float)g.pad;
   const long long sx = (long long)g.dims[1] * g.dims[2], sy = g.dims[2];
   for (int at = warp; at < a.n; at += (gridDim.x * blockDim.x) / kWarp) {
     const float4 p = a.pos[at];
-    // coordinates relative to the grid origin
-    const float x[3] = {(float)((double)p.x - g.min[0]), (float)((double)p.y - g.min[1]),
-                        (float)((double)p.z - g.min[2])};
+    // coordinates relative to the grid origin, lane k forming axis k in
+    // FP64 (the slow FP64 pipe is then busy for one instruction, not three)
+    float xk = 0.0f;
+    if (lane < 3) xk = (float)((double)(lane == 0 ? p.x : (lane == 1 ? p.y : p.z)) - g.min[lane]);
+    const float x[3] = {__shfl_sync(0xffffffffu, xk, 0), __shfl_sync(0xffffffffu, xk, 1),
+                        __shfl_sync(0xffffffffu, xk, 2)};
     const float reach = p.w + a.w + eps;
     const float bury = p.w - a.w - eps;
     int b[3], e[3];

@@ -79,6 +79,34 @@ def test_modified_set_vs_oracle(glob, cls, cutoff):
     ctx.close()
 
 
+@pytest.mark.parametrize("cls", ["gbmv2", "gbsw_integral"])
+def test_modified_set_cutoff_periodic_vs_oracle(cls):
+    """The modified set under CutoffPeriodic: integrals on the box-sampled
+    table with minimum-image point distances, pair terms by minimum image,
+    in a box barely wider than twice the cutoff (the box changes the
+    result)."""
+    from openmmcustomgbintegralforce_gb300.spec import TABLE_PERIODIC
+
+    g = make_globule(600, seed=23)
+    pos = g.positions - g.positions.min(axis=0)
+    box = (2.8, 2.8, 2.9)
+    if cls == "gbmv2":
+        m = GBModel.gbmv2(box=box, cutoff=1.3, periodic=True)
+    else:
+        m = GBModel.gbsw_integral(box=box, cutoff=1.3, periodic=True, table_mode=TABLE_PERIODIC)
+    P = modified_params(g)
+    ctx = CustomContext(m, g.n, MODIFIED)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(pos)
+    ref = CustomOracle(m, MODIFIED).energy_forces(pos, P)
+    print(f"{cls} periodic: energy {abs(E / ref['energy'] - 1):.2e} forces {rel_rms(F, ref['forces']):.2e}")
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    flat = CustomOracle(m.replace(periodic=False), MODIFIED).energy_forces(pos, P)
+    assert abs(flat["energy"] / ref["energy"] - 1) > 1e-4
+    ctx.close()
+
+
 def test_global_update(glob):
     g = glob
     m = model_of("gbmv2", g)
