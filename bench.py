@@ -611,6 +611,64 @@ def measure_config(name, steps, jitter_A, dev, flush):
     return res
 
 
+def measure_custom(dev, flush, steps: int = 50):
+    """The compiled-expression path (gbx_create_custom) at the GBMV-II 10k
+    configuration: the canonical CHARMM set written as user expressions,
+    against the fixed kernels on the same input (the results agree to FP32
+    rounding), and a modified set outside it; device evals/s from CUDA events
+    around each call (L2 flushed between calls) and e2e through host arrays."""
+    import torch
+
+    from openmmcustomgbintegralforce_gb300._lib import EXEC_CHECK, EXEC_ENERGY, EXEC_FORCES, Context, CustomContext
+    from openmmcustomgbintegralforce_gb300.expression_sets import CANONICAL, MODIFIED, modified_params
+
+    w = workloads()["gbmv10k"]
+    g = make_globule(w["n"], seed=w["seed"])
+    model = model_for(w, g)
+    n = g.n
+    ctxs = {"fixed": Context(model, n), "canonical_expressions": CustomContext(model, n, CANONICAL),
+            "modified_expressions": CustomContext(model, n, MODIFIED)}
+    ctxs["fixed"].set_particle_parameters(g.charge, g.radius)
+    ctxs["canonical_expressions"].set_custom_parameters(np.stack([g.charge, g.radius], axis=1))
+    ctxs["modified_expressions"].set_custom_parameters(modified_params(g))
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    posq = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    posq[:, :3] = torch.from_numpy(g.positions.astype(np.float32)).to(dev)
+    force = torch.zeros(3 * n, dtype=torch.int64, device=dev)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    out = {}
+    host = {}
+    for name, ctx in ctxs.items():
+        for _ in range(3):
+            ctx.execute_device(posq.data_ptr(), force.data_ptr(), n, energy.data_ptr(),
+                               EXEC_FORCES | EXEC_ENERGY | EXEC_CHECK, sptr)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for a, b in ev:
+                flush.fill_(1.0)
+                a.record(stream)
+                ctx.execute_device(posq.data_ptr(), force.data_ptr(), n, energy.data_ptr(), EXEC_FORCES | EXEC_ENERGY,
+                                   sptr)
+                b.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        ctx.execute_host(g.positions)
+        t = []
+        for _ in range(10):
+            t0 = time.perf_counter()
+            host[name] = ctx.execute_host(g.positions)
+            t.append(time.perf_counter() - t0)
+        out[name] = {"evals_per_s": 1000.0 / ms, "ms_per_step": ms, "e2e_evals_per_s": 1.0 / float(np.mean(t))}
+    (E0, F0), (E1, F1) = host["fixed"], host["canonical_expressions"]
+    out["canonical_expressions"]["vs_fixed_kernels"] = {"energy_rel": abs(E1 / E0 - 1.0), "force_rel_rms": rel_rms(F1, F0)}
+    for c in ctxs.values():
+        c.close()
+    return {"workload": "gbmv10k through gbx_create_custom", "desc": w["desc"], "atoms": n, **out,
+            "parity": "the modified set against the FP64 expression oracle: tests/test_gpu_custom.py"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -743,6 +801,7 @@ def main():
             line["batched"] = measure_batched(batch_set, max(3, min(args.steps, 10)))
         if not args.no_configs and world == 1:
             line["configs"] = {k: measure_config(wl, st, jit, dev, flush) for k, (wl, st, jit) in CONFIG_RUNS.items()}
+            line["configs"]["f2_compiled_expressions_gbmv2_10k"] = measure_custom(dev, flush)
         print(json.dumps(line))
 
 

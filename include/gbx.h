@@ -147,13 +147,18 @@ GBX_API gbx_status gbx_set_particle_parameters(gbx_context* ctx, const double* c
  * CharmmReferenceGBMV.cpp:151-444 on the CPU): the expressions and their
  * derivatives are compiled for the device when the context is created (NVRTC,
  * loaded at run time).  Variables: per-particle parameters, globals, the GB
- * integrals and earlier computed values by name; pair terms read r and every
- * per-particle quantity with the suffix 1 or 2 (atom 1 is the lower index).
- * One or two integrals; computed values are SingleParticle; pair terms run
- * over every pair (no exclusions).  Per-particle parameters must include
- * "radius" (GBSWIntegral.cpp:79-80).  gbx_adjoint is not available here.
+ * integrals and earlier computed values by name, and in computed values and
+ * single-particle terms the particle's coordinates x, y, z (their gradients
+ * become forces, CharmmReferenceGBMV.cpp:232-262,409-435); pair terms read r
+ * and every per-particle quantity with the suffix 1 or 2 (atom 1 is the
+ * lower index).  GBX_TERM_PAIR terms skip the excluded pairs,
+ * GBX_TERM_PAIR_NO_EXCLUSIONS terms do not (CharmmReferenceGBMV.cpp:196-200).
+ * One or two integrals; computed values are SingleParticle.  Per-particle
+ * parameters must include "radius" (GBSWIntegral.cpp:79-80); x, y and z name
+ * no parameter or global.  gbx_adjoint is not available here.  Zero-fill
+ * the struct before setting it: fields added later default to none.
  * ------------------------------------------------------------------------ */
-enum { GBX_TERM_SINGLE = 0, GBX_TERM_PAIR = 1 };
+enum { GBX_TERM_SINGLE = 0, GBX_TERM_PAIR = 1, GBX_TERM_PAIR_NO_EXCLUSIONS = 2 };
 typedef struct {
   int num_params;
   const char* const* param_names;
@@ -169,6 +174,10 @@ typedef struct {
   int num_terms;
   const char* const* term_expressions;
   const int* term_types; /* GBX_TERM_* */
+  int num_exclusions;    /* addExclusion (CharmmGBMVForce.h:416) */
+  const int* exclusions; /* [num_exclusions][2] particle pairs */
+  int num_param_derivs;  /* addEnergyParameterDerivative (CharmmGBMVForce.h:258): globals whose */
+  const char* const* param_deriv_names; /* energy derivative gbx_get_custom_param_derivs reports */
 } gbx_custom;
 
 GBX_API gbx_status gbx_create_custom(const gbx_config* cfg, int num_atoms, const gbx_custom* custom,
@@ -176,6 +185,9 @@ GBX_API gbx_status gbx_create_custom(const gbx_config* cfg, int num_atoms, const
 /* Per-particle parameters [num_atoms][num_params] (the radius among them). */
 GBX_API gbx_status gbx_set_custom_parameters(gbx_context* ctx, const double* params);
 GBX_API gbx_status gbx_set_custom_global(gbx_context* ctx, const char* name, double value);
+/* dE/dg of the last execute for each global named in param_deriv_names, in
+ * that order (synchronises the context's stream). */
+GBX_API gbx_status gbx_get_custom_param_derivs(gbx_context* ctx, double* out, int count);
 /* Checks an expression set without a device: parses it, checks every
  * variable and compiles the generated code.  On failure `log` (may be NULL)
  * receives the reason. */

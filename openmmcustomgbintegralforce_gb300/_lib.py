@@ -31,7 +31,7 @@ EXPORTED = (
     "gbx_get_born_radii", "gbx_get_integrals", "gbx_get_dEdB", "gbx_build_lookup_table", "gbx_get_lookup_table",
     "gbx_adjoint_host", "gbx_adjoint", "gbx_get_work", "gbx_get_chain_work", "gbx_set_chain_records",
     "gbx_get_chain_records", "gbx_get_launches", "gbx_set_timing", "gbx_get_stage_times", "gbx_pair_noalloc",
-    "gbx_create_custom", "gbx_set_custom_parameters", "gbx_set_custom_global", "gbx_custom_check",
+    "gbx_create_custom", "gbx_get_custom_param_derivs", "gbx_set_custom_parameters", "gbx_set_custom_global", "gbx_custom_check",
     "gbx_batch_create", "gbx_batch_destroy", "gbx_batch_molecule", "gbx_batch_buffers", "gbx_batch_execute",
     "gbx_batch_execute_host", "gbx_batch_adjoint", "gbx_batch_adjoint_host", "gbx_batch_tune",
     "gbx_batch_last_error",
@@ -134,6 +134,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.gbx_set_box.argtypes = [vp, vp]
     L.gbx_set_atom_order.argtypes = [vp, vp]
     L.gbx_create_custom.argtypes = [vp, ci, vp, vp]
+    L.gbx_get_custom_param_derivs.argtypes = [vp, vp, ci]
     L.gbx_set_custom_parameters.argtypes = [vp, vp]
     L.gbx_set_custom_global.argtypes = [vp, ctypes.c_char_p, cd]
     L.gbx_custom_check.argtypes = [vp, ctypes.c_char_p, sz]
@@ -353,10 +354,12 @@ class GbxCustom(ctypes.Structure):
         ("value_expressions", ctypes.POINTER(ctypes.c_char_p)),
         ("num_terms", ctypes.c_int), ("term_expressions", ctypes.POINTER(ctypes.c_char_p)),
         ("term_types", ctypes.POINTER(ctypes.c_int)),
+        ("num_exclusions", ctypes.c_int), ("exclusions", ctypes.POINTER(ctypes.c_int)),
+        ("num_param_derivs", ctypes.c_int), ("param_deriv_names", ctypes.POINTER(ctypes.c_char_p)),
     ]
 
 
-TERM_SINGLE, TERM_PAIR = 0, 1
+TERM_SINGLE, TERM_PAIR, TERM_PAIR_NO_EXCLUSIONS = 0, 1, 2
 
 
 def custom_struct(custom: dict):
@@ -390,7 +393,14 @@ def custom_struct(custom: dict):
     c.term_expressions = strs([e for e, _ in terms])
     tt = (ctypes.c_int * max(1, len(terms)))(*[int(t) for _, t in terms])
     c.term_types = tt
-    keep += [gv, io, tt]
+    ex = [int(v) for pair in custom.get("exclusions", []) for v in pair]
+    ea = (ctypes.c_int * max(1, len(ex)))(*ex)
+    c.num_exclusions = len(ex) // 2
+    c.exclusions = ea
+    pd = list(custom.get("param_derivs", []))
+    c.num_param_derivs = len(pd)
+    c.param_deriv_names = strs(pd)
+    keep += [gv, io, tt, ea]
     return c, keep
 
 
@@ -409,7 +419,10 @@ class CustomContext(Context):
     (gbx_create_custom): ``custom`` is a dict with ``params`` (names, one of
     them "radius"), ``globals`` ({name: value}), ``integrals`` ([(name,
     order)]), ``values`` ([(name, expression)]) and ``terms`` ([(expression,
-    TERM_SINGLE | TERM_PAIR)]).  The integral class, quadrature and table
+    TERM_SINGLE | TERM_PAIR | TERM_PAIR_NO_EXCLUSIONS)]), and optionally
+    ``exclusions`` ([(i, j)], skipped by TERM_PAIR terms) and
+    ``param_derivs`` ([global names] whose energy derivative
+    ``param_derivs()`` returns).  The integral class, quadrature and table
     come from ``model``."""
 
     def __init__(self, model: GBModel, num_atoms: int, custom: dict):
@@ -432,6 +445,13 @@ class CustomContext(Context):
 
     def set_custom_global(self, name: str, value: float):
         self._check(self.lib.gbx_set_custom_global(self.h, name.encode(), float(value)))
+
+    def param_derivs(self):
+        """dE/dg of the last call for each global in ``custom["param_derivs"]``."""
+        k = len(self.custom.get("param_derivs", []))
+        out = np.zeros(max(1, k))
+        self._check(self.lib.gbx_get_custom_param_derivs(self.h, _p(out), k))
+        return out[:k]
 
 
 class Batch:

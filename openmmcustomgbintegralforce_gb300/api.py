@@ -346,7 +346,8 @@ def _check_canonical(force: CharmmGBMVForce):
     want_int = [("I4", [4]), ("I7", [7])]
     got_int = [(force.getGBIntegralParameters(k)[0], force.getGBIntegralParameters(k)[1][:1])
                for k in range(force.getNumGBIntegrals())]
-    ok = got_int == want_int and "q" in names
+    # energy parameter derivatives come from the compiled path only
+    ok = got_int == want_int and "q" in names and force.getNumEnergyParameterDerivatives() == 0
     ok = ok and [(_norm(n), _norm(e), t) for n, e, t in (force.getComputedValueParameters(k)
                                                           for k in range(force.getNumComputedValues()))] == \
         [("B", _norm(CANONICAL_BORN), SingleParticle)]
@@ -360,11 +361,12 @@ def _check_canonical(force: CharmmGBMVForce):
 
 
 def custom_spec(force: CharmmGBMVForce) -> dict:
-    """The force's expressions as a gbx_create_custom description (computed
-    values SingleParticle; energy terms SingleParticle or pair without
-    exclusions)."""
-    if force.getNumExclusions() or force.getNumTabulatedFunctions():
-        raise GBXError(4, "exclusions and tabulated functions are not supported by the compiled expressions")
+    """The force's expressions as a gbx_create_custom description: computed
+    values SingleParticle; energy terms SingleParticle, ParticlePair (skips
+    the force's exclusions) or ParticlePairNoExclusions; the globals named
+    by addEnergyParameterDerivative."""
+    if force.getNumTabulatedFunctions():
+        raise GBXError(4, "tabulated functions are not supported by the compiled expressions")
     if force.getGBIntegralType() == CustomIntegral:
         raise GBXError(4, "CustomIntegral has no implementation")
     names = [force.getPerParticleParameterName(i) for i in range(force.getNumPerParticleParameters())]
@@ -387,10 +389,13 @@ def custom_spec(force: CharmmGBMVForce) -> dict:
     terms = []
     for k in range(force.getNumEnergyTerms()):
         expr, t = force.getEnergyTermParameters(k)
-        terms.append((expr, 0 if t == SingleParticle else 1))
+        terms.append((expr, {SingleParticle: 0, ParticlePair: 1, ParticlePairNoExclusions: 2}[t]))
     globals_ = {force.getGlobalParameterName(k): force.getGlobalParameterDefaultValue(k)
                 for k in range(force.getNumGlobalParameters())}
-    return {"params": names, "globals": globals_, "integrals": integrals, "values": values, "terms": terms}
+    return {"params": names, "globals": globals_, "integrals": integrals, "values": values, "terms": terms,
+            "exclusions": [force.getExclusionParticles(k) for k in range(force.getNumExclusions())],
+            "param_derivs": [force.getEnergyParameterDerivativeName(k)
+                             for k in range(force.getNumEnergyParameterDerivatives())]}
 
 
 class CalcCharmmGBSWForceKernel:
@@ -514,3 +519,10 @@ class CalcCharmmGBMVForceKernel:
 
     def execute(self, positions, includeForces: bool = True, includeEnergy: bool = True):
         return self.ctx.execute_host(positions, forces=includeForces, energy=includeEnergy)
+
+    def getEnergyParameterDerivatives(self) -> dict:
+        """dE/dg of the last execute for each global the force named with
+        addEnergyParameterDerivative (State.getEnergyParameterDerivatives)."""
+        if self.custom is None or not self.custom["param_derivs"]:
+            return {}
+        return dict(zip(self.custom["param_derivs"], (float(v) for v in self.ctx.param_derivs())))

@@ -472,7 +472,7 @@ gbx_status run_pipeline(Context* ctx, const float4* posq, unsigned long long* fo
     GBX_TRY(mark());
     GBX_TRY(gbx::launch_custom_energy(ctx, ctx->d_pos, force, stride));
     GBX_TRY(mark());
-    GBX_TRY(gbx::launch_custom_chain_prep(ctx));
+    GBX_TRY(gbx::launch_custom_chain_prep(ctx, force, stride));
     GBX_TRY(mark());
     if (chain) GBX_TRY(gbx::launch_chain(ctx, ctx->d_pos, force, stride, false));
     GBX_TRY(mark());
@@ -876,10 +876,28 @@ gbx_status custom_spec_of(const gbx_custom* cu, gbx::gbx_custom_spec& spec, std:
   }
   for (int k = 0; k < cu->num_terms; ++k) {
     spec.term_expressions.push_back(str(cu->term_expressions[k]));
-    if (cu->term_types[k] != GBX_TERM_SINGLE && cu->term_types[k] != GBX_TERM_PAIR)
+    if (cu->term_types[k] != GBX_TERM_SINGLE && cu->term_types[k] != GBX_TERM_PAIR &&
+        cu->term_types[k] != GBX_TERM_PAIR_NO_EXCLUSIONS)
       return why = "unknown energy term type", GBX_ERR_INVALID_ARGUMENT;
     spec.term_types.push_back(cu->term_types[k]);
   }
+  if (cu->num_exclusions < 0 || (cu->num_exclusions > 0 && !cu->exclusions) || cu->num_param_derivs < 0 ||
+      (cu->num_param_derivs > 0 && !cu->param_deriv_names))
+    return why = "exclusions and parameter derivatives need their arrays", GBX_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < cu->num_exclusions; ++k) {
+    spec.exclusions.push_back(cu->exclusions[2 * k]);
+    spec.exclusions.push_back(cu->exclusions[2 * k + 1]);
+  }
+  for (int k = 0; k < cu->num_param_derivs; ++k) {
+    spec.param_derivs.push_back(str(cu->param_deriv_names[k]));
+    if (std::find(spec.globals.begin(), spec.globals.end(), spec.param_derivs.back()) == spec.globals.end())
+      return why = "energy parameter derivative of an unknown global '" + spec.param_derivs.back() + "'",
+             GBX_ERR_INVALID_ARGUMENT;
+  }
+  for (const auto* names : {&spec.params, &spec.globals})
+    for (const auto& nm : *names)
+      if (nm == "x" || nm == "y" || nm == "z")
+        return why = "x, y and z are the particle's coordinates, not parameter names", GBX_ERR_INVALID_ARGUMENT;
   if (std::find(spec.params.begin(), spec.params.end(), std::string("radius")) == spec.params.end())
     return why = "the per-particle parameter 'radius' must be defined", GBX_ERR_INVALID_ARGUMENT;
   return GBX_OK;
@@ -887,6 +905,17 @@ gbx_status custom_spec_of(const gbx_custom* cu, gbx::gbx_custom_spec& spec, std:
 }  // namespace
 
 extern "C" {
+
+gbx_status gbx_get_custom_param_derivs(gbx_context* handle, double* out, int count) {
+  Context* ctx = reinterpret_cast<Context*>(handle);
+  if (!ctx || !out || count < 0) return GBX_ERR_INVALID_ARGUMENT;
+  if (!ctx->custom) {
+    ctx->last_error = "parameter derivatives belong to the compiled-expression path";
+    return GBX_ERR_UNSUPPORTED;
+  }
+  if (!ctx->have_result) return GBX_ERR_NOT_READY;
+  return gbx::custom_param_derivs(ctx, out, count);
+}
 
 gbx_status gbx_custom_check(const gbx_custom* cu, char* log, size_t len) {
   gbx::gbx_custom_spec spec;

@@ -116,6 +116,11 @@ struct CustomArgs {
   double* born;              // [n] the first computed value (reported)
   unsigned long long* dEdB;  // [n] dE/d(first computed value), fixed point
   unsigned* status;
+  double* dVdX;              // [nv][3][n] total derivatives of the values by the particle's coordinates
+  const int* excl_start;     // [n + 1] each particle's excluded partners (CSR, ascending)
+  const int* excl;
+  double* dVdG;              // [nv][npd][n] total derivatives of the values by the requested globals
+  double* pd_part;           // [blocks][npd] per-block energy derivatives by the requested globals
 };
 )";
 
@@ -168,6 +173,14 @@ struct CustomPlan {
   double* d_dVdI = nullptr;
   unsigned long long* d_dEdV = nullptr;
   unsigned long long* d_dEdI = nullptr;
+  double* d_dVdX = nullptr;
+  int* d_excl_start = nullptr;
+  int* d_excl = nullptr;
+  double* d_dVdG = nullptr;
+  double* d_pd_part = nullptr;
+  bool coords = false;      // some computed value or single-particle term reads x, y or z
+  bool excluding = false;   // exclusions exist and some term honours them
+  std::vector<int> pd_index;  // requested globals, as indices into spec.globals
   int value_blocks = 0, pair_blocks = 0;
   std::string source;  // kept for diagnostics
 };
@@ -200,30 +213,42 @@ Names variable_names(const gbx_custom_spec& s) {
     nm.pair[s.value_names[k] + "1"] = "va" + std::to_string(k);
     nm.pair[s.value_names[k] + "2"] = "vb" + std::to_string(k);
   }
+  nm.single["x"] = "cx";
+  nm.single["y"] = "cy";
+  nm.single["z"] = "cz";
   nm.pair["r"] = "r";
   return nm;
 }
 
-const char* kReduceEnergy =
-    "  s_e[threadIdx.x] = e;\n  __syncthreads();\n"
-    "  for (int st = blockDim.x / 2; st > 0; st >>= 1) {\n"
-    "    if (threadIdx.x < st) s_e[threadIdx.x] += s_e[threadIdx.x + st];\n    __syncthreads();\n  }\n"
-    "  if (threadIdx.x == 0) a.energy_part[blockIdx.x] = s_e[0];\n}\n\n";
+// Per-block reduction of a double held by every thread into out[blockIdx.x * stride + k].
+std::string block_sum(const std::string& v, const std::string& out) {
+  return "  s_e[threadIdx.x] = " + v + ";\n  __syncthreads();\n"
+         "  for (int st = blockDim.x / 2; st > 0; st >>= 1) {\n"
+         "    if (threadIdx.x < st) s_e[threadIdx.x] += s_e[threadIdx.x + st];\n    __syncthreads();\n  }\n"
+         "  if (threadIdx.x == 0) " + out + " = s_e[0];\n  __syncthreads();\n";
+}
 
 std::string generate(const CustomPlan& p) {
   const gbx_custom_spec& s = p.spec;
   const int np = (int)s.params.size(), ng = (int)s.globals.size(), ni = (int)s.integrals.size(),
-            nv = (int)s.value_names.size();
+            nv = (int)s.value_names.size(), npd = (int)p.pd_index.size();
   const Names nm = variable_names(s);
+  const char* kCoord[3] = {"x", "y", "z"};
+  auto D = [](const expr::Ptr& e, const std::string& v) { return expr::derivative(e, v); };
   std::ostringstream o;
   o << kArgsDecl << kPrelude;
 
-  // ---- per-atom values, their derivatives by the integrals, single-particle terms
+  // ---- per-atom values, their derivatives, single-particle terms (FP64);
+  // every expression and derivative shares its common subexpressions
+  expr::SharedEmitter ve(nm.single, false, "s", "  ");
   o << "extern \"C\" __global__ void __launch_bounds__(" << kValueThreads << ") gbx_values(CustomArgs a) {\n";
   o << "  __shared__ double s_e[" << kValueThreads << "];\n";
-  o << "  const int i = blockIdx.x * blockDim.x + threadIdx.x;\n  double e = 0.0;\n  if (i < a.n) {\n";
+  o << "  const int i = blockIdx.x * blockDim.x + threadIdx.x;\n  double e = 0.0;\n";
+  for (int k = 0; k < npd; ++k) o << "  double pd" << k << " = 0.0;\n";
+  o << "  if (i < a.n) {\n";
   for (int k = 0; k < np; ++k) o << "  const double p" << k << " = a.params[" << k << " * a.n + i];\n";
   for (int k = 0; k < ng; ++k) o << "  const double g" << k << " = a.globals[" << k << "];\n";
+  if (p.coords) o << "  const float4 xp = a.pos[i];\n  const double cx = xp.x, cy = xp.y, cz = xp.z;\n";
   for (int k = 0; k < ni; ++k) {
     o << "  double J" << k << " = 0.0;\n";
     o << "  for (int c = 0; c < a.chunks; ++c) J" << k << " += (double)a.J[(" << k
@@ -231,39 +256,68 @@ std::string generate(const CustomPlan& p) {
     o << "  const double I" << k << " = a.S[" << k << "] - J" << k << ";\n";
     o << "  a.I[" << k << " * a.n + i] = I" << k << ";\n  a.If[" << k << " * a.n + i] = (float)I" << k << ";\n";
   }
+  // total derivative of value m by a variable: its partial plus the chain
+  // through the earlier values (forward mode)
+  auto total = [&](int m, const std::string& var, const std::string& prefix, const std::string& suffix) {
+    std::string t = ve(D(p.values[m], var));
+    for (int l = 0; l < m; ++l)
+      t += " + " + ve(D(p.values[m], s.value_names[l])) + " * " + prefix + std::to_string(l) + suffix;
+    return t;
+  };
   for (int m = 0; m < nv; ++m) {
-    o << "  const double v" << m << " = " << expr::emit(p.values[m], nm.single, false) << ";\n";
+    const std::string vm = ve(p.values[m]);
+    std::ostringstream body;
+    for (int k = 0; k < ni; ++k)
+      body << "  const double dv" << m << "_" << k << " = " << total(m, s.integrals[k], "dv", "_" + std::to_string(k))
+           << ";\n  a.dVdI[(" << m << " * " << ni << " + " << k << ") * a.n + i] = dv" << m << "_" << k << ";\n";
+    if (p.coords)
+      for (int c = 0; c < 3; ++c)
+        body << "  const double dx" << m << "_" << c << " = " << total(m, kCoord[c], "dx", "_" + std::to_string(c))
+             << ";\n  a.dVdX[(" << m << " * 3 + " << c << ") * a.n + i] = dx" << m << "_" << c << ";\n";
+    for (int k = 0; k < npd; ++k)
+      body << "  const double dg" << m << "_" << k << " = "
+           << total(m, s.globals[p.pd_index[k]], "dg", "_" + std::to_string(k)) << ";\n  a.dVdG[(" << m << " * "
+           << npd << " + " << k << ") * a.n + i] = dg" << m << "_" << k << ";\n";
+    o << ve.take_decls();
+    o << "  const double v" << m << " = " << vm << ";\n";
     o << "  a.V[" << m << " * a.n + i] = v" << m << ";\n  a.Vf[" << m << " * a.n + i] = (float)v" << m << ";\n";
-    for (int k = 0; k < ni; ++k) {
-      // total derivative: partial by I_k plus the chain through earlier values
-      o << "  const double dv" << m << "_" << k << " = "
-        << expr::emit(expr::derivative(p.values[m], s.integrals[k]), nm.single, false);
-      for (int l = 0; l < m; ++l)
-        o << " + " << expr::emit(expr::derivative(p.values[m], s.value_names[l]), nm.single, false) << " * dv" << l
-          << "_" << k;
-      o << ";\n  a.dVdI[(" << m << " * " << ni << " + " << k << ") * a.n + i] = dv" << m << "_" << k << ";\n";
-    }
+    o << body.str();
   }
   if (nv > 0) o << "  a.born[i] = v0;\n  if (!isfinite(v0)) atomicOr(a.status, 8u);\n";
   for (int m = 0; m < nv; ++m) o << "  double dEdV" << m << " = 0.0;\n";
   for (int k = 0; k < ni; ++k) o << "  double dEdI" << k << " = 0.0;\n";
-  for (size_t t = 0; t < p.terms.size(); ++t) {
-    if (p.term_types[t] != 0) continue;
-    o << "  e += " << expr::emit(p.terms[t], nm.single, false) << ";\n";
-    for (int m = 0; m < nv; ++m)
-      o << "  dEdV" << m << " += " << expr::emit(expr::derivative(p.terms[t], s.value_names[m]), nm.single, false)
-        << ";\n";
-    for (int k = 0; k < ni; ++k)
-      o << "  dEdI" << k << " += " << expr::emit(expr::derivative(p.terms[t], s.integrals[k]), nm.single, false)
-        << ";\n";
+  if (p.coords) o << "  double tfx = 0.0, tfy = 0.0, tfz = 0.0;\n";
+  {
+    std::ostringstream acc;
+    for (size_t t = 0; t < p.terms.size(); ++t) {
+      if (p.term_types[t] != 0) continue;
+      acc << "  e += " << ve(p.terms[t]) << ";\n";
+      for (int m = 0; m < nv; ++m) acc << "  dEdV" << m << " += " << ve(D(p.terms[t], s.value_names[m])) << ";\n";
+      for (int k = 0; k < ni; ++k) acc << "  dEdI" << k << " += " << ve(D(p.terms[t], s.integrals[k])) << ";\n";
+      if (p.coords) {
+        acc << "  tfx += " << ve(D(p.terms[t], "x")) << ";\n";
+        acc << "  tfy += " << ve(D(p.terms[t], "y")) << ";\n";
+        acc << "  tfz += " << ve(D(p.terms[t], "z")) << ";\n";
+      }
+      for (int k = 0; k < npd; ++k) acc << "  pd" << k << " += " << ve(D(p.terms[t], s.globals[p.pd_index[k]])) << ";\n";
+    }
+    o << ve.take_decls() << acc.str();
   }
   for (int m = 0; m < nv; ++m)
     o << "  a.dEdV[" << m << " * a.n + i] = (unsigned long long)gbx_fixed(dEdV" << m << ");\n";
   for (int k = 0; k < ni; ++k)
     o << "  a.dEdI[" << k << " * a.n + i] = (unsigned long long)gbx_fixed(dEdI" << k << ");\n";
-  o << "  }\n" << kReduceEnergy;
+  // a single-particle term's explicit coordinate dependence is a force on the particle
+  if (p.coords)
+    o << "  gbx_add_fixed(a.force + i, -tfx);\n  gbx_add_fixed(a.force + a.stride + i, -tfy);\n"
+         "  gbx_add_fixed(a.force + 2 * a.stride + i, -tfz);\n";
+  o << "  }\n" << block_sum("e", "a.energy_part[blockIdx.x]");
+  for (int k = 0; k < npd; ++k)
+    o << block_sum("pd" + std::to_string(k), "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
+  o << "}\n\n";
 
-  // ---- pair terms
+  // ---- pair terms (FP32, fast math); each thread sums its own particle's
+  // side of every pair it is in
   o << "extern \"C\" __global__ void __launch_bounds__(" << kPairThreads << ") gbx_pair(CustomArgs a) {\n";
   o << "  __shared__ float4 s_pos[" << kPairThreads << "];\n";
   if (np) o << "  __shared__ float s_p[" << np << "][" << kPairThreads << "];\n";
@@ -280,6 +334,9 @@ std::string generate(const CustomPlan& p) {
   o << "  float fx = 0.f, fy = 0.f, fz = 0.f;\n  double e = 0.0;\n";
   for (int k = 0; k < nv; ++k) o << "  float gV" << k << " = 0.f;\n";
   for (int k = 0; k < ni; ++k) o << "  float gI" << k << " = 0.f;\n";
+  for (int k = 0; k < npd; ++k) o << "  float pdp" << k << " = 0.f;\n";
+  // the particle's excluded partners, walked in step with j (both ascend)
+  if (p.excluding) o << "  int ex = own ? a.excl_start[i] : 0;\n  const int ex_end = own ? a.excl_start[i + 1] : 0;\n";
   o << "  for (int base = 0; base < a.n; base += " << kPairThreads << ") {\n";
   o << "    const int jl = base + threadIdx.x;\n    if (jl < a.n) {\n      s_pos[threadIdx.x] = a.pos[jl];\n";
   for (int k = 0; k < np; ++k) o << "      s_p[" << k << "][threadIdx.x] = a.paramsf[" << k << " * a.n + jl];\n";
@@ -287,7 +344,11 @@ std::string generate(const CustomPlan& p) {
   for (int k = 0; k < ni; ++k) o << "      s_I[" << k << "][threadIdx.x] = a.If[" << k << " * a.n + jl];\n";
   o << "    }\n    __syncthreads();\n";
   o << "    const int jn = min(" << kPairThreads << ", a.n - base);\n";
-  o << "    for (int t = 0; t < jn && own; ++t) {\n      const int j = base + t;\n      if (j == i) continue;\n";
+  o << "    for (int t = 0; t < jn && own; ++t) {\n      const int j = base + t;\n";
+  if (p.excluding)
+    o << "      while (ex < ex_end && a.excl[ex] < j) ++ex;\n"
+         "      const bool excluded = ex < ex_end && a.excl[ex] == j;\n";
+  o << "      if (j == i) continue;\n";
   o << "      const float4 xj = s_pos[t];\n";
   o << "      float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;\n";
   o << "      if (a.periodic) {\n        dx -= a.L[0] * floorf(dx * a.iL[0] + 0.5f);\n        dy -= a.L[1] * "
@@ -311,45 +372,78 @@ std::string generate(const CustomPlan& p) {
     o << "      const float Ia" << K << " = lo ? I" << K << "_i : s_I[" << K << "][t];\n";
     o << "      const float Ib" << K << " = lo ? s_I[" << K << "][t] : I" << K << "_i;\n";
   }
-  o << "      float dEdr = 0.f;\n";
-  for (size_t t = 0; t < p.terms.size(); ++t) {
-    if (p.term_types[t] != 1) continue;
-    o << "      if (lo) e += (double)(" << expr::emit(p.terms[t], nm.pair, true) << ");\n";
-    o << "      dEdr += " << expr::emit(expr::derivative(p.terms[t], "r"), nm.pair, true) << ";\n";
-    for (int k = 0; k < nv; ++k) {
-      const std::string n1 = s.value_names[k] + "1", n2 = s.value_names[k] + "2";
-      o << "      gV" << k << " += lo ? " << expr::emit(expr::derivative(p.terms[t], n1), nm.pair, true) << " : "
-        << expr::emit(expr::derivative(p.terms[t], n2), nm.pair, true) << ";\n";
+  {
+    expr::SharedEmitter pe(nm.pair, true, "u", "      ");
+    std::ostringstream acc;
+    acc << "      float dEdr = 0.f;\n";
+    for (size_t t = 0; t < p.terms.size(); ++t) {
+      if (p.term_types[t] == 0) continue;
+      // ParticlePair: an excluded pair contributes nothing
+      const bool skip = p.excluding && p.term_types[t] == 1;
+      auto W = [&](const std::string& x) { return skip ? "(excluded ? 0.f : " + x + ")" : x; };
+      acc << "      if (lo) e += (double)" << W(pe(p.terms[t])) << ";\n";
+      acc << "      dEdr += " << W(pe(D(p.terms[t], "r"))) << ";\n";
+      for (int k = 0; k < nv; ++k) {
+        const std::string n1 = s.value_names[k] + "1", n2 = s.value_names[k] + "2";
+        acc << "      gV" << k << " += " << W("(lo ? " + pe(D(p.terms[t], n1)) + " : " + pe(D(p.terms[t], n2)) + ")")
+            << ";\n";
+      }
+      for (int k = 0; k < ni; ++k) {
+        const std::string n1 = s.integrals[k] + "1", n2 = s.integrals[k] + "2";
+        acc << "      gI" << k << " += " << W("(lo ? " + pe(D(p.terms[t], n1)) + " : " + pe(D(p.terms[t], n2)) + ")")
+            << ";\n";
+      }
+      for (int k = 0; k < npd; ++k)
+        acc << "      if (lo) pdp" << k << " += " << W(pe(D(p.terms[t], s.globals[p.pd_index[k]]))) << ";\n";
     }
-    for (int k = 0; k < ni; ++k) {
-      const std::string n1 = s.integrals[k] + "1", n2 = s.integrals[k] + "2";
-      o << "      gI" << k << " += lo ? " << expr::emit(expr::derivative(p.terms[t], n1), nm.pair, true) << " : "
-        << expr::emit(expr::derivative(p.terms[t], n2), nm.pair, true) << ";\n";
-    }
+    o << pe.take_decls() << acc.str();
   }
   // F_i = -dE/dx_i = -(dE/dr) (x_i - x_j) / r
-  o << "      const float s = dEdr / r;\n      fx -= s * dx;\n      fy -= s * dy;\n      fz -= s * dz;\n";
+  o << "      const float sr = dEdr / r;\n      fx -= sr * dx;\n      fy -= sr * dy;\n      fz -= sr * dz;\n";
   o << "    }\n    __syncthreads();\n  }\n";
   o << "  if (own) {\n";
   o << "    gbx_add_fixed(a.force + i, (double)fx);\n    gbx_add_fixed(a.force + a.stride + i, (double)fy);\n"
        "    gbx_add_fixed(a.force + 2 * a.stride + i, (double)fz);\n";
   for (int k = 0; k < nv; ++k) o << "    gbx_add_fixed(a.dEdV + " << k << " * a.n + i, (double)gV" << k << ");\n";
   for (int k = 0; k < ni; ++k) o << "    gbx_add_fixed(a.dEdI + " << k << " * a.n + i, (double)gI" << k << ");\n";
-  o << "  }\n" << kReduceEnergy;
+  o << "  }\n" << block_sum("e", "a.energy_part[blockIdx.x]");
+  for (int k = 0; k < npd; ++k)
+    o << block_sum("(double)pdp" + std::to_string(k),
+                   "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
+  o << "}\n\n";
 
-  // ---- the integrals' adjoint for the chain rule
-  o << "extern \"C\" __global__ void gbx_chain(CustomArgs a) {\n";
-  o << "  const int i = blockIdx.x * blockDim.x + threadIdx.x;\n  if (i >= a.n) return;\n";
+  // ---- the integrals' adjoint for the chain rule; the values' explicit
+  // coordinate and global dependence
+  o << "extern \"C\" __global__ void __launch_bounds__(" << kValueThreads << ") gbx_chain(CustomArgs a) {\n";
+  if (npd) o << "  __shared__ double s_e[" << kValueThreads << "];\n";
+  o << "  const int i = blockIdx.x * blockDim.x + threadIdx.x;\n";
+  for (int k = 0; k < npd; ++k) o << "  double pd" << k << " = 0.0;\n";
+  o << "  if (i < a.n) {\n";
+  for (int m = 0; m < nv; ++m)
+    o << "  const double ev" << m << " = (double)(long long)a.dEdV[" << m << " * a.n + i] / 4294967296.0;\n";
   for (int k = 0; k < ni; ++k) {
     o << "  double t" << k << " = (double)(long long)a.dEdI[" << k << " * a.n + i] / 4294967296.0;\n";
     for (int m = 0; m < nv; ++m)
-      o << "  t" << k << " += (double)(long long)a.dEdV[" << m << " * a.n + i] / 4294967296.0 * a.dVdI[(" << m
-        << " * " << ni << " + " << k << ") * a.n + i];\n";
+      o << "  t" << k << " += ev" << m << " * a.dVdI[(" << m << " * " << ni << " + " << k << ") * a.n + i];\n";
   }
   // I = S - J: dE/dJ = -dE/dI
   o << "  a.dEdJ[i] = make_float2(" << (ni > 0 ? "(float)(-t0)" : "0.f") << ", "
     << (ni > 1 ? "(float)(-t1)" : "0.f") << ");\n";
   if (nv > 0) o << "  a.dEdB[i] = a.dEdV[i];\n";
+  if (p.coords && nv > 0) {
+    for (int c = 0; c < 3; ++c) {
+      o << "  double fc" << c << " = 0.0;\n";
+      for (int m = 0; m < nv; ++m)
+        o << "  fc" << c << " += ev" << m << " * a.dVdX[(" << m << " * 3 + " << c << ") * a.n + i];\n";
+      o << "  gbx_add_fixed(a.force + " << c << " * a.stride + i, -fc" << c << ");\n";
+    }
+  }
+  for (int k = 0; k < npd; ++k)
+    for (int m = 0; m < nv; ++m)
+      o << "  pd" << k << " += ev" << m << " * a.dVdG[(" << m << " * " << npd << " + " << k << ") * a.n + i];\n";
+  o << "  }\n";
+  for (int k = 0; k < npd; ++k)
+    o << block_sum("pd" + std::to_string(k), "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
   o << "}\n";
   return o.str();
 }
@@ -366,8 +460,9 @@ gbx_status compile(CustomPlan& p, std::string& err) {
     err = "nvrtcCreateProgram failed";
     return GBX_ERR_CUDA;
   }
-  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
-  const nvrtcResult cr = nv.compile(prog, 3, opts);
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--use_fast_math",
+                        "-diag-suppress=177"};
+  const nvrtcResult cr = nv.compile(prog, 5, opts);
   if (cr != NVRTC_SUCCESS) {
     size_t ls = 0;
     nv.log_size(prog, &ls);
@@ -418,6 +513,11 @@ struct CustomArgs {
   double* born;
   unsigned long long* dEdB;
   unsigned* status;
+  double* dVdX;
+  const int* excl_start;
+  const int* excl;
+  double* dVdG;
+  double* pd_part;
 };
 
 template <class T>
@@ -475,6 +575,45 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
     if (!check(plan->terms[t], plan->term_types[t] == 0 ? nm.single : nm.pair, "energy term",
                spec.value_names.size()))
       return GBX_ERR_INVALID_ARGUMENT;
+  // coordinates read by a computed value or a single-particle term
+  auto reads_coords = [](const expr::Ptr& e) {
+    std::vector<std::string> vars;
+    expr::variables(e, vars);
+    for (auto& v : vars)
+      if (v == "x" || v == "y" || v == "z") return true;
+    return false;
+  };
+  for (auto& e : plan->values) plan->coords = plan->coords || reads_coords(e);
+  for (size_t t = 0; t < plan->terms.size(); ++t)
+    if (plan->term_types[t] == 0) plan->coords = plan->coords || reads_coords(plan->terms[t]);
+  for (auto& g : spec.param_derivs)
+    plan->pd_index.push_back((int)(std::find(spec.globals.begin(), spec.globals.end(), g) - spec.globals.begin()));
+  bool pair_with_exclusions = false;
+  for (int t : plan->term_types) pair_with_exclusions = pair_with_exclusions || t == 1;
+  plan->excluding = !spec.exclusions.empty() && pair_with_exclusions;
+  // each particle's excluded partners, both directions, ascending
+  std::vector<int> excl_start, excl;
+  if (plan->excluding) {
+    const int n = ctx->n;
+    std::vector<std::vector<int>> per(n);
+    for (size_t k = 0; k + 1 < spec.exclusions.size(); k += 2) {
+      const int a = spec.exclusions[k], b = spec.exclusions[k + 1];
+      if (a < 0 || b < 0 || a >= n || b >= n || a == b) {
+        ctx->last_error = "exclusion of particles " + std::to_string(a) + " and " + std::to_string(b) +
+                          " is out of range";
+        return GBX_ERR_INVALID_ARGUMENT;
+      }
+      per[a].push_back(b);
+      per[b].push_back(a);
+    }
+    excl_start.push_back(0);
+    for (auto& v : per) {
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      excl.insert(excl.end(), v.begin(), v.end());
+      excl_start.push_back((int)excl.size());
+    }
+  }
   std::string err;
   try {
     const gbx_status s = compile(*plan, err);
@@ -500,6 +639,21 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_dVdI, (size_t)nv * ni * n));
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_dEdV, (size_t)nv * n));
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_dEdI, (size_t)ni * n));
+  const int npd = (int)plan->pd_index.size();
+  if (plan->coords) GBX_TRY_CUSTOM(alloc(ctx, &plan->d_dVdX, (size_t)nv * 3 * n));
+  if (npd) {
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_dVdG, (size_t)nv * npd * n));
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_pd_part, (size_t)(2 * plan->value_blocks + plan->pair_blocks) * npd));
+  }
+  if (plan->excluding) {
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl_start, excl_start.size()));
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl, excl.size()));
+    if (cudaMemcpy(plan->d_excl_start, excl_start.data(), sizeof(int) * excl_start.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        (!excl.empty() &&
+         cudaMemcpy(plan->d_excl, excl.data(), sizeof(int) * excl.size(), cudaMemcpyHostToDevice) != cudaSuccess))
+      return GBX_ERR_CUDA;
+  }
   const double S[2] = {ctx->S4, ctx->S7};  // the sums of the two integrals' weights
   if (cudaMemcpy(plan->d_S, S, sizeof(double) * ni, cudaMemcpyHostToDevice) != cudaSuccess ||
       (!spec.globals.empty() && cudaMemcpy(plan->d_globals, spec.global_values.data(),
@@ -513,7 +667,9 @@ void custom_destroy(Context* ctx) {
   CustomPlan* p = ctx->custom;
   if (!p) return;
   for (void* q : {(void*)p->d_params, (void*)p->d_paramsf, (void*)p->d_S, (void*)p->d_globals, (void*)p->d_V,
-                  (void*)p->d_Vf, (void*)p->d_If, (void*)p->d_dVdI, (void*)p->d_dEdV, (void*)p->d_dEdI})
+                  (void*)p->d_Vf, (void*)p->d_If, (void*)p->d_dVdI, (void*)p->d_dEdV, (void*)p->d_dEdI,
+                  (void*)p->d_dVdX, (void*)p->d_excl_start, (void*)p->d_excl, (void*)p->d_dVdG,
+                  (void*)p->d_pd_part})
     if (q) cudaFree(q);
   if (p->library) cudaLibraryUnload(p->library);
   delete p;
@@ -594,6 +750,11 @@ CustomArgs args_of(Context* ctx, const float4* pos, unsigned long long* force, i
   a.born = ctx->d_born;
   a.dEdB = ctx->d_dEdB_fx;
   a.status = ctx->d_status;
+  a.dVdX = p->d_dVdX;
+  a.excl_start = p->d_excl_start;
+  a.excl = p->d_excl;
+  a.dVdG = p->d_dVdG;
+  a.pd_part = p->d_pd_part;
   return a;
 }
 }  // namespace
@@ -607,6 +768,7 @@ gbx_status launch_custom_energy(Context* ctx, const float4* pos, unsigned long l
   if (e == cudaSuccess) {
     CustomArgs b = a;
     b.energy_part = ctx->d_energy_part + p->value_blocks;
+    if (b.pd_part) b.pd_part += (size_t)p->value_blocks * p->pd_index.size();
     void* bargs[] = {&b};
     e = cudaLaunchKernel((const void*)p->k_pair, dim3(p->pair_blocks), dim3(kPairThreads), bargs, 0, st);
   }
@@ -619,9 +781,10 @@ gbx_status launch_custom_energy(Context* ctx, const float4* pos, unsigned long l
   return GBX_OK;
 }
 
-gbx_status launch_custom_chain_prep(Context* ctx) {
+gbx_status launch_custom_chain_prep(Context* ctx, unsigned long long* force, int stride) {
   CustomPlan* p = ctx->custom;
-  CustomArgs a = args_of(ctx, ctx->d_pos, nullptr, ctx->n);
+  CustomArgs a = args_of(ctx, ctx->d_pos, force, stride);
+  if (a.pd_part) a.pd_part += (size_t)(p->value_blocks + p->pair_blocks) * p->pd_index.size();
   void* args[] = {&a};
   const cudaError_t e = cudaLaunchKernel((const void*)p->k_chain, dim3(p->value_blocks), dim3(kValueThreads), args,
                                          0, ctx->stream);
@@ -629,6 +792,27 @@ gbx_status launch_custom_chain_prep(Context* ctx) {
   if (e != cudaSuccess) {
     ctx->last_error = std::string("custom chain launch: ") + cudaGetErrorString(e);
     return GBX_ERR_CUDA;
+  }
+  return GBX_OK;
+}
+
+gbx_status custom_param_derivs(Context* ctx, double* out, int count) {
+  CustomPlan* p = ctx->custom;
+  const int npd = (int)p->pd_index.size();
+  if (count > npd) {
+    ctx->last_error = "more parameter derivatives asked for than were requested at creation";
+    return GBX_ERR_INVALID_ARGUMENT;
+  }
+  if (npd == 0) return GBX_OK;
+  const size_t parts = (size_t)(2 * p->value_blocks + p->pair_blocks);
+  std::vector<double> h(parts * npd);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+      cudaMemcpy(h.data(), p->d_pd_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  for (int k = 0; k < count; ++k) {
+    double v = 0.0;
+    for (size_t b = 0; b < parts; ++b) v += h[b * npd + k];  // fixed order: values, pairs, chain blocks
+    out[k] = v;
   }
   return GBX_OK;
 }
@@ -642,6 +826,19 @@ gbx_status custom_compile_only(const gbx_custom_spec& spec, std::string& log) {
     for (auto& e : spec.value_expressions) p.values.push_back(expr::parse(e));
     for (auto& e : spec.term_expressions) p.terms.push_back(expr::parse(e));
     p.term_types = spec.term_types;
+    auto reads_coords = [](const expr::Ptr& e) {
+      std::vector<std::string> vars;
+      expr::variables(e, vars);
+      for (auto& v : vars)
+        if (v == "x" || v == "y" || v == "z") return true;
+      return false;
+    };
+    for (auto& e : p.values) p.coords = p.coords || reads_coords(e);
+    for (size_t t = 0; t < p.terms.size(); ++t)
+      if (p.term_types[t] == 0) p.coords = p.coords || reads_coords(p.terms[t]);
+    for (auto& g : spec.param_derivs)
+      p.pd_index.push_back((int)(std::find(spec.globals.begin(), spec.globals.end(), g) - spec.globals.begin()));
+    for (int t : p.term_types) p.excluding = p.excluding || (t == 1 && !spec.exclusions.empty());
     const Nvrtc& nv = nvrtc();
     if (!nv.ok()) {
       log = "NVRTC could not be loaded";
@@ -651,8 +848,9 @@ gbx_status custom_compile_only(const gbx_custom_spec& spec, std::string& log) {
     nvrtcProgram prog;
     if (nv.create(&prog, p.source.c_str(), "gbx_custom.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
       return GBX_ERR_CUDA;
-    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
-    const nvrtcResult cr = nv.compile(prog, 3, opts);
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--use_fast_math",
+                          "-diag-suppress=177"};
+    const nvrtcResult cr = nv.compile(prog, 5, opts);
     size_t ls = 0;
     nv.log_size(prog, &ls);
     log.assign(ls, '\0');

@@ -402,5 +402,47 @@ std::string emit(const Ptr& e, const std::map<std::string, std::string>& rename,
   return number(0.0, fp32);
 }
 
+SharedEmitter::SharedEmitter(const std::map<std::string, std::string>& rename, bool fp32, std::string prefix,
+                             std::string indent)
+    : rename_(rename), fp32_(fp32), prefix_(std::move(prefix)), indent_(std::move(indent)) {}
+
+std::string SharedEmitter::take_decls() {
+  std::string d;
+  d.swap(decls_);
+  return d;
+}
+
+std::string SharedEmitter::operator()(const Ptr& e) { return node(e); }
+
+std::string SharedEmitter::node(const Ptr& e) {
+  if (e->op == Op::Const || e->op == Op::Var) return emit(e, rename_, fp32_);
+  auto hit = by_node_.find(e.get());
+  if (hit != by_node_.end()) return hit->second;
+  // the node's text over its children's names
+  std::vector<std::string> a;
+  for (auto& x : e->args) a.push_back(node(x));
+  std::vector<Ptr> leaves;
+  for (size_t k = 0; k < a.size(); ++k) leaves.push_back(variable("\x01" + std::to_string(k)));
+  std::map<std::string, std::string> rn;
+  for (size_t k = 0; k < a.size(); ++k) rn["\x01" + std::to_string(k)] = a[k];
+  Node shell = *e;
+  shell.args.clear();
+  for (size_t k = 0; k < e->args.size(); ++k)
+    shell.args.push_back(e->args[k]->op == Op::Const ? e->args[k] : leaves[k]);
+  const std::string text = emit(std::make_shared<const Node>(shell), rn, fp32_);
+  std::string name;
+  auto same = by_text_.find(text);
+  if (same != by_text_.end()) {
+    name = same->second;
+  } else {
+    name = prefix_ + std::to_string(by_text_.size());
+    by_text_[text] = name;
+    decls_ += indent_ + "const " + (fp32_ ? "float " : "double ") + name + " = " + text + ";\n";
+  }
+  by_node_[e.get()] = name;
+  keep_.push_back(e);
+  return name;
+}
+
 }  // namespace expr
 }  // namespace gbx

@@ -42,5 +42,28 @@ void variables(const Ptr& e, std::vector<std::string>& out);
 // float forms of the math functions.
 std::string emit(const Ptr& e, const std::map<std::string, std::string>& rename, bool fp32);
 
+// Emits several expressions with their common subexpressions formed once:
+// the first time a node's text appears it becomes a temporary
+// "const T <prefix><k> = ...;" appended to the pending declarations, and
+// later uses name the temporary.  take_decls() hands the pending
+// declarations to the caller, who writes them before the code that uses the
+// returned names (so expressions emitted later may reuse earlier ones).
+class SharedEmitter {
+ public:
+  SharedEmitter(const std::map<std::string, std::string>& rename, bool fp32, std::string prefix,
+                std::string indent);
+  std::string operator()(const Ptr& e);
+  std::string take_decls();
+
+ private:
+  std::string node(const Ptr& e);
+  const std::map<std::string, std::string>& rename_;
+  bool fp32_;
+  std::string prefix_, indent_, decls_;
+  std::map<const Node*, std::string> by_node_;
+  std::map<std::string, std::string> by_text_;
+  std::vector<Ptr> keep_;  // nodes whose address keys by_node_
+};
+
 }  // namespace expr
 }  // namespace gbx

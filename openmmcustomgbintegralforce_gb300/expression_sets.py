@@ -1,4 +1,5 @@
-"""Expression sets for the custom CharmmGBMVForce path (shared by tests).
+"""Example expression sets for the compiled CharmmGBMVForce path (used by the
+tests and the benchmark).
 
 CANONICAL is the canonical CHARMM set written as user expressions.  MODIFIED
 is outside it: a per-atom scale of the Born radius through a second computed
@@ -36,3 +37,35 @@ def modified_params(g, seed=0):
     rng = np.random.default_rng(seed)
     s = 0.9 + 0.2 * rng.random(g.n)
     return np.stack([g.charge, g.radius, s], axis=1)
+
+
+# Outside the canonical set in the ways the compiled path supports beyond
+# MODIFIED: a computed value and a single-particle term that read the atom's
+# coordinates (a slab-like dielectric scaling along z and a harmonic
+# restraint), a ParticlePair term (excluded pairs skipped) beside a
+# ParticlePairNoExclusions term, and energy derivatives by two globals.
+EXTENDED = {
+    "params": ["q", "radius"],
+    "globals": {"alpha0": -0.180, "alpha1": 1.817, "eps": 78.5, "kr": 2.0},
+    "integrals": [("I4", 4), ("I7", 7)],
+    "values": [("B", "1/(alpha0*(1/0.05-I4)+alpha1*(1/(4*0.05^4)-I7)^(1/4))"),
+               ("Bz", "B*(1+0.1*tanh(z-zc)); zc=1.3")],
+    "terms": [(f"-0.5*{K}*(1-1/eps)*q^2/Bz", 0),
+              ("kr*((x-1.2)^2+(y-1.3)^2)", 0),
+              (f"-{K}*(1-1/eps)*q1*q2/f; f=sqrt(r^2+Bz1*Bz2*exp(-r^2/(4*Bz1*Bz2)))", 1),
+              ("0.01*q1*q2/(r+0.3)", 2)],
+    "param_derivs": ["eps", "kr"],
+}
+
+
+def extended_exclusions(n, seed=0):
+    """Pairs of near neighbours in index order, as bonded exclusions would be."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = set()
+    for i in range(n - 1):
+        out.add((i, i + 1))
+        if i + 2 < n and rng.random() < 0.5:
+            out.add((i, i + 2))
+    return sorted(out)

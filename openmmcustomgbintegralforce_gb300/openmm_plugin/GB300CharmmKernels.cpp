@@ -185,8 +185,8 @@ bool isCanonicalGBMVForce(const CharmmGBMVForce& force, int& chargeIndex, int& r
     if (pi[0] < 2) throw OpenMMException("GBSWIntegral: the order of integral must be greater or equal to 2");
   }
   bool ok = chargeIndex >= 0 && force.getNumGBIntegrals() == 2 && force.getNumComputedValues() == 1 &&
-            force.getNumEnergyTerms() == 2 && force.getNumExclusions() == 0 &&
-            force.getNumTabulatedFunctions() == 0;
+            force.getNumEnergyTerms() == 2 && force.getNumTabulatedFunctions() == 0 &&
+            force.getNumEnergyParameterDerivatives() == 0;
   const char* integralNames[2] = {"I4", "I7"};
   const int orders[2] = {4, 7};
   for (int k = 0; ok && k < 2; ++k) {
@@ -253,11 +253,11 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     state.create(cfg, system.getNumParticles());
   } else {
     // the force's own expressions, compiled for the device
-    if (force.getNumExclusions() > 0 || force.getNumTabulatedFunctions() > 0)
-      throw OpenMMException("GB300: exclusions and tabulated functions are not supported");
+    if (force.getNumTabulatedFunctions() > 0)
+      throw OpenMMException("GB300: tabulated functions are not supported");
     std::vector<std::string> params, integrals, values, valueExprs, terms;
     std::vector<double> globalValues;
-    std::vector<int> orders, types;
+    std::vector<int> orders, types, exclusions;
     for (int k = 0; k < force.getNumPerParticleParameters(); ++k)
       params.push_back(force.getPerParticleParameterName(k));
     for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
@@ -286,7 +286,21 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
       CharmmGBMVForce::ComputationType type;
       force.getEnergyTermParameters(k, expr, type);
       terms.push_back(expr);
-      types.push_back(type == CharmmGBMVForce::SingleParticle ? GBX_TERM_SINGLE : GBX_TERM_PAIR);
+      types.push_back(type == CharmmGBMVForce::SingleParticle ? GBX_TERM_SINGLE
+                      : type == CharmmGBMVForce::ParticlePair ? GBX_TERM_PAIR
+                                                              : GBX_TERM_PAIR_NO_EXCLUSIONS);
+    }
+    for (int k = 0; k < force.getNumExclusions(); ++k) {
+      int a = 0, b = 0;
+      force.getExclusionParticles(k, a, b);
+      exclusions.push_back(a);
+      exclusions.push_back(b);
+    }
+    // the derivatives reach the context through the platform's workspace
+    // for derivatives formed outside its own kernels
+    for (int k = 0; k < force.getNumEnergyParameterDerivatives(); ++k) {
+      paramDerivNames.push_back(force.getEnergyParameterDerivativeName(k));
+      state.cu.addEnergyParameterDerivative(paramDerivNames.back());
     }
     auto ptrs = [](const std::vector<std::string>& v) {
       std::vector<const char*> p;
@@ -294,8 +308,8 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
       return p;
     };
     const auto pn = ptrs(params), gn = ptrs(globalNames), in = ptrs(integrals), vn = ptrs(values),
-               ve = ptrs(valueExprs), te = ptrs(terms);
-    gbx_custom cs;
+               ve = ptrs(valueExprs), te = ptrs(terms), pd = ptrs(paramDerivNames);
+    gbx_custom cs{};
     cs.num_params = (int)params.size();
     cs.param_names = pn.data();
     cs.num_globals = (int)globalNames.size();
@@ -310,6 +324,10 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     cs.num_terms = (int)terms.size();
     cs.term_expressions = te.data();
     cs.term_types = types.data();
+    cs.num_exclusions = (int)exclusions.size() / 2;
+    cs.exclusions = exclusions.data();
+    cs.num_param_derivs = (int)paramDerivNames.size();
+    cs.param_deriv_names = pd.data();
     state.createCustom(cfg, system.getNumParticles(), cs);
   }
   copyParameters(force);
@@ -347,7 +365,15 @@ double GB300CalcCharmmGBMVForceKernel::execute(OpenMM::ContextImpl& context, boo
   }
   const auto b = state.cu.getPeriodicBoxSize();  // double4: x, y, z edges
   state.setBox(b.x, b.y, b.z);
-  return state.execute(includeForces, includeEnergy);
+  const double e = state.execute(includeForces, includeEnergy);
+  if (!paramDerivNames.empty()) {
+    // read back after the step (this waits for the context's stream)
+    std::vector<double> d(paramDerivNames.size());
+    state.check(gbx_get_custom_param_derivs(state.handle, d.data(), (int)d.size()), "gbx_get_custom_param_derivs");
+    auto& workspace = state.cu.getEnergyParamDerivWorkspace();
+    for (size_t k = 0; k < d.size(); ++k) workspace[paramDerivNames[k]] += d[k];
+  }
+  return e;
 }
 
 void GB300CalcCharmmGBMVForceKernel::copyParametersToContext(OpenMM::ContextImpl&, const CharmmGBMVForce& force) {

@@ -83,6 +83,7 @@ class GB300CalcCharmmGBMVForceKernel : public OpenMM::CalcCharmmGBMVForceKernel 
   std::string alphaNames[2];
   bool custom = false;                    // expressions outside the canonical set
   std::vector<std::string> globalNames;   // the force's global parameters (custom)
+  std::vector<std::string> paramDerivNames;  // addEnergyParameterDerivative (custom)
 };
 
 // Whether the force uses the canonical CHARMM expression set (parameters q

@@ -65,7 +65,12 @@ def _ev(e, env, count):
 class CustomOracle:
     """``custom`` as for ``_lib.CustomContext``; ``model`` gives the integral
     class, quadrature and table (its ``orders`` are replaced by the
-    integrals')."""
+    integrals').  Term types: 0 single particle, 1 particle pair (excluded
+    pairs skipped, CharmmReferenceGBMV.cpp:272-284), 2 particle pair without
+    exclusions.  Computed values and single-particle terms may read the
+    atom's coordinates x, y, z (their gradients are forces,
+    CharmmReferenceGBMV.cpp:232-262,409-435); ``param_derivs`` names globals
+    whose energy derivative is returned (:225-229,263-264,438-443)."""
 
     def __init__(self, model, custom):
         self.custom = custom
@@ -76,8 +81,10 @@ class CustomOracle:
         self.integrals = [k for k, _ in custom["integrals"]]
         self.values = list(custom.get("values", []))
         self.terms = list(custom["terms"])
+        self.exclusions = [tuple(sorted(e)) for e in custom.get("exclusions", [])]
+        self.param_derivs = list(custom.get("param_derivs", []))
         vnames = [v for v, _ in self.values]
-        single_names = self.params + list(self.globals) + self.integrals + vnames
+        single_names = self.params + list(self.globals) + self.integrals + vnames + ["x", "y", "z"]
         pair_names = ["r"] + list(self.globals) + [f"{x}{s}" for x in self.params + self.integrals + vnames
                                                    for s in "12"]
         self.vexpr = [parse(e, single_names) for _, e in self.values]
@@ -95,22 +102,28 @@ class CustomOracle:
         env = {p: params[:, k] for k, p in enumerate(self.params)}
         env.update({g: np.full(n, v) for g, v in self.globals.items()})
         env.update({name: I[k] for k, name in enumerate(self.integrals)})
-        V, dVdI = [], []
+        env.update({"x": pos[:, 0], "y": pos[:, 1], "z": pos[:, 2]})
+        coords = ("x", "y", "z")
+        V, dVdI, dVdX, dVdG = [], [], [], []
         for m, (name, _) in enumerate(self.values):
             e = self.vexpr[m]
             V.append(_ev(e, env, n).copy())
-            d = []
-            for k in range(ni):  # total derivative: the partial plus the chain through earlier values
-                tot = _ev(sp.diff(e, sp.Symbol(self.integrals[k])), env, n).copy()
+
+            def total(var, earlier):  # the partial plus the chain through earlier values
+                t = _ev(sp.diff(e, sp.Symbol(var)), env, n).copy()
                 for l in range(m):
-                    tot += _ev(sp.diff(e, sp.Symbol(vnames[l])), env, n) * dVdI[l][k]
-                d.append(tot)
-            dVdI.append(d)
+                    t += _ev(sp.diff(e, sp.Symbol(vnames[l])), env, n) * earlier[l]
+                return t
+
+            dVdI.append([total(self.integrals[k], [d[k] for d in dVdI]) for k in range(ni)])
+            dVdX.append([total(c, [d[a] for d in dVdX]) for a, c in enumerate(coords)])
+            dVdG.append([total(g, [d[k] for d in dVdG]) for k, g in enumerate(self.param_derivs)])
             env[name] = V[-1]
         E = 0.0
         F = np.zeros((n, 3))
         dEdV = np.zeros((nv, n))
         dEdI = np.zeros((ni, n))
+        dEdG = np.zeros(len(self.param_derivs))
         for e, t in self.texpr:
             if t != 0:
                 continue
@@ -119,7 +132,11 @@ class CustomOracle:
                 dEdV[m] += _ev(sp.diff(e, sp.Symbol(v)), env, n)
             for k, name in enumerate(self.integrals):
                 dEdI[k] += _ev(sp.diff(e, sp.Symbol(name)), env, n)
-        pair_terms = [e for e, t in self.texpr if t == 1]
+            for a, c in enumerate(coords):
+                F[:, a] -= _ev(sp.diff(e, sp.Symbol(c)), env, n)
+            for k, g in enumerate(self.param_derivs):
+                dEdG[k] += float(_ev(sp.diff(e, sp.Symbol(g)), env, n).sum())
+        pair_terms = [(e, t) for e, t in self.texpr if t != 0]
         if pair_terms:
             a, b = np.triu_indices(n, k=1)  # atom 1 = a < atom 2 = b
             d = pos[a] - pos[b]
@@ -128,30 +145,42 @@ class CustomOracle:
                 d -= L * np.floor(d / L + 0.5)
             r = np.sqrt((d ** 2).sum(axis=1))
             keep = r < self.model.cutoff if self.model.cutoff > 0 else np.ones(len(r), bool)
-            a, b, d, r = a[keep], b[keep], d[keep], r[keep]
-            m_ = len(r)
-            penv = {"r": r}
-            penv.update({g: np.full(m_, v) for g, v in self.globals.items()})
-            for x in self.params + self.integrals + vnames:
-                arr = env[x]
-                penv[x + "1"] = arr[a]
-                penv[x + "2"] = arr[b]
-            for e in pair_terms:
+            excluded = np.zeros(len(r), bool)
+            if self.exclusions:
+                ex = {i * n + j for i, j in self.exclusions}
+                excluded = np.fromiter((int(i) * n + int(j) in ex for i, j in zip(a, b)), bool, count=len(a))
+            for e, t in pair_terms:
+                sel = keep & ~excluded if t == 1 else keep
+                aa, bb, dd, rr = a[sel], b[sel], d[sel], r[sel]
+                m_ = len(rr)
+                penv = {"r": rr}
+                penv.update({g: np.full(m_, v) for g, v in self.globals.items()})
+                for x in self.params + self.integrals + vnames:
+                    arr = env[x]
+                    penv[x + "1"] = arr[aa]
+                    penv[x + "2"] = arr[bb]
                 E += float(_ev(e, penv, m_).sum())
-                g = _ev(sp.diff(e, sp.Symbol("r")), penv, m_) / r
-                fpair = -g[:, None] * d  # force on atom 1 (d = x1 - x2)
-                np.add.at(F, a, fpair)
-                np.add.at(F, b, -fpair)
-                for m, v in enumerate(vnames):
-                    np.add.at(dEdV[m], a, _ev(sp.diff(e, sp.Symbol(v + "1")), penv, m_))
-                    np.add.at(dEdV[m], b, _ev(sp.diff(e, sp.Symbol(v + "2")), penv, m_))
+                g = _ev(sp.diff(e, sp.Symbol("r")), penv, m_) / rr
+                fpair = -g[:, None] * dd  # force on atom 1 (d = x1 - x2)
+                np.add.at(F, aa, fpair)
+                np.add.at(F, bb, -fpair)
+                for mm, v in enumerate(vnames):
+                    np.add.at(dEdV[mm], aa, _ev(sp.diff(e, sp.Symbol(v + "1")), penv, m_))
+                    np.add.at(dEdV[mm], bb, _ev(sp.diff(e, sp.Symbol(v + "2")), penv, m_))
                 for k, name in enumerate(self.integrals):
-                    np.add.at(dEdI[k], a, _ev(sp.diff(e, sp.Symbol(name + "1")), penv, m_))
-                    np.add.at(dEdI[k], b, _ev(sp.diff(e, sp.Symbol(name + "2")), penv, m_))
+                    np.add.at(dEdI[k], aa, _ev(sp.diff(e, sp.Symbol(name + "1")), penv, m_))
+                    np.add.at(dEdI[k], bb, _ev(sp.diff(e, sp.Symbol(name + "2")), penv, m_))
+                for k, gname in enumerate(self.param_derivs):
+                    dEdG[k] += float(_ev(sp.diff(e, sp.Symbol(gname)), penv, m_).sum())
         tot = dEdI.copy()
         for m in range(nv):
             for k in range(ni):
                 tot[k] += dEdV[m] * dVdI[m][k]
+            for a_ in range(3):
+                F[:, a_] -= dEdV[m] * dVdX[m][a_]
+            for k in range(len(self.param_derivs)):
+                dEdG[k] += float((dEdV[m] * dVdG[m][k]).sum())
         Fc, _ = orc.integral_chain(pos, radius, tot.reshape(-1))
         F += Fc
-        return {"energy": E, "forces": F, "values": np.array(V), "integrals": I, "dEdV": dEdV}
+        return {"energy": E, "forces": F, "values": np.array(V), "integrals": I, "dEdV": dEdV,
+                "param_derivs": dEdG}

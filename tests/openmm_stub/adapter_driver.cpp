@@ -187,7 +187,8 @@ int main() {
     std::unique_ptr<KernelImpl> k(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
     auto& gbmv = dynamic_cast<CalcCharmmGBMVForceKernel&>(*k);
     gbmv.initialize(system, force);
-    EXPECT(logged("create_custom n=4 model=1 params q radius integrals I4:4 I7:7 values B terms 0 1 0"));
+    EXPECT(logged("create_custom n=4 model=1 params q radius integrals I4:4 I7:7 values B terms 0 2 0"));
+    EXPECT(!logged("param_derivs"));
     EXPECT(logged("custom_params p00=0.2 p01=0.17"));
     context.setParameter("gamma", 0.5);
     gbmv.execute(context, true, true);
@@ -198,6 +199,32 @@ int main() {
     gbmv.execute(context, true, true);
     EXPECT(count("custom_global gamma 0.75") == 1);
     dump("gbmv expressions outside the canonical set: compiled");
+  }
+  g_log.clear();
+  {
+    // exclusions with a ParticlePair term, and energy derivatives by globals
+    CharmmGBMVForce force;
+    canonical(force, CharmmGBMVForce::GBMVIntegralTypeII);
+    force.addGlobalParameter("kr", 2.0);
+    force.addEnergyTerm("0.01*q1*q2/r", CharmmGBMVForce::ParticlePair);
+    force.addExclusion(0, 1);
+    force.addExclusion(2, 3);
+    force.addEnergyParameterDerivative("kr");
+    force.addEnergyParameterDerivative("alpha1");
+    context.setParameter("kr", 2.0);
+    KernelFactory* gf = cuda.factories["CalcCharmmGBMVForce"];
+    std::unique_ptr<KernelImpl> k(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
+    auto& gbmv = dynamic_cast<CalcCharmmGBMVForceKernel&>(*k);
+    gbmv.initialize(system, force);
+    EXPECT(logged("create_custom n=4 model=2 params q radius integrals I4:4 I7:7 values B terms 0 2 1 "
+                  "exclusions 0-1 2-3 param_derivs kr alpha1"));
+    EXPECT(cu.paramDerivNames.size() == 2 && cu.paramDerivNames[0] == "kr" && cu.paramDerivNames[1] == "alpha1");
+    cu.paramDerivWorkspace.clear();
+    gbmv.execute(context, true, true);
+    gbmv.execute(context, true, true);
+    EXPECT(count("param_derivs 2") == 2);
+    EXPECT(cu.paramDerivWorkspace["kr"] == 1.0 && cu.paramDerivWorkspace["alpha1"] == 2.0);  // two steps summed
+    dump("gbmv exclusions and energy parameter derivatives");
   }
   {
     CharmmGBMVForce force;

@@ -75,7 +75,21 @@ gbx_status gbx_create_custom(const gbx_config* cfg, int n, const gbx_custom* cs,
   for (int k = 0; k < cs->num_values; ++k) s += std::string(" ") + cs->value_names[k];
   s += " terms";
   for (int k = 0; k < cs->num_terms; ++k) s += " " + std::to_string(cs->term_types[k]);
+  if (cs->num_exclusions > 0) {
+    s += " exclusions";
+    for (int k = 0; k < cs->num_exclusions; ++k)
+      s += " " + std::to_string(cs->exclusions[2 * k]) + "-" + std::to_string(cs->exclusions[2 * k + 1]);
+  }
+  if (cs->num_param_derivs > 0) {
+    s += " param_derivs";
+    for (int k = 0; k < cs->num_param_derivs; ++k) s += std::string(" ") + cs->param_deriv_names[k];
+  }
   log(s);
+  return GBX_OK;
+}
+gbx_status gbx_get_custom_param_derivs(gbx_context*, double* out, int count) {
+  log("param_derivs " + std::to_string(count));
+  for (int k = 0; k < count; ++k) out[k] = 0.5 * (k + 1);  // 0.5, 1.0, ...
   return GBX_OK;
 }
 gbx_status gbx_set_custom_parameters(gbx_context*, const double* p) {

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <map>
+#include <string>
 #include <vector>
 
 #include "CudaArray.h"
@@ -27,6 +29,10 @@ class CudaContext {
   bool getAtomsWereReordered() const { return reordered; }
   BoxSize getPeriodicBoxSize() const { return box; }
   CUstream getCurrentStream() { return stream; }
+  // energy parameter derivatives: the names a force registers, and the
+  // context's workspace for derivatives formed outside its own kernels
+  void addEnergyParameterDerivative(const std::string& name) { paramDerivNames.push_back(name); }
+  std::map<std::string, double>& getEnergyParamDerivWorkspace() { return paramDerivWorkspace; }
 
   // test controls
   CudaArray posq, force, energy;
@@ -36,5 +42,7 @@ class CudaContext {
   BoxSize box{2.0, 2.0, 2.0, 0.0};
   CUstream stream = nullptr;
   int current_calls = 0;
+  std::vector<std::string> paramDerivNames;
+  std::map<std::string, double> paramDerivWorkspace;
 };
 }  // namespace OpenMM

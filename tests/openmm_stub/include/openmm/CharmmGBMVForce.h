@@ -3,6 +3,7 @@
 // 63-526 in the reference plugin) that a kernel reads.
 #pragma once
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace OpenMM {
@@ -18,7 +19,8 @@ class CharmmGBMVForce {
   int getNumComputedValues() const { return (int)values_.size(); }
   int getNumGBIntegrals() const { return (int)integrals_.size(); }
   int getNumEnergyTerms() const { return (int)terms_.size(); }
-  int getNumExclusions() const { return 0; }
+  int getNumExclusions() const { return (int)exclusions_.size(); }
+  int getNumEnergyParameterDerivatives() const { return (int)derivs_.size(); }
   int getNumTabulatedFunctions() const { return 0; }
   NonbondedMethod getNonbondedMethod() const { return method_; }
   void setNonbondedMethod(NonbondedMethod m) { method_ = m; }
@@ -72,6 +74,19 @@ class CharmmGBMVForce {
     expression = terms_[index].expr;
     type = terms_[index].type;
   }
+  int addExclusion(int particle1, int particle2) {
+    exclusions_.push_back({particle1, particle2});
+    return (int)exclusions_.size() - 1;
+  }
+  void getExclusionParticles(int index, int& particle1, int& particle2) const {
+    particle1 = exclusions_[index].first;
+    particle2 = exclusions_[index].second;
+  }
+  void addEnergyParameterDerivative(const std::string& name) {
+    for (size_t k = 0; k < gnames_.size(); ++k)
+      if (gnames_[k] == name) derivs_.push_back((int)k);
+  }
+  const std::string& getEnergyParameterDerivativeName(int index) const { return gnames_[derivs_[index]]; }
 
  private:
   struct Expr {
@@ -88,6 +103,8 @@ class CharmmGBMVForce {
   std::vector<std::vector<double>> params_;
   std::vector<Expr> values_, terms_;
   std::vector<Integral> integrals_;
+  std::vector<std::pair<int, int>> exclusions_;
+  std::vector<int> derivs_;
   GBIntegralType itype_ = GBSWIntegral;
   NonbondedMethod method_ = NoCutoff;
   double cutoff_ = 1.0;

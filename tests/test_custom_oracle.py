@@ -14,7 +14,8 @@ from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle import oracle as O
 from oracle.custom import CustomOracle
-from tests.custom_sets import CANONICAL, MODIFIED, modified_params
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, extended_exclusions,
+                                                               modified_params)
 
 
 @pytest.fixture(scope="module")
@@ -49,6 +50,40 @@ def test_modified_expressions_forces_are_energy_gradient(glob):
         xm[i, d] -= h
         fd = -(orc.energy_forces(xp, P)["energy"] - orc.energy_forces(xm, P)["energy"]) / (2 * h)
         assert abs(fd - F[i, d]) <= 1e-6 * np.abs(F).max() + 1e-5 * abs(F[i, d]), (i, d, fd, F[i, d])
+
+
+def test_extended_expressions_gradients(glob):
+    """Coordinates in a computed value and a single-particle term, excluded
+    pairs skipped by a ParticlePair term only, and the energy derivatives
+    by globals: forces and parameter derivatives against FP64 central
+    differences of the oracle's own energy."""
+    g = glob
+    m = GBModel.gbmv2(box=box_for(g.positions, margin=1.0))
+    P = np.stack([g.charge, g.radius], axis=1)
+    ext = dict(EXTENDED, exclusions=extended_exclusions(g.n))
+    orc = CustomOracle(m, ext)
+    out = orc.energy_forces(g.positions, P)
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    F = out["forces"]
+    for flat in rng.choice(3 * g.n, size=6, replace=False):
+        i, d = int(flat) // 3, int(flat) % 3
+        xp, xm = g.positions.copy(), g.positions.copy()
+        xp[i, d] += h
+        xm[i, d] -= h
+        fd = -(orc.energy_forces(xp, P)["energy"] - orc.energy_forces(xm, P)["energy"]) / (2 * h)
+        assert abs(fd - F[i, d]) <= 1e-6 * np.abs(F).max() + 1e-5 * abs(F[i, d]), (i, d, fd, F[i, d])
+    for k, name in enumerate(ext["param_derivs"]):
+        gp, gm = dict(ext["globals"]), dict(ext["globals"])
+        gp[name] += h
+        gm[name] -= h
+        ep = CustomOracle(m, dict(ext, globals=gp)).energy_forces(g.positions, P)["energy"]
+        em = CustomOracle(m, dict(ext, globals=gm)).energy_forces(g.positions, P)["energy"]
+        fd = (ep - em) / (2 * h)
+        assert abs(fd - out["param_derivs"][k]) <= 1e-6 * abs(fd) + 1e-6, (name, fd, out["param_derivs"][k])
+    # the exclusions change the ParticlePair term
+    plain = CustomOracle(m, EXTENDED).energy_forces(g.positions, P)
+    assert abs(plain["energy"] / out["energy"] - 1) > 1e-4
 
 
 def test_library_compiles_and_refuses_expression_sets():

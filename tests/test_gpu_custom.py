@@ -7,6 +7,9 @@ through the C ABI, against the FP64 custom-expression oracle
 * a set outside it (a second computed value, globals, a nonpolar
   single-particle term, a Lepton definition) for the GBMV-II and
   GBSW-integral classes, with and without a cutoff;
+* coordinates in a computed value and a single-particle term, exclusions
+  skipped by a ParticlePair term only, and energy derivatives by globals
+  (addEnergyParameterDerivative);
 * a global parameter update, bit-reproducible calls, and a refused
   expression.
 
@@ -22,7 +25,8 @@ from openmmcustomgbintegralforce_gb300._lib import Context, CustomContext, GBXEr
 from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle.custom import CustomOracle
-from tests.custom_sets import CANONICAL, MODIFIED, modified_params
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, extended_exclusions,
+                                                               modified_params)
 
 pytestmark = pytest.mark.gpu
 
@@ -161,3 +165,70 @@ def test_kernel_mirror_compiles_a_non_canonical_force(glob):
     ref = CustomOracle(GBModel.gbmv2(box=box), MODIFIED).energy_forces(g.positions, P)
     assert abs(E / ref["energy"] - 1) < E_TOL
     assert rel_rms(F, ref["forces"]) < F_TOL
+
+
+@pytest.mark.parametrize("cls", ["gbmv2", "gbsw_integral"])
+def test_extended_set_vs_oracle(glob, cls):
+    """Coordinates, exclusions and parameter derivatives: energy, forces,
+    the computed values and dE/dg against the oracle; the exclusions
+    change the result; repeated calls are bit-identical."""
+    g = glob
+    m = model_of(cls, g)
+    P = np.stack([g.charge, g.radius], axis=1)
+    ext = dict(EXTENDED, exclusions=extended_exclusions(g.n))
+    ctx = CustomContext(m, g.n, ext)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(g.positions)
+    pd = ctx.param_derivs()
+    E2, F2 = ctx.execute_host(g.positions)
+    assert E2 == E and np.array_equal(F2, F) and np.array_equal(ctx.param_derivs(), pd)
+    ref = CustomOracle(m, ext).energy_forces(g.positions, P)
+    print(f"{cls} extended: energy {abs(E / ref['energy'] - 1):.2e} forces {rel_rms(F, ref['forces']):.2e} "
+          f"param derivs {np.abs(pd / ref['param_derivs'] - 1).max():.2e}")
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    assert np.abs(ctx.born_radii() / ref["values"][0] - 1).max() < B_TOL
+    assert np.abs(pd / ref["param_derivs"] - 1).max() < E_TOL * 5
+    plain = CustomOracle(m, EXTENDED).energy_forces(g.positions, P)
+    assert abs(plain["energy"] / E - 1) > 1e-4
+    ctx.close()
+
+
+def test_kernel_mirror_exclusions_and_param_derivs(glob):
+    """The GBMV kernel mirror passes the force's exclusions and energy
+    parameter derivatives to the compiled path."""
+    from openmmcustomgbintegralforce_gb300 import api
+
+    g = glob
+    f = api.CharmmGBMVForce()
+    for p in EXTENDED["params"]:
+        f.addPerParticleParameter(p)
+    for k, v in EXTENDED["globals"].items():
+        f.addGlobalParameter(k, v)
+    for name in EXTENDED["param_derivs"]:
+        f.addEnergyParameterDerivative(name)
+    for name, order in EXTENDED["integrals"]:
+        f.addGBIntegral(name, [order], [])
+    for name, e in EXTENDED["values"]:
+        f.addComputedValue(name, e, api.SingleParticle)
+    kinds = {0: api.SingleParticle, 1: api.ParticlePair, 2: api.ParticlePairNoExclusions}
+    for e, t in EXTENDED["terms"]:
+        f.addEnergyTerm(e, kinds[t])
+    excl = extended_exclusions(g.n)
+    for i, j in excl:
+        f.addExclusion(i, j)
+    f.setGBIntegralType(api.GBMVIntegralTypeII)
+    P = np.stack([g.charge, g.radius], axis=1)
+    for row in P:
+        f.addParticle(list(row))
+    box = box_for(g.positions, margin=1.0)
+    k = api.CalcCharmmGBMVForceKernel(box=box)
+    k.initialize(g.n, f)
+    E, F = k.execute(g.positions)
+    pd = k.getEnergyParameterDerivatives()
+    ref = CustomOracle(GBModel.gbmv2(box=box), dict(EXTENDED, exclusions=excl)).energy_forces(g.positions, P)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    assert sorted(pd) == sorted(EXTENDED["param_derivs"])
+    for n, v in zip(EXTENDED["param_derivs"], ref["param_derivs"]):
+        assert abs(pd[n] / v - 1) < E_TOL * 5

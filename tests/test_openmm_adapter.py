@@ -11,7 +11,9 @@ each reorder (parameters are not re-sent), the flags of each OpenMM
 precision mode, the box and global-parameter updates, an earlier step's
 overflowed table surfacing as an OpenMMException, a force outside the
 canonical expression set handed to gbx_create_custom with its global
-parameters followed, and the refusal of CustomIntegral.
+parameters followed, a force's exclusions, term types and energy parameter
+derivatives passed on (the derivatives summed into the context's workspace
+each step), and the refusal of CustomIntegral.
 """
 import os
 import shutil
