@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <set>
 #include <new>
 #include <sstream>
 #include <stdexcept>
@@ -117,8 +118,9 @@ struct CustomArgs {
   unsigned long long* dEdB;  // [n] dE/d(first computed value), fixed point
   unsigned* status;
   double* dVdX;              // [nv][3][n] total derivatives of the values by the particle's coordinates
-  const int* excl_start;     // [n + 1] each particle's excluded partners (CSR, ascending)
-  const int* excl;
+  const int* excl_row;       // [tiles + 1] each 32-particle tile's entries in excl_tile
+  const int* excl_tile;      // the partner tile J >= I of each entry
+  const unsigned* excl_mask; // [entries][32] bit b of word l: particles l of I and b of J are excluded
   double* dVdG;              // [nv][npd][n] total derivatives of the values by the requested globals
   double* pd_part;           // [blocks][npd] per-block energy derivatives by the requested globals
 };
@@ -174,8 +176,9 @@ struct CustomPlan {
   unsigned long long* d_dEdV = nullptr;
   unsigned long long* d_dEdI = nullptr;
   double* d_dVdX = nullptr;
-  int* d_excl_start = nullptr;
-  int* d_excl = nullptr;
+  int* d_excl_row = nullptr;
+  int* d_excl_tile = nullptr;
+  unsigned* d_excl_mask = nullptr;
   double* d_dVdG = nullptr;
   double* d_pd_part = nullptr;
   bool coords = false;      // some computed value or single-particle term reads x, y or z
@@ -316,101 +319,169 @@ std::string generate(const CustomPlan& p) {
     o << block_sum("pd" + std::to_string(k), "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
   o << "}\n\n";
 
-  // ---- pair terms (FP32, fast math); each thread sums its own particle's
-  // side of every pair it is in
-  o << "extern \"C\" __global__ void __launch_bounds__(" << kPairThreads << ") gbx_pair(CustomArgs a) {\n";
-  o << "  __shared__ float4 s_pos[" << kPairThreads << "];\n";
-  if (np) o << "  __shared__ float s_p[" << np << "][" << kPairThreads << "];\n";
-  if (nv) o << "  __shared__ float s_v[" << nv << "][" << kPairThreads << "];\n";
-  if (ni) o << "  __shared__ float s_I[" << ni << "][" << kPairThreads << "];\n";
-  o << "  __shared__ double s_e[" << kPairThreads << "];\n";
-  o << "  const int i = blockIdx.x * blockDim.x + threadIdx.x;\n";
-  o << "  const bool own = i < a.n;\n  const int ii = own ? i : 0;\n";
-  o << "  const float4 xi = a.pos[ii];\n";
-  for (int k = 0; k < np; ++k) o << "  const float p" << k << "_i = a.paramsf[" << k << " * a.n + ii];\n";
-  for (int k = 0; k < nv; ++k) o << "  const float v" << k << "_i = a.Vf[" << k << " * a.n + ii];\n";
-  for (int k = 0; k < ni; ++k) o << "  const float I" << k << "_i = a.If[" << k << " * a.n + ii];\n";
-  for (int k = 0; k < ng; ++k) o << "  const float gf" << k << " = (float)a.globals[" << k << "];\n";
-  o << "  float fx = 0.f, fy = 0.f, fz = 0.f;\n  double e = 0.0;\n";
-  for (int k = 0; k < nv; ++k) o << "  float gV" << k << " = 0.f;\n";
-  for (int k = 0; k < ni; ++k) o << "  float gI" << k << " = 0.f;\n";
-  for (int k = 0; k < npd; ++k) o << "  float pdp" << k << " = 0.f;\n";
-  // the particle's excluded partners, walked in step with j (both ascend)
-  if (p.excluding) o << "  int ex = own ? a.excl_start[i] : 0;\n  const int ex_end = own ? a.excl_start[i + 1] : 0;\n";
-  o << "  for (int base = 0; base < a.n; base += " << kPairThreads << ") {\n";
-  o << "    const int jl = base + threadIdx.x;\n    if (jl < a.n) {\n      s_pos[threadIdx.x] = a.pos[jl];\n";
-  for (int k = 0; k < np; ++k) o << "      s_p[" << k << "][threadIdx.x] = a.paramsf[" << k << " * a.n + jl];\n";
-  for (int k = 0; k < nv; ++k) o << "      s_v[" << k << "][threadIdx.x] = a.Vf[" << k << " * a.n + jl];\n";
-  for (int k = 0; k < ni; ++k) o << "      s_I[" << k << "][threadIdx.x] = a.If[" << k << " * a.n + jl];\n";
-  o << "    }\n    __syncthreads();\n";
-  o << "    const int jn = min(" << kPairThreads << ", a.n - base);\n";
-  o << "    for (int t = 0; t < jn && own; ++t) {\n      const int j = base + t;\n";
-  if (p.excluding)
-    o << "      while (ex < ex_end && a.excl[ex] < j) ++ex;\n"
-         "      const bool excluded = ex < ex_end && a.excl[ex] == j;\n";
-  o << "      if (j == i) continue;\n";
-  o << "      const float4 xj = s_pos[t];\n";
-  o << "      float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;\n";
-  o << "      if (a.periodic) {\n        dx -= a.L[0] * floorf(dx * a.iL[0] + 0.5f);\n        dy -= a.L[1] * "
-       "floorf(dy * a.iL[1] + 0.5f);\n        dz -= a.L[2] * floorf(dz * a.iL[2] + 0.5f);\n      }\n";
-  o << "      const float r2 = dx * dx + dy * dy + dz * dz;\n";
-  o << "      if (a.cutoff2 > 0.f && r2 >= a.cutoff2) continue;\n      const float r = sqrtf(r2);\n";
-  // atom 1 is the lower index (CharmmReferenceGBMV.cpp:281-283): this atom is 1 when j > i
-  o << "      const bool lo = i < j;\n";
-  for (int k = 0; k < np; ++k) {
-    const std::string K = std::to_string(k);
-    o << "      const float pa" << K << " = lo ? p" << K << "_i : s_p[" << K << "][t];\n";
-    o << "      const float pb" << K << " = lo ? s_p[" << K << "][t] : p" << K << "_i;\n";
-  }
-  for (int k = 0; k < nv; ++k) {
-    const std::string K = std::to_string(k);
-    o << "      const float va" << K << " = lo ? v" << K << "_i : s_v[" << K << "][t];\n";
-    o << "      const float vb" << K << " = lo ? s_v[" << K << "][t] : v" << K << "_i;\n";
-  }
-  for (int k = 0; k < ni; ++k) {
-    const std::string K = std::to_string(k);
-    o << "      const float Ia" << K << " = lo ? I" << K << "_i : s_I[" << K << "][t];\n";
-    o << "      const float Ib" << K << " = lo ? s_I[" << K << "][t] : I" << K << "_i;\n";
-  }
+  // ---- pair terms (FP32, fast math).  Each unordered pair once: tiles of
+  // 32 particles, tile pairs (I, J) with I <= J numbered row by row and
+  // split into contiguous runs, one run per warp.  A lane holds particle i
+  // of tile I; tile J's particles and their sums rotate through the warp
+  // by one lane a step, so at step k lane l meets particle (l + k) mod 32
+  // of tile J.  On a diagonal tile steps 1..15, and step 16 for the lower
+  // half of the lanes, meet every pair once.
   {
-    expr::SharedEmitter pe(nm.pair, true, "u", "      ");
+    // what the pair terms read: per-particle inputs rotated with j, and the
+    // derivatives summed for each particle
+    std::set<std::string> used;
+    for (size_t t = 0; t < p.terms.size(); ++t) {
+      if (p.term_types[t] == 0) continue;
+      std::vector<std::string> vars;
+      expr::variables(p.terms[t], vars);
+      used.insert(vars.begin(), vars.end());
+    }
+    auto uses = [&](const std::string& name) { return used.count(name + "1") || used.count(name + "2"); };
+    std::vector<int> up, uv, ui;
+    for (int k = 0; k < np; ++k)
+      if (uses(s.params[k])) up.push_back(k);
+    for (int k = 0; k < nv; ++k)
+      if (uses(s.value_names[k])) uv.push_back(k);
+    for (int k = 0; k < ni; ++k)
+      if (uses(s.integrals[k])) ui.push_back(k);
+    std::vector<std::string> inputs;  // "p0", "v1", "I0": arrays a.paramsf / a.Vf / a.If
+    auto array_of = [](const std::string& in) {
+      return in[0] == 'p' ? std::string("a.paramsf") : in[0] == 'v' ? std::string("a.Vf") : std::string("a.If");
+    };
+    for (int k : up) inputs.push_back("p" + std::to_string(k));
+    for (int k : uv) inputs.push_back("v" + std::to_string(k));
+    for (int k : ui) inputs.push_back("I" + std::to_string(k));
+    std::vector<std::string> sums = {"fx", "fy", "fz"};  // per-particle sums
+    for (int k : uv) sums.push_back("gV" + std::to_string(k));
+    for (int k : ui) sums.push_back("gI" + std::to_string(k));
+    // the rotation: every lane takes the j data and sums of the next lane
+    std::string rot;
+    auto shfl = [&](const std::string& v) {
+      rot += "      " + v + " = __shfl_sync(0xffffffffu, " + v + ", (lane + 1) & 31);\n";
+    };
+    for (const char* c : {"xj.x", "xj.y", "xj.z"}) shfl(c);
+    shfl("jn");
+    for (auto& in : inputs) shfl(in + "_j");
+    for (auto& sm : sums) shfl(sm + "_j");
+    auto sum_target = [](const std::string& sname, const std::string& idx) {
+      if (sname == "fx") return "a.force + " + idx;
+      if (sname == "fy") return "a.force + a.stride + " + idx;
+      if (sname == "fz") return "a.force + 2 * a.stride + " + idx;
+      if (sname[1] == 'V') return "a.dEdV + " + sname.substr(2) + " * a.n + " + idx;
+      return "a.dEdI + " + sname.substr(2) + " * a.n + " + idx;
+    };
+
+    o << "extern \"C\" __global__ void __launch_bounds__(" << kPairThreads << ") gbx_pair(CustomArgs a) {\n";
+    o << "  __shared__ double s_e[" << kPairThreads << "];\n";
+    o << "  const int lane = threadIdx.x & 31;\n";
+    o << "  const int nt = (a.n + 31) >> 5;\n";
+    o << "  const long long T = (long long)nt * (nt + 1) / 2;\n";
+    o << "  const long long W = (long long)gridDim.x * (blockDim.x >> 5);\n";
+    o << "  const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);\n";
+    o << "  long long t = w * T / W;\n  const long long t_end = (w + 1) * T / W;\n";
+    // the row of tile t: the largest I with I * nt - I * (I - 1) / 2 <= t
+    o << "  auto row_start = [nt](long long r) { return r * nt - r * (r - 1) / 2; };\n";
+    o << "  const double b2 = 2.0 * nt + 1.0;\n";
+    o << "  int I = (int)((b2 - sqrt(fmax(b2 * b2 - 8.0 * (double)t, 0.0))) * 0.5);\n";
+    o << "  I = max(0, min(I, nt - 1));\n";
+    o << "  while (I > 0 && row_start(I) > t) --I;\n  while (I + 1 < nt && row_start(I + 1) <= t) ++I;\n";
+    o << "  int J = I + (int)(t - row_start(I));\n";
+    o << "  double e = 0.0;\n";
+    for (int k = 0; k < npd; ++k) o << "  double pdp" << k << " = 0.0;\n";
+    for (int k = 0; k < ng; ++k) o << "  const float gf" << k << " = (float)a.globals[" << k << "];\n";
+    o << "  int cur = -1, i = 0;\n  bool iok = false;\n  float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);\n";
+    for (auto& in : inputs) o << "  float " << in << "_i = 0.f;\n";
+    for (auto& sm : sums) o << "  float " << sm << "_i = 0.f;\n";
+    o << "  for (; t < t_end; ++t) {\n";
+    o << "    if (I != cur) {\n";
+    o << "      if (iok) {\n";
+    for (auto& sm : sums) o << "        gbx_add_fixed(" << sum_target(sm, "i") << ", (double)" << sm << "_i);\n";
+    o << "      }\n";
+    o << "      cur = I;\n      i = I * 32 + lane;\n      iok = i < a.n;\n      const int ii = iok ? i : 0;\n";
+    o << "      xi = a.pos[ii];\n";
+    for (auto& in : inputs)
+      o << "      " << in << "_i = " << array_of(in) << "[" << in.substr(1) << " * a.n + ii];\n";
+    for (auto& sm : sums) o << "      " << sm << "_i = 0.f;\n";
+    o << "    }\n";
+    o << "    const bool diag = I == J;\n";
+    o << "    const int j0 = J * 32 + lane;\n    const int jj = j0 < a.n ? j0 : 0;\n";
+    o << "    float4 xj = a.pos[jj];\n";
+    o << "    int jn = j0;\n";  // the particle this lane's j data belongs to, rotated with it
+    for (auto& in : inputs) o << "    float " << in << "_j = " << array_of(in) << "[" << in.substr(1) << " * a.n + jj];\n";
+    for (auto& sm : sums) o << "    float " << sm << "_j = 0.f;\n";
+    if (p.excluding) {
+      // the tile's exclusion mask: bit b of lane l's word excludes particle
+      // b of tile J for particle l of tile I
+      o << "    unsigned xmask = 0u;\n";
+      o << "    for (int q = a.excl_row[I]; q < a.excl_row[I + 1]; ++q)\n";
+      o << "      if (a.excl_tile[q] == J) { xmask = a.excl_mask[q * 32 + lane]; break; }\n";
+    }
+    o << "    float et = 0.f;\n";
+    for (int k = 0; k < npd; ++k) o << "    float pdt" << k << " = 0.f;\n";
+    o << "    for (int k = 0; k < 32; ++k) {\n";
+    o << "      const int jl = (lane + k) & 31;\n      const int j = J * 32 + jl;\n";
+    o << "      if (iok && j < a.n && (!diag || (k >= 1 && (k < 16 || lane < 16)))) {\n";
+    o << "        float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;\n";
+    o << "        if (a.periodic) {\n          dx -= a.L[0] * floorf(dx * a.iL[0] + 0.5f);\n          dy -= a.L[1] * "
+         "floorf(dy * a.iL[1] + 0.5f);\n          dz -= a.L[2] * floorf(dz * a.iL[2] + 0.5f);\n        }\n";
+    o << "        const float r2 = dx * dx + dy * dy + dz * dz;\n";
+    o << "        if (a.cutoff2 <= 0.f || r2 < a.cutoff2) {\n";
+    o << "          const float r = sqrtf(r2);\n";
+    if (p.excluding) o << "          const bool excluded = (xmask >> jl) & 1u;\n";
+    // atom 1 is the lower index (CharmmReferenceGBMV.cpp:281-283)
+    o << "          const bool lo = i < j;\n";
+    auto side = [&](const std::string& a_name, const std::string& b_name, const std::string& in) {
+      o << "          const float " << a_name << " = lo ? " << in << "_i : " << in << "_j;\n";
+      o << "          const float " << b_name << " = lo ? " << in << "_j : " << in << "_i;\n";
+    };
+    for (int k : up) side("pa" + std::to_string(k), "pb" + std::to_string(k), "p" + std::to_string(k));
+    for (int k : uv) side("va" + std::to_string(k), "vb" + std::to_string(k), "v" + std::to_string(k));
+    for (int k : ui) side("Ia" + std::to_string(k), "Ib" + std::to_string(k), "I" + std::to_string(k));
+    expr::SharedEmitter pe(nm.pair, true, "u", "          ");
     std::ostringstream acc;
-    acc << "      float dEdr = 0.f;\n";
+    acc << "          float dEdr = 0.f;\n";
     for (size_t t = 0; t < p.terms.size(); ++t) {
       if (p.term_types[t] == 0) continue;
       // ParticlePair: an excluded pair contributes nothing
       const bool skip = p.excluding && p.term_types[t] == 1;
       auto W = [&](const std::string& x) { return skip ? "(excluded ? 0.f : " + x + ")" : x; };
-      acc << "      if (lo) e += (double)" << W(pe(p.terms[t])) << ";\n";
-      acc << "      dEdr += " << W(pe(D(p.terms[t], "r"))) << ";\n";
-      for (int k = 0; k < nv; ++k) {
-        const std::string n1 = s.value_names[k] + "1", n2 = s.value_names[k] + "2";
-        acc << "      gV" << k << " += " << W("(lo ? " + pe(D(p.terms[t], n1)) + " : " + pe(D(p.terms[t], n2)) + ")")
-            << ";\n";
-      }
-      for (int k = 0; k < ni; ++k) {
-        const std::string n1 = s.integrals[k] + "1", n2 = s.integrals[k] + "2";
-        acc << "      gI" << k << " += " << W("(lo ? " + pe(D(p.terms[t], n1)) + " : " + pe(D(p.terms[t], n2)) + ")")
-            << ";\n";
-      }
+      acc << "          et += " << W(pe(p.terms[t])) << ";\n";
+      acc << "          dEdr += " << W(pe(D(p.terms[t], "r"))) << ";\n";
+      auto both = [&](const std::string& sname, const std::string& base) {
+        const std::string d1 = W(pe(D(p.terms[t], base + "1"))), d2 = W(pe(D(p.terms[t], base + "2")));
+        acc << "          " << sname << "_i += lo ? " << d1 << " : " << d2 << ";\n";
+        acc << "          " << sname << "_j += lo ? " << d2 << " : " << d1 << ";\n";
+      };
+      for (int k : uv) both("gV" + std::to_string(k), s.value_names[k]);
+      for (int k : ui) both("gI" + std::to_string(k), s.integrals[k]);
       for (int k = 0; k < npd; ++k)
-        acc << "      if (lo) pdp" << k << " += " << W(pe(D(p.terms[t], s.globals[p.pd_index[k]]))) << ";\n";
+        acc << "          pdt" << k << " += " << W(pe(D(p.terms[t], s.globals[p.pd_index[k]]))) << ";\n";
     }
     o << pe.take_decls() << acc.str();
+    // F_i = -dE/dx_i = -(dE/dr) (x_i - x_j) / r, and F_j the opposite
+    o << "          const float sr = dEdr / r;\n";
+    o << "          fx_i -= sr * dx;\n          fy_i -= sr * dy;\n          fz_i -= sr * dz;\n";
+    o << "          fx_j += sr * dx;\n          fy_j += sr * dy;\n          fz_j += sr * dz;\n";
+    o << "        }\n      }\n";
+    o << "      if (diag && k == 16) break;\n";
+    o << rot;
+    o << "    }\n";
+    o << "    e += (double)et;\n";
+    for (int k = 0; k < npd; ++k) o << "    pdp" << k << " += (double)pdt" << k << ";\n";
+    o << "    if (jn < a.n) {\n";
+    for (auto& sm : sums) o << "      gbx_add_fixed(" << sum_target(sm, "jn") << ", (double)" << sm << "_j);\n";
+    o << "    }\n";
+    o << "    if (++J == nt) { ++I; J = I; }\n";
+    o << "  }\n";
+    o << "  if (iok) {\n";
+    for (auto& sm : sums) o << "    gbx_add_fixed(" << sum_target(sm, "i") << ", (double)" << sm << "_i);\n";
+    o << "  }\n";
+    o << block_sum("e", "a.energy_part[blockIdx.x]");
+    for (int k = 0; k < npd; ++k)
+      o << block_sum("pdp" + std::to_string(k),
+                     "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
+    o << "}\n\n";
   }
-  // F_i = -dE/dx_i = -(dE/dr) (x_i - x_j) / r
-  o << "      const float sr = dEdr / r;\n      fx -= sr * dx;\n      fy -= sr * dy;\n      fz -= sr * dz;\n";
-  o << "    }\n    __syncthreads();\n  }\n";
-  o << "  if (own) {\n";
-  o << "    gbx_add_fixed(a.force + i, (double)fx);\n    gbx_add_fixed(a.force + a.stride + i, (double)fy);\n"
-       "    gbx_add_fixed(a.force + 2 * a.stride + i, (double)fz);\n";
-  for (int k = 0; k < nv; ++k) o << "    gbx_add_fixed(a.dEdV + " << k << " * a.n + i, (double)gV" << k << ");\n";
-  for (int k = 0; k < ni; ++k) o << "    gbx_add_fixed(a.dEdI + " << k << " * a.n + i, (double)gI" << k << ");\n";
-  o << "  }\n" << block_sum("e", "a.energy_part[blockIdx.x]");
-  for (int k = 0; k < npd; ++k)
-    o << block_sum("(double)pdp" + std::to_string(k),
-                   "a.pd_part[blockIdx.x * " + std::to_string(npd) + " + " + std::to_string(k) + "]");
-  o << "}\n\n";
 
   // ---- the integrals' adjoint for the chain rule; the values' explicit
   // coordinate and global dependence
@@ -514,8 +585,9 @@ struct CustomArgs {
   unsigned long long* dEdB;
   unsigned* status;
   double* dVdX;
-  const int* excl_start;
-  const int* excl;
+  const int* excl_row;
+  const int* excl_tile;
+  const unsigned* excl_mask;
   double* dVdG;
   double* pd_part;
 };
@@ -591,11 +663,14 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
   bool pair_with_exclusions = false;
   for (int t : plan->term_types) pair_with_exclusions = pair_with_exclusions || t == 1;
   plan->excluding = !spec.exclusions.empty() && pair_with_exclusions;
-  // each particle's excluded partners, both directions, ascending
-  std::vector<int> excl_start, excl;
+  // exclusions as 32 x 32 bit masks of the tile pairs (I <= J) that hold
+  // any: bit b of word l excludes particle l of tile I with particle b of
+  // tile J (on a diagonal tile both ways)
+  std::vector<int> excl_row, excl_tile;
+  std::vector<unsigned> excl_mask;
   if (plan->excluding) {
-    const int n = ctx->n;
-    std::vector<std::vector<int>> per(n);
+    const int n = ctx->n, nt = (n + 31) / 32;
+    std::vector<std::map<int, std::vector<unsigned>>> rows(nt);
     for (size_t k = 0; k + 1 < spec.exclusions.size(); k += 2) {
       const int a = spec.exclusions[k], b = spec.exclusions[k + 1];
       if (a < 0 || b < 0 || a >= n || b >= n || a == b) {
@@ -603,15 +678,19 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
                           " is out of range";
         return GBX_ERR_INVALID_ARGUMENT;
       }
-      per[a].push_back(b);
-      per[b].push_back(a);
+      const int lo = std::min(a, b), hi = std::max(a, b);
+      auto& m = rows[lo / 32][hi / 32];
+      m.resize(32, 0u);
+      m[lo % 32] |= 1u << (hi % 32);
+      if (lo / 32 == hi / 32) m[hi % 32] |= 1u << (lo % 32);
     }
-    excl_start.push_back(0);
-    for (auto& v : per) {
-      std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
-      excl.insert(excl.end(), v.begin(), v.end());
-      excl_start.push_back((int)excl.size());
+    excl_row.push_back(0);
+    for (auto& row : rows) {
+      for (auto& [J, m] : row) {
+        excl_tile.push_back(J);
+        excl_mask.insert(excl_mask.end(), m.begin(), m.end());
+      }
+      excl_row.push_back((int)excl_tile.size());
     }
   }
   std::string err;
@@ -628,7 +707,12 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
   const int n = ctx->n, np = (int)spec.params.size(), ni = (int)spec.integrals.size(),
             nv = (int)spec.value_names.size();
   plan->value_blocks = (n + kValueThreads - 1) / kValueThreads;
-  plan->pair_blocks = (n + kPairThreads - 1) / kPairThreads;
+  {
+    // tile pairs over warps: up to 16 warps per multiprocessor
+    const long long nt = (n + 31) / 32, tiles = nt * (nt + 1) / 2;
+    const long long warps = std::min<long long>(tiles, 16LL * std::max(ctx->sms, 1));
+    plan->pair_blocks = (int)((warps + kPairThreads / 32 - 1) / (kPairThreads / 32));
+  }
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_params, (size_t)np * n));
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_paramsf, (size_t)np * n));
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_S, (size_t)ni));
@@ -646,12 +730,16 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
     GBX_TRY_CUSTOM(alloc(ctx, &plan->d_pd_part, (size_t)(2 * plan->value_blocks + plan->pair_blocks) * npd));
   }
   if (plan->excluding) {
-    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl_start, excl_start.size()));
-    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl, excl.size()));
-    if (cudaMemcpy(plan->d_excl_start, excl_start.data(), sizeof(int) * excl_start.size(), cudaMemcpyHostToDevice) !=
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl_row, excl_row.size()));
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl_tile, excl_tile.size()));
+    GBX_TRY_CUSTOM(alloc(ctx, &plan->d_excl_mask, excl_mask.size()));
+    if (cudaMemcpy(plan->d_excl_row, excl_row.data(), sizeof(int) * excl_row.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
-        (!excl.empty() &&
-         cudaMemcpy(plan->d_excl, excl.data(), sizeof(int) * excl.size(), cudaMemcpyHostToDevice) != cudaSuccess))
+        (!excl_tile.empty() &&
+         (cudaMemcpy(plan->d_excl_tile, excl_tile.data(), sizeof(int) * excl_tile.size(), cudaMemcpyHostToDevice) !=
+              cudaSuccess ||
+          cudaMemcpy(plan->d_excl_mask, excl_mask.data(), sizeof(unsigned) * excl_mask.size(),
+                     cudaMemcpyHostToDevice) != cudaSuccess)))
       return GBX_ERR_CUDA;
   }
   const double S[2] = {ctx->S4, ctx->S7};  // the sums of the two integrals' weights
@@ -668,8 +756,8 @@ void custom_destroy(Context* ctx) {
   if (!p) return;
   for (void* q : {(void*)p->d_params, (void*)p->d_paramsf, (void*)p->d_S, (void*)p->d_globals, (void*)p->d_V,
                   (void*)p->d_Vf, (void*)p->d_If, (void*)p->d_dVdI, (void*)p->d_dEdV, (void*)p->d_dEdI,
-                  (void*)p->d_dVdX, (void*)p->d_excl_start, (void*)p->d_excl, (void*)p->d_dVdG,
-                  (void*)p->d_pd_part})
+                  (void*)p->d_dVdX, (void*)p->d_excl_row, (void*)p->d_excl_tile, (void*)p->d_excl_mask,
+                  (void*)p->d_dVdG, (void*)p->d_pd_part})
     if (q) cudaFree(q);
   if (p->library) cudaLibraryUnload(p->library);
   delete p;
@@ -751,8 +839,9 @@ CustomArgs args_of(Context* ctx, const float4* pos, unsigned long long* force, i
   a.dEdB = ctx->d_dEdB_fx;
   a.status = ctx->d_status;
   a.dVdX = p->d_dVdX;
-  a.excl_start = p->d_excl_start;
-  a.excl = p->d_excl;
+  a.excl_row = p->d_excl_row;
+  a.excl_tile = p->d_excl_tile;
+  a.excl_mask = p->d_excl_mask;
   a.dVdG = p->d_dVdG;
   a.pd_part = p->d_pd_part;
   return a;
