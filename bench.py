@@ -679,12 +679,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-molecule measurement")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' measurements")
+    ap.add_argument("--only-expressions", action="store_true",
+                    help="measure only the compiled-expression path (GBMV-II 10k) and print its JSON")
     ap.add_argument("--jitter", type=float, default=0.0,
                     help="A: fresh N(0, jitter) position noise before every timed step (MD-like back-to-back "
                          "evaluations); the FP64 error is then taken on the last jittered conformation")
     args = ap.parse_args()
     batch_set = None
-    if args.impl == "gb300" and not args.no_batch and int(os.environ.get("RANK", "0")) == 0:
+    if args.impl == "gb300" and not args.no_batch and not args.only_expressions and int(os.environ.get("RANK", "0")) == 0:
         # generated before any CUDA work, in a spawn-started pool
         batch_set = make_batch(batch_sizes(BATCH_MOLECULES, 500, 8000, seed=BATCH_SEED), seed=BATCH_SEED)
     world, rank, local = dist_setup(args)
@@ -698,6 +700,10 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.only_expressions:
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+        print(json.dumps(measure_custom(dev, flush, steps=args.steps)))
+        return
     w = workloads()[args.workload]
     g = make_globule(w["n"], seed=w["seed"])
     model = model_for(w, g)

@@ -150,6 +150,18 @@ __device__ __forceinline__ void gbx_add_fixed(unsigned long long* p, double v) {
   const long long q = gbx_fixed(v);
   if (q) atomicAdd(p, (unsigned long long)q);
 }
+// FP32 sums to fixed point without the FP64 pipe: floor(v) 2^32 plus the
+// fraction's 2^32 multiple, two 32-bit conversions (|v| < 2^31; within
+// 2^-25 of round(v 2^32))
+__device__ __forceinline__ long long gbx_fixed_f(float v) {
+  const float hf = floorf(v);
+  const unsigned lo = __float2uint_rn((v - hf) * 4294967296.0f);
+  return (long long)(((unsigned long long)(long long)__float2int_rz(hf) << 32) + lo);
+}
+__device__ __forceinline__ void gbx_add_fixed_f(unsigned long long* p, float v) {
+  const long long q = gbx_fixed_f(v);
+  if (q) atomicAdd(p, (unsigned long long)q);
+}
 )";
 
 constexpr int kValueThreads = 256;
@@ -183,6 +195,8 @@ struct CustomPlan {
   double* d_pd_part = nullptr;
   bool coords = false;      // some computed value or single-particle term reads x, y or z
   bool excluding = false;   // exclusions exist and some term honours them
+  bool cutoff = false;      // pair terms only within the cutoff (fixed at creation)
+  bool periodic = false;    // pair distances by minimum image (fixed at creation)
   std::vector<int> pd_index;  // requested globals, as indices into spec.globals
   int value_blocks = 0, pair_blocks = 0;
   std::string source;  // kept for diagnostics
@@ -357,10 +371,9 @@ std::string generate(const CustomPlan& p) {
     // the rotation: every lane takes the j data and sums of the next lane
     std::string rot;
     auto shfl = [&](const std::string& v) {
-      rot += "      " + v + " = __shfl_sync(0xffffffffu, " + v + ", (lane + 1) & 31);\n";
+      rot += "        " + v + " = __shfl_sync(0xffffffffu, " + v + ", (lane + 1) & 31);\n";
     };
     for (const char* c : {"xj.x", "xj.y", "xj.z"}) shfl(c);
-    shfl("jn");
     for (auto& in : inputs) shfl(in + "_j");
     for (auto& sm : sums) shfl(sm + "_j");
     auto sum_target = [](const std::string& sname, const std::string& idx) {
@@ -395,7 +408,7 @@ std::string generate(const CustomPlan& p) {
     o << "  for (; t < t_end; ++t) {\n";
     o << "    if (I != cur) {\n";
     o << "      if (iok) {\n";
-    for (auto& sm : sums) o << "        gbx_add_fixed(" << sum_target(sm, "i") << ", (double)" << sm << "_i);\n";
+    for (auto& sm : sums) o << "        gbx_add_fixed_f(" << sum_target(sm, "i") << ", " << sm << "_i);\n";
     o << "      }\n";
     o << "      cur = I;\n      i = I * 32 + lane;\n      iok = i < a.n;\n      const int ii = iok ? i : 0;\n";
     o << "      xi = a.pos[ii];\n";
@@ -406,7 +419,6 @@ std::string generate(const CustomPlan& p) {
     o << "    const bool diag = I == J;\n";
     o << "    const int j0 = J * 32 + lane;\n    const int jj = j0 < a.n ? j0 : 0;\n";
     o << "    float4 xj = a.pos[jj];\n";
-    o << "    int jn = j0;\n";  // the particle this lane's j data belongs to, rotated with it
     for (auto& in : inputs) o << "    float " << in << "_j = " << array_of(in) << "[" << in.substr(1) << " * a.n + jj];\n";
     for (auto& sm : sums) o << "    float " << sm << "_j = 0.f;\n";
     if (p.excluding) {
@@ -418,63 +430,95 @@ std::string generate(const CustomPlan& p) {
     }
     o << "    float et = 0.f;\n";
     for (int k = 0; k < npd; ++k) o << "    float pdt" << k << " = 0.f;\n";
-    o << "    for (int k = 0; k < 32; ++k) {\n";
-    o << "      const int jl = (lane + k) & 31;\n      const int j = J * 32 + jl;\n";
-    o << "      if (iok && j < a.n && (!diag || (k >= 1 && (k < 16 || lane < 16)))) {\n";
-    o << "        float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;\n";
-    o << "        if (a.periodic) {\n          dx -= a.L[0] * floorf(dx * a.iL[0] + 0.5f);\n          dy -= a.L[1] * "
-         "floorf(dy * a.iL[1] + 0.5f);\n          dz -= a.L[2] * floorf(dz * a.iL[2] + 0.5f);\n        }\n";
-    o << "        const float r2 = dx * dx + dy * dy + dz * dz;\n";
-    o << "        if (a.cutoff2 <= 0.f || r2 < a.cutoff2) {\n";
-    o << "          const float r = sqrtf(r2);\n";
-    if (p.excluding) o << "          const bool excluded = (xmask >> jl) & 1u;\n";
-    // atom 1 is the lower index (CharmmReferenceGBMV.cpp:281-283)
-    o << "          const bool lo = i < j;\n";
-    auto side = [&](const std::string& a_name, const std::string& b_name, const std::string& in) {
-      o << "          const float " << a_name << " = lo ? " << in << "_i : " << in << "_j;\n";
-      o << "          const float " << b_name << " = lo ? " << in << "_j : " << in << "_i;\n";
-    };
-    for (int k : up) side("pa" + std::to_string(k), "pb" + std::to_string(k), "p" + std::to_string(k));
-    for (int k : uv) side("va" + std::to_string(k), "vb" + std::to_string(k), "v" + std::to_string(k));
-    for (int k : ui) side("Ia" + std::to_string(k), "Ib" + std::to_string(k), "I" + std::to_string(k));
-    expr::SharedEmitter pe(nm.pair, true, "u", "          ");
-    std::ostringstream acc;
-    acc << "          float dEdr = 0.f;\n";
-    for (size_t t = 0; t < p.terms.size(); ++t) {
-      if (p.term_types[t] == 0) continue;
-      // ParticlePair: an excluded pair contributes nothing
-      const bool skip = p.excluding && p.term_types[t] == 1;
-      auto W = [&](const std::string& x) { return skip ? "(excluded ? 0.f : " + x + ")" : x; };
-      acc << "          et += " << W(pe(p.terms[t])) << ";\n";
-      acc << "          dEdr += " << W(pe(D(p.terms[t], "r"))) << ";\n";
-      auto both = [&](const std::string& sname, const std::string& base) {
-        const std::string d1 = W(pe(D(p.terms[t], base + "1"))), d2 = W(pe(D(p.terms[t], base + "2")));
-        acc << "          " << sname << "_i += lo ? " << d1 << " : " << d2 << ";\n";
-        acc << "          " << sname << "_j += lo ? " << d2 << " : " << d1 << ";\n";
+    // one pair: `full` for a whole off-diagonal tile (i < j always, every
+    // particle present), else the general case with the ordering selects
+    auto pair_body = [&](bool full, const std::string& ind) {
+      std::ostringstream b;
+      b << ind << "float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;\n";
+      if (p.periodic)
+        b << ind << "dx -= a.L[0] * floorf(dx * a.iL[0] + 0.5f);\n" << ind
+          << "dy -= a.L[1] * floorf(dy * a.iL[1] + 0.5f);\n" << ind << "dz -= a.L[2] * floorf(dz * a.iL[2] + 0.5f);\n";
+      b << ind << "const float r2 = dx * dx + dy * dy + dz * dz;\n";
+      std::string in2 = ind;
+      if (p.cutoff) {
+        b << ind << "if (r2 < a.cutoff2) {\n";
+        in2 += "  ";
+      }
+      b << in2 << "const float r = sqrtf(r2);\n";
+      if (p.excluding) b << in2 << "const bool excluded = (xmask >> jl) & 1u;\n";
+      // atom 1 is the lower index (CharmmReferenceGBMV.cpp:281-283)
+      if (!full) b << in2 << "const bool lo = i < j;\n";
+      auto side = [&](const std::string& a_name, const std::string& b_name, const std::string& in) {
+        if (full) {
+          b << in2 << "const float " << a_name << " = " << in << "_i, " << b_name << " = " << in << "_j;\n";
+        } else {
+          b << in2 << "const float " << a_name << " = lo ? " << in << "_i : " << in << "_j;\n";
+          b << in2 << "const float " << b_name << " = lo ? " << in << "_j : " << in << "_i;\n";
+        }
       };
-      for (int k : uv) both("gV" + std::to_string(k), s.value_names[k]);
-      for (int k : ui) both("gI" + std::to_string(k), s.integrals[k]);
-      for (int k = 0; k < npd; ++k)
-        acc << "          pdt" << k << " += " << W(pe(D(p.terms[t], s.globals[p.pd_index[k]]))) << ";\n";
-    }
-    o << pe.take_decls() << acc.str();
-    // F_i = -dE/dx_i = -(dE/dr) (x_i - x_j) / r, and F_j the opposite
-    o << "          const float sr = dEdr / r;\n";
-    o << "          fx_i -= sr * dx;\n          fy_i -= sr * dy;\n          fz_i -= sr * dz;\n";
-    o << "          fx_j += sr * dx;\n          fy_j += sr * dy;\n          fz_j += sr * dz;\n";
-    o << "        }\n      }\n";
-    o << "      if (diag && k == 16) break;\n";
+      for (int k : up) side("pa" + std::to_string(k), "pb" + std::to_string(k), "p" + std::to_string(k));
+      for (int k : uv) side("va" + std::to_string(k), "vb" + std::to_string(k), "v" + std::to_string(k));
+      for (int k : ui) side("Ia" + std::to_string(k), "Ib" + std::to_string(k), "I" + std::to_string(k));
+      expr::SharedEmitter pe(nm.pair, true, "u", in2);
+      std::ostringstream acc;
+      acc << in2 << "float dEdr = 0.f;\n";
+      for (size_t t = 0; t < p.terms.size(); ++t) {
+        if (p.term_types[t] == 0) continue;
+        // ParticlePair: an excluded pair contributes nothing
+        const bool skip = p.excluding && p.term_types[t] == 1;
+        auto W = [&](const std::string& x) { return skip ? "(excluded ? 0.f : " + x + ")" : x; };
+        acc << in2 << "et += " << W(pe(p.terms[t])) << ";\n";
+        acc << in2 << "dEdr += " << W(pe(D(p.terms[t], "r"))) << ";\n";
+        auto both = [&](const std::string& sname, const std::string& base) {
+          const std::string d1 = W(pe(D(p.terms[t], base + "1"))), d2 = W(pe(D(p.terms[t], base + "2")));
+          if (full) {
+            acc << in2 << sname << "_i += " << d1 << ";\n" << in2 << sname << "_j += " << d2 << ";\n";
+          } else {
+            acc << in2 << sname << "_i += lo ? " << d1 << " : " << d2 << ";\n";
+            acc << in2 << sname << "_j += lo ? " << d2 << " : " << d1 << ";\n";
+          }
+        };
+        for (int k : uv) both("gV" + std::to_string(k), s.value_names[k]);
+        for (int k : ui) both("gI" + std::to_string(k), s.integrals[k]);
+        for (int k = 0; k < npd; ++k)
+          acc << in2 << "pdt" << k << " += " << W(pe(D(p.terms[t], s.globals[p.pd_index[k]]))) << ";\n";
+      }
+      b << pe.take_decls() << acc.str();
+      // F_i = -dE/dx_i = -(dE/dr) (x_i - x_j) / r, and F_j the opposite
+      b << in2 << "const float sr = dEdr / r;\n";
+      b << in2 << "fx_i -= sr * dx;\n" << in2 << "fy_i -= sr * dy;\n" << in2 << "fz_i -= sr * dz;\n";
+      b << in2 << "fx_j += sr * dx;\n" << in2 << "fy_j += sr * dy;\n" << in2 << "fz_j += sr * dz;\n";
+      if (p.cutoff) b << ind << "}\n";
+      return b.str();
+    };
+    o << "    if (!diag && J * 32 + 32 <= a.n) {\n";
+    o << "      for (int k = 0; k < 32; ++k) {\n";
+    if (p.excluding) o << "        const int jl = (lane + k) & 31;\n";
+    o << pair_body(true, "        ");
     o << rot;
+    o << "      }\n";
+    o << "    } else {\n";
+    o << "      for (int k = 0; k < 32; ++k) {\n";
+    o << "        const int jl = (lane + k) & 31;\n        const int j = J * 32 + jl;\n";
+    o << "        if (iok && j < a.n && (!diag || (k >= 1 && (k < 16 || lane < 16)))) {\n";
+    o << pair_body(false, "          ");
+    o << "        }\n";
+    o << "        if (diag && k == 16) break;\n";
+    o << rot;
+    o << "      }\n";
     o << "    }\n";
     o << "    e += (double)et;\n";
     for (int k = 0; k < npd; ++k) o << "    pdp" << k << " += (double)pdt" << k << ";\n";
+    // the j data's particle after the rotations: 32 steps bring it back, a
+    // diagonal tile stops after 16
+    o << "    const int jn = J * 32 + ((lane + (diag ? 16 : 0)) & 31);\n";
     o << "    if (jn < a.n) {\n";
-    for (auto& sm : sums) o << "      gbx_add_fixed(" << sum_target(sm, "jn") << ", (double)" << sm << "_j);\n";
+    for (auto& sm : sums) o << "      gbx_add_fixed_f(" << sum_target(sm, "jn") << ", " << sm << "_j);\n";
     o << "    }\n";
     o << "    if (++J == nt) { ++I; J = I; }\n";
     o << "  }\n";
     o << "  if (iok) {\n";
-    for (auto& sm : sums) o << "    gbx_add_fixed(" << sum_target(sm, "i") << ", (double)" << sm << "_i);\n";
+    for (auto& sm : sums) o << "    gbx_add_fixed_f(" << sum_target(sm, "i") << ", " << sm << "_i);\n";
     o << "  }\n";
     o << block_sum("e", "a.energy_part[blockIdx.x]");
     for (int k = 0; k < npd; ++k)
@@ -663,6 +707,8 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
   bool pair_with_exclusions = false;
   for (int t : plan->term_types) pair_with_exclusions = pair_with_exclusions || t == 1;
   plan->excluding = !spec.exclusions.empty() && pair_with_exclusions;
+  plan->cutoff = ctx->cfg.cutoff > 0;
+  plan->periodic = ctx->cfg.periodic != 0;
   // exclusions as 32 x 32 bit masks of the tile pairs (I <= J) that hold
   // any: bit b of word l excludes particle l of tile I with particle b of
   // tile J (on a diagonal tile both ways)
@@ -708,9 +754,9 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
             nv = (int)spec.value_names.size();
   plan->value_blocks = (n + kValueThreads - 1) / kValueThreads;
   {
-    // tile pairs over warps: up to 16 warps per multiprocessor
+    // tile pairs over warps: up to 32 warps per multiprocessor
     const long long nt = (n + 31) / 32, tiles = nt * (nt + 1) / 2;
-    const long long warps = std::min<long long>(tiles, 16LL * std::max(ctx->sms, 1));
+    const long long warps = std::min<long long>(tiles, 32LL * std::max(ctx->sms, 1));
     plan->pair_blocks = (int)((warps + kPairThreads / 32 - 1) / (kPairThreads / 32));
   }
   GBX_TRY_CUSTOM(alloc(ctx, &plan->d_params, (size_t)np * n));

@@ -414,6 +414,15 @@ std::string SharedEmitter::take_decls() {
 
 std::string SharedEmitter::operator()(const Ptr& e) { return node(e); }
 
+std::string SharedEmitter::intern(const std::string& text) {
+  auto same = by_text_.find(text);
+  if (same != by_text_.end()) return same->second;
+  const std::string name = prefix_ + std::to_string(by_text_.size());
+  by_text_[text] = name;
+  decls_ += indent_ + "const " + (fp32_ ? "float " : "double ") + name + " = " + text + ";\n";
+  return name;
+}
+
 std::string SharedEmitter::node(const Ptr& e) {
   if (e->op == Op::Const || e->op == Op::Var) return emit(e, rename_, fp32_);
   auto hit = by_node_.find(e.get());
@@ -421,6 +430,25 @@ std::string SharedEmitter::node(const Ptr& e) {
   // the node's text over its children's names
   std::vector<std::string> a;
   for (auto& x : e->args) a.push_back(node(x));
+  if (fp32_ && e->op == Op::Div && e->args[1]->op != Op::Const) {
+    // FP32 quotients share one reciprocal per denominator (the generated
+    // FP32 code is compiled with fast math, where a quotient is a
+    // reciprocal and a product anyway)
+    // 1 / (x x) as the square of 1 / x (one reciprocal serves both)
+    const Ptr& den = e->args[1];
+    std::string r;
+    if (den->op == Op::Mul && den->args[0]->op != Op::Const && node(den->args[0]) == node(den->args[1])) {
+      const std::string rx = intern("(1.0f / " + node(den->args[0]) + ")");
+      r = intern("(" + rx + " * " + rx + ")");
+    } else {
+      r = intern("(1.0f / " + a[1] + ")");
+    }
+    const bool one = e->args[0]->op == Op::Const && e->args[0]->value == 1.0;
+    const std::string name = one ? r : intern("(" + a[0] + " * " + r + ")");
+    by_node_[e.get()] = name;
+    keep_.push_back(e);
+    return name;
+  }
   std::vector<Ptr> leaves;
   for (size_t k = 0; k < a.size(); ++k) leaves.push_back(variable("\x01" + std::to_string(k)));
   std::map<std::string, std::string> rn;
@@ -429,16 +457,7 @@ std::string SharedEmitter::node(const Ptr& e) {
   shell.args.clear();
   for (size_t k = 0; k < e->args.size(); ++k)
     shell.args.push_back(e->args[k]->op == Op::Const ? e->args[k] : leaves[k]);
-  const std::string text = emit(std::make_shared<const Node>(shell), rn, fp32_);
-  std::string name;
-  auto same = by_text_.find(text);
-  if (same != by_text_.end()) {
-    name = same->second;
-  } else {
-    name = prefix_ + std::to_string(by_text_.size());
-    by_text_[text] = name;
-    decls_ += indent_ + "const " + (fp32_ ? "float " : "double ") + name + " = " + text + ";\n";
-  }
+  const std::string name = intern(emit(std::make_shared<const Node>(shell), rn, fp32_));
   by_node_[e.get()] = name;
   keep_.push_back(e);
   return name;

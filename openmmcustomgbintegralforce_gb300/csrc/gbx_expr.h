@@ -57,6 +57,7 @@ class SharedEmitter {
 
  private:
   std::string node(const Ptr& e);
+  std::string intern(const std::string& text);  // the temporary holding `text`, declared on first use
   const std::map<std::string, std::string>& rename_;
   bool fp32_;
   std::string prefix_, indent_, decls_;
