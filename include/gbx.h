@@ -153,7 +153,8 @@ GBX_API gbx_status gbx_set_particle_parameters(gbx_context* ctx, const double* c
  * and every per-particle quantity with the suffix 1 or 2 (atom 1 is the
  * lower index).  GBX_TERM_PAIR terms skip the excluded pairs,
  * GBX_TERM_PAIR_NO_EXCLUSIONS terms do not (CharmmReferenceGBMV.cpp:196-200).
- * One or two integrals; computed values are SingleParticle.  Per-particle
+ * Tabulated functions of one variable (Continuous1DFunction) may appear in
+ * any expression.  One or two integrals; computed values are SingleParticle.  Per-particle
  * parameters must include "radius" (GBSWIntegral.cpp:79-80); x, y and z name
  * no parameter or global.  gbx_adjoint is not available here.  Zero-fill
  * the struct before setting it: fields added later default to none.
@@ -178,6 +179,15 @@ typedef struct {
   const int* exclusions; /* [num_exclusions][2] particle pairs */
   int num_param_derivs;  /* addEnergyParameterDerivative (CharmmGBMVForce.h:258): globals whose */
   const char* const* param_deriv_names; /* energy derivative gbx_get_custom_param_derivs reports */
+  /* addTabulatedFunction (CharmmGBMVForce.h:442) with OpenMM's Continuous1DFunction: a natural
+   * cubic spline through function_sizes[k] (>= 2) values at evenly spaced points from
+   * function_ranges[2k] to function_ranges[2k+1], zero outside that range; called by name with
+   * one argument in any expression.  Values of all functions concatenated. */
+  int num_functions;
+  const char* const* function_names;
+  const int* function_sizes;
+  const double* function_values;
+  const double* function_ranges;
 } gbx_custom;
 
 GBX_API gbx_status gbx_create_custom(const gbx_config* cfg, int num_atoms, const gbx_custom* custom,

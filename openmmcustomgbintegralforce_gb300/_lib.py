@@ -356,6 +356,9 @@ class GbxCustom(ctypes.Structure):
         ("term_types", ctypes.POINTER(ctypes.c_int)),
         ("num_exclusions", ctypes.c_int), ("exclusions", ctypes.POINTER(ctypes.c_int)),
         ("num_param_derivs", ctypes.c_int), ("param_deriv_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("num_functions", ctypes.c_int), ("function_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("function_sizes", ctypes.POINTER(ctypes.c_int)), ("function_values", ctypes.POINTER(ctypes.c_double)),
+        ("function_ranges", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -400,7 +403,17 @@ def custom_struct(custom: dict):
     pd = list(custom.get("param_derivs", []))
     c.num_param_derivs = len(pd)
     c.param_deriv_names = strs(pd)
-    keep += [gv, io, tt, ea]
+    fns = list(custom.get("functions", {}).items())  # name -> (values, min, max)
+    fv = [float(v) for _, (vals_, _, _) in fns for v in vals_]
+    fs = (ctypes.c_int * max(1, len(fns)))(*[len(vals_) for _, (vals_, _, _) in fns])
+    fva = (ctypes.c_double * max(1, len(fv)))(*fv)
+    fr = (ctypes.c_double * max(1, 2 * len(fns)))(*[float(x) for _, (_, lo, hi) in fns for x in (lo, hi)])
+    c.num_functions = len(fns)
+    c.function_names = strs([k for k, _ in fns])
+    c.function_sizes = fs
+    c.function_values = fva
+    c.function_ranges = fr
+    keep += [gv, io, tt, ea, fs, fva, fr]
     return c, keep
 
 
@@ -420,10 +433,11 @@ class CustomContext(Context):
     them "radius"), ``globals`` ({name: value}), ``integrals`` ([(name,
     order)]), ``values`` ([(name, expression)]) and ``terms`` ([(expression,
     TERM_SINGLE | TERM_PAIR | TERM_PAIR_NO_EXCLUSIONS)]), and optionally
-    ``exclusions`` ([(i, j)], skipped by TERM_PAIR terms) and
+    ``exclusions`` ([(i, j)], skipped by TERM_PAIR terms),
     ``param_derivs`` ([global names] whose energy derivative
-    ``param_derivs()`` returns).  The integral class, quadrature and table
-    come from ``model``."""
+    ``param_derivs()`` returns) and ``functions`` ({name: (values, min,
+    max)}: Continuous1DFunction tables, called by name in any expression).
+    The integral class, quadrature and table come from ``model``."""
 
     def __init__(self, model: GBModel, num_atoms: int, custom: dict):
         self.lib = load()

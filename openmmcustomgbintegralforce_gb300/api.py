@@ -120,6 +120,26 @@ class CharmmGBSWForce:
         return p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
 
 
+class Continuous1DFunction:
+    """OpenMM's tabulated function of one variable: a natural cubic spline
+    through ``values`` at evenly spaced points from ``min`` to ``max``, zero
+    outside that range (the only TabulatedFunction type the compiled
+    expressions take)."""
+
+    def __init__(self, values, min, max):
+        self.setFunctionParameters(values, min, max)
+
+    def getFunctionParameters(self):
+        return list(self._values), self._min, self._max
+
+    def setFunctionParameters(self, values, min, max):
+        if len(values) < 2:
+            raise OpenMMException("Continuous1DFunction: must have at least two points")
+        if max <= min:
+            raise OpenMMException("Continuous1DFunction: max <= min for a tabulated function.")
+        self._values, self._min, self._max = [float(v) for v in values], float(min), float(max)
+
+
 class CharmmGBMVForce:
     """CustomGBForce-style GB force with GB integrals (CharmmGBMVForce.h:63-526)."""
 
@@ -280,6 +300,19 @@ class CharmmGBMVForce:
         self._terms.append([expression, int(type)])
         return len(self._terms) - 1
 
+    # --- tabulated functions (CharmmGBMVForce.h:434-463)
+    def addTabulatedFunction(self, name, function):
+        self._functions.append([name, function])
+        return len(self._functions) - 1
+
+    def getTabulatedFunction(self, index):
+        _assert_index(index, self._functions)
+        return self._functions[index][1]
+
+    def getTabulatedFunctionName(self, index):
+        _assert_index(index, self._functions)
+        return self._functions[index][0]
+
     def getEnergyTermParameters(self, index):
         _assert_index(index, self._terms)
         return tuple(self._terms[index])
@@ -364,9 +397,15 @@ def custom_spec(force: CharmmGBMVForce) -> dict:
     """The force's expressions as a gbx_create_custom description: computed
     values SingleParticle; energy terms SingleParticle, ParticlePair (skips
     the force's exclusions) or ParticlePairNoExclusions; the globals named
-    by addEnergyParameterDerivative."""
-    if force.getNumTabulatedFunctions():
-        raise GBXError(4, "tabulated functions are not supported by the compiled expressions")
+    by addEnergyParameterDerivative; its tabulated functions
+    (Continuous1DFunction)."""
+    functions = {}
+    for k in range(force.getNumTabulatedFunctions()):
+        fn = force.getTabulatedFunction(k)
+        if not isinstance(fn, Continuous1DFunction):
+            raise GBXError(4, "only Continuous1DFunction tabulated functions are supported by the compiled expressions")
+        values, lo, hi = fn.getFunctionParameters()
+        functions[force.getTabulatedFunctionName(k)] = (values, lo, hi)
     if force.getGBIntegralType() == CustomIntegral:
         raise GBXError(4, "CustomIntegral has no implementation")
     names = [force.getPerParticleParameterName(i) for i in range(force.getNumPerParticleParameters())]
@@ -395,7 +434,8 @@ def custom_spec(force: CharmmGBMVForce) -> dict:
     return {"params": names, "globals": globals_, "integrals": integrals, "values": values, "terms": terms,
             "exclusions": [force.getExclusionParticles(k) for k in range(force.getNumExclusions())],
             "param_derivs": [force.getEnergyParameterDerivativeName(k)
-                             for k in range(force.getNumEnergyParameterDerivatives())]}
+                             for k in range(force.getNumEnergyParameterDerivatives())],
+            "functions": functions}
 
 
 class CalcCharmmGBSWForceKernel:

@@ -6,6 +6,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cctype>
+#include <cmath>
 #include <new>
 #include <string>
 #include <vector>
@@ -898,6 +900,31 @@ gbx_status custom_spec_of(const gbx_custom* cu, gbx::gbx_custom_spec& spec, std:
     for (const auto& nm : *names)
       if (nm == "x" || nm == "y" || nm == "z")
         return why = "x, y and z are the particle's coordinates, not parameter names", GBX_ERR_INVALID_ARGUMENT;
+  if (cu->num_functions < 0 ||
+      (cu->num_functions > 0 &&
+       (!cu->function_names || !cu->function_sizes || !cu->function_values || !cu->function_ranges)))
+    return why = "tabulated functions need their names, sizes, values and ranges", GBX_ERR_INVALID_ARGUMENT;
+  size_t off = 0;
+  for (int k = 0; k < cu->num_functions; ++k) {
+    gbx::gbx_custom_spec::Function f;
+    f.name = str(cu->function_names[k]);
+    bool ident = !f.name.empty() && (std::isalpha((unsigned char)f.name[0]) || f.name[0] == '_');
+    for (char ch : f.name) ident = ident && (std::isalnum((unsigned char)ch) || ch == '_');
+    if (!ident) return why = "tabulated function name '" + f.name + "' is not an identifier", GBX_ERR_INVALID_ARGUMENT;
+    const int m = cu->function_sizes[k];
+    f.x0 = cu->function_ranges[2 * k];
+    f.x1 = cu->function_ranges[2 * k + 1];
+    // Continuous1DFunction needs at least two values and max > min
+    if (m < 2 || !(f.x1 > f.x0) || !std::isfinite(f.x0) || !std::isfinite(f.x1))
+      return why = "tabulated function '" + f.name + "' needs at least 2 values and max > min", GBX_ERR_INVALID_ARGUMENT;
+    f.y.assign(cu->function_values + off, cu->function_values + off + m);
+    off += (size_t)m;
+    for (double v : f.y)
+      if (!std::isfinite(v)) return why = "tabulated function '" + f.name + "' has a non-finite value", GBX_ERR_INVALID_ARGUMENT;
+    for (const auto& g : spec.functions)
+      if (g.name == f.name) return why = "tabulated function '" + f.name + "' defined twice", GBX_ERR_INVALID_ARGUMENT;
+    spec.functions.push_back(std::move(f));
+  }
   if (std::find(spec.params.begin(), spec.params.end(), std::string("radius")) == spec.params.end())
     return why = "the per-particle parameter 'radius' must be defined", GBX_ERR_INVALID_ARGUMENT;
   return GBX_OK;

@@ -30,6 +30,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -162,6 +163,21 @@ __device__ __forceinline__ void gbx_add_fixed_f(unsigned long long* p, float v) 
   const long long q = gbx_fixed_f(v);
   if (q) atomicAdd(p, (unsigned long long)q);
 }
+// A tabulated function (natural cubic spline, zero outside [x0, x1]) and its
+// first and second derivatives: interval i holds c0 + u (c1 + u (c2 + u c3))
+// in u = (x - x_i) / h
+template <class T, int D>
+__device__ __forceinline__ T gbx_spline(const T* __restrict__ c, int intervals, T x0, T x1, T ih, T x) {
+  if (!(x >= x0 && x <= x1)) return T(0);
+  const T s = (x - x0) * ih;
+  int i = (int)s;
+  i = i < intervals - 1 ? i : intervals - 1;
+  const T u = s - (T)i;
+  const T* k = c + 4 * i;
+  if (D == 0) return k[0] + u * (k[1] + u * (k[2] + u * k[3]));
+  if (D == 1) return (k[1] + u * ((T)2 * k[2] + (T)3 * u * k[3])) * ih;
+  return ((T)2 * k[2] + (T)6 * u * k[3]) * ih * ih;
+}
 )";
 
 constexpr int kValueThreads = 256;
@@ -245,6 +261,69 @@ std::string block_sum(const std::string& v, const std::string& out) {
          "  if (threadIdx.x == 0) " + out + " = s_e[0];\n  __syncthreads();\n";
 }
 
+// Natural cubic spline through evenly spaced values (second derivatives M
+// from the tridiagonal system M[i-1] + 4 M[i] + M[i+1] = 6 (y[i+1] - 2 y[i]
+// + y[i-1]) / h^2 with M = 0 at both ends, the standard construction OpenMM
+// documents for Continuous1DFunction), as four power-form coefficients per
+// interval in u = (x - x_i) / h.
+std::vector<double> spline_coefficients(const gbx_custom_spec::Function& f) {
+  const int n = (int)f.y.size();
+  const double h = (f.x1 - f.x0) / (n - 1);
+  std::vector<double> M(n, 0.0), cp(n, 0.0), dp(n, 0.0);
+  for (int i = 1; i < n - 1; ++i) {
+    const double rhs = 6.0 * (f.y[i + 1] - 2.0 * f.y[i] + f.y[i - 1]) / (h * h);
+    const double den = 4.0 - cp[i - 1];
+    cp[i] = 1.0 / den;
+    dp[i] = (rhs - dp[i - 1]) / den;
+  }
+  for (int i = n - 2; i >= 1; --i) M[i] = dp[i] - cp[i] * M[i + 1];
+  std::vector<double> c;
+  const double h6 = h * h / 6.0;
+  for (int i = 0; i + 1 < n; ++i) {
+    c.push_back(f.y[i]);
+    c.push_back((f.y[i + 1] - f.y[i]) - h6 * (2.0 * M[i] + M[i + 1]));
+    c.push_back(3.0 * h6 * M[i]);
+    c.push_back(h6 * (M[i + 1] - M[i]));
+  }
+  return c;
+}
+
+// Each tabulated function's coefficients (FP64 and FP32 copies) and
+// gbx_tab_<name>_<derivative>(x) in both precisions.
+std::string tabulated_source(const gbx_custom_spec& s) {
+  std::ostringstream o;
+  char buf[64];
+  auto d = [&](double v) {
+    std::snprintf(buf, sizeof(buf), "%.17g", v);
+    return std::string(buf);
+  };
+  auto f = [&](double v) {
+    std::snprintf(buf, sizeof(buf), "%.9ef", (double)(float)v);
+    return std::string(buf);
+  };
+  for (size_t k = 0; k < s.functions.size(); ++k) {
+    const auto& fn = s.functions[k];
+    const std::vector<double> c = spline_coefficients(fn);
+    const int intervals = (int)fn.y.size() - 1;
+    const double ih = intervals / (fn.x1 - fn.x0);
+    const std::string K = std::to_string(k);
+    o << "__device__ const double gbx_tcd_" << K << "[" << c.size() << "] = {";
+    for (size_t q = 0; q < c.size(); ++q) o << (q ? ", " : "") << d(c[q]);
+    o << "};\n__device__ const float gbx_tcf_" << K << "[" << c.size() << "] = {";
+    for (size_t q = 0; q < c.size(); ++q) o << (q ? ", " : "") << f(c[q]);
+    o << "};\n";
+    for (int D = 0; D < 3; ++D) {
+      o << "__device__ __forceinline__ double gbx_tab_" << fn.name << "_" << D << "(double x) { return gbx_spline<double, "
+        << D << ">(gbx_tcd_" << K << ", " << intervals << ", " << d(fn.x0) << ", " << d(fn.x1) << ", " << d(ih)
+        << ", x); }\n";
+      o << "__device__ __forceinline__ float gbx_tab_" << fn.name << "_" << D << "(float x) { return gbx_spline<float, "
+        << D << ">(gbx_tcf_" << K << ", " << intervals << ", " << f(fn.x0) << ", " << f(fn.x1) << ", " << f(ih)
+        << ", x); }\n";
+    }
+  }
+  return o.str();
+}
+
 std::string generate(const CustomPlan& p) {
   const gbx_custom_spec& s = p.spec;
   const int np = (int)s.params.size(), ng = (int)s.globals.size(), ni = (int)s.integrals.size(),
@@ -253,7 +332,7 @@ std::string generate(const CustomPlan& p) {
   const char* kCoord[3] = {"x", "y", "z"};
   auto D = [](const expr::Ptr& e, const std::string& v) { return expr::derivative(e, v); };
   std::ostringstream o;
-  o << kArgsDecl << kPrelude;
+  o << kArgsDecl << kPrelude << tabulated_source(s);
 
   // ---- per-atom values, their derivatives, single-particle terms (FP64);
   // every expression and derivative shares its common subexpressions
@@ -656,8 +735,10 @@ gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec) {
   ctx->custom = plan;
   plan->spec = spec;
   try {
-    for (auto& e : spec.value_expressions) plan->values.push_back(expr::parse(e));
-    for (auto& e : spec.term_expressions) plan->terms.push_back(expr::parse(e));
+    std::set<std::string> fnames;
+    for (auto& f : spec.functions) fnames.insert(f.name);
+    for (auto& e : spec.value_expressions) plan->values.push_back(expr::parse(e, fnames));
+    for (auto& e : spec.term_expressions) plan->terms.push_back(expr::parse(e, fnames));
   } catch (const std::exception& e) {
     ctx->last_error = std::string("expression: ") + e.what();
     return GBX_ERR_INVALID_ARGUMENT;
@@ -958,8 +1039,10 @@ gbx_status custom_compile_only(const gbx_custom_spec& spec, std::string& log) {
   CustomPlan p;
   p.spec = spec;
   try {
-    for (auto& e : spec.value_expressions) p.values.push_back(expr::parse(e));
-    for (auto& e : spec.term_expressions) p.terms.push_back(expr::parse(e));
+    std::set<std::string> fnames;
+    for (auto& f : spec.functions) fnames.insert(f.name);
+    for (auto& e : spec.value_expressions) p.values.push_back(expr::parse(e, fnames));
+    for (auto& e : spec.term_expressions) p.terms.push_back(expr::parse(e, fnames));
     p.term_types = spec.term_types;
     auto reads_coords = [](const expr::Ptr& e) {
       std::vector<std::string> vars;

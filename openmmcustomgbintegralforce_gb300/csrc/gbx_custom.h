@@ -20,6 +20,12 @@ struct gbx_custom_spec {
   std::vector<int> integral_orders, term_types;  // term types: 0 single particle, 1 pair, 2 pair without exclusions
   std::vector<int> exclusions;                   // [pairs][2]
   std::vector<std::string> param_derivs;         // globals whose energy derivative is reported
+  struct Function {                              // Continuous1DFunction: natural cubic spline,
+    std::string name;                            // zero outside [x0, x1]
+    double x0 = 0.0, x1 = 1.0;
+    std::vector<double> y;                       // values at evenly spaced points
+  };
+  std::vector<Function> functions;
 };
 
 gbx_status custom_build(Context* ctx, const gbx_custom_spec& spec);

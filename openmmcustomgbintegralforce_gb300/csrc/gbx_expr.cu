@@ -97,7 +97,7 @@ Ptr pw(const Ptr& a, const Ptr& b) {
 // ---------------------------------------------------------------------------
 class Parser {
  public:
-  explicit Parser(const std::string& s) : s_(s) {}
+  Parser(const std::string& s, const std::set<std::string>& functions) : s_(s), functions_(functions) {}
   Ptr expression() {
     Ptr e = term();
     for (;;) {
@@ -191,6 +191,11 @@ class Parser {
           skip();
         }
         expect(')');
+        if (functions_.count(name)) {
+          if (args.size() != 1)
+            throw std::runtime_error("tabulated function " + name + " takes one argument " + where());
+          return make(Op::Func, std::move(args), 0.0, "@0:" + name);
+        }
         const bool unary_fn = unary_functions().count(name) != 0;
         const bool binary_fn = name == "min" || name == "max";
         const bool ternary_fn = name == "select";
@@ -213,6 +218,7 @@ class Parser {
     ++p_;
   }
   const std::string& s_;
+  const std::set<std::string>& functions_;
   size_t p_ = 0;
 };
 
@@ -259,7 +265,7 @@ std::string number(double v, bool fp32) {
 Ptr constant(double v) { return make(Op::Const, {}, v); }
 Ptr variable(const std::string& name) { return make(Op::Var, {}, 0.0, name); }
 
-Ptr parse(const std::string& text) {
+Ptr parse(const std::string& text, const std::set<std::string>& functions) {
   std::vector<std::string> parts;
   std::stringstream ss(text);
   std::string part;
@@ -273,12 +279,12 @@ Ptr parse(const std::string& text) {
     if (eq == std::string::npos) throw std::runtime_error("definition without '=': " + d);
     const std::string name = trim(d.substr(0, eq));
     const std::string body = d.substr(eq + 1);
-    Parser p(body);
+    Parser p(body, functions);
     Ptr e = p.expression();
     if (!p.at_end()) throw std::runtime_error("trailing characters " + p.where());
     defs[name] = e;
   }
-  Parser p(parts[0]);
+  Parser p(parts[0], functions);
   Ptr e = p.expression();
   if (!p.at_end()) throw std::runtime_error("trailing characters " + p.where());
   std::set<std::string> active;
@@ -331,7 +337,12 @@ Ptr derivative(const Ptr& e, const std::string& v) {
       const Ptr du = derivative(u, v);
       if (is_const(du, 0.0)) return constant(0.0);
       Ptr g;  // d f / d u
-      if (f == "sqrt") g = div(constant(0.5), e);
+      if (f[0] == '@') {
+        // a tabulated function: its next derivative (a cubic spline has two)
+        const int k = f[1] - '0';
+        if (k >= 2) throw std::runtime_error("third derivative of tabulated function " + f.substr(3) + " requested");
+        g = make(Op::Func, {u}, 0.0, "@" + std::to_string(k + 1) + ":" + f.substr(3));
+      } else if (f == "sqrt") g = div(constant(0.5), e);
       else if (f == "exp") g = e;
       else if (f == "log") g = div(constant(1.0), u);
       else if (f == "sin") g = func("cos", {u});
@@ -388,6 +399,7 @@ std::string emit(const Ptr& e, const std::map<std::string, std::string>& rename,
       std::vector<std::string> a;
       for (auto& x : e->args) a.push_back(emit(x, rename, fp32));
       const std::string& n = e->name;
+      if (n[0] == '@') return "gbx_tab_" + n.substr(3) + "_" + n.substr(1, 1) + "(" + a[0] + ")";
       if (n == "step") return "((" + a[0] + ") >= 0 ? " + number(1.0, fp32) + " : " + number(0.0, fp32) + ")";
       if (n == "square") return "gbx_ipow2(" + a[0] + ")";
       if (n == "cube") return "gbx_ipow3(" + a[0] + ")";

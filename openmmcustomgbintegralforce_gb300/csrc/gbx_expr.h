@@ -5,6 +5,7 @@
 
 #include <map>
 #include <memory>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -24,9 +25,12 @@ struct Node {
 };
 
 // Parses "expr" or "expr; name1 = def1; name2 = def2 ..." (definitions are
-// substituted, later ones may use earlier ones).  Throws std::runtime_error
-// with a message on a syntax error or an unknown function.
-Ptr parse(const std::string& text);
+// substituted, later ones may use earlier ones).  `functions` names the
+// force's tabulated functions of one variable; a call f(u) becomes a node
+// Op::Func named "@0:f" ("@k:f" is its k-th derivative).  Throws
+// std::runtime_error with a message on a syntax error or an unknown
+// function.
+Ptr parse(const std::string& text, const std::set<std::string>& functions = {});
 
 Ptr constant(double v);
 Ptr variable(const std::string& name);
@@ -39,7 +43,9 @@ void variables(const Ptr& e, std::vector<std::string>& out);
 
 // C source of the expression; every variable is rendered through `rename`
 // (a name missing from it throws).  `fp32` selects float literals and the
-// float forms of the math functions.
+// float forms of the math functions.  A tabulated function's k-th
+// derivative "@k:f" is the call gbx_tab_f_k(u), which the generated source
+// defines in FP64 and FP32.
 std::string emit(const Ptr& e, const std::map<std::string, std::string>& rename, bool fp32);
 
 // Emits several expressions with their common subexpressions formed once:

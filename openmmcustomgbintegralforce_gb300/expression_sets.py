@@ -4,7 +4,9 @@ tests and the benchmark).
 CANONICAL is the canonical CHARMM set written as user expressions.  MODIFIED
 is outside it: a per-atom scale of the Born radius through a second computed
 value, the solvent dielectric as a global parameter, an ACE-style nonpolar
-single-particle term and a Lepton definition in the pair term.
+single-particle term and a Lepton definition in the pair term.  EXTENDED
+adds coordinates, exclusions and energy parameter derivatives; TABULATED
+calls tabulated functions.
 """
 from openmmcustomgbintegralforce_gb300.spec import ONE_4PI_EPS0
 
@@ -69,3 +71,33 @@ def extended_exclusions(n, seed=0):
         if i + 2 < n and rng.random() < 0.5:
             out.add((i, i + 2))
     return sorted(out)
+
+
+def tabulated_functions():
+    """Two Continuous1DFunction tables: a smooth scaling of a radius over
+    [0.05, 3] nm, and a pair correction over [0, 2] nm that goes to zero
+    with zero slope at its upper end (beyond it the function is zero, so
+    the farther pairs of a 1,000-atom globule fall outside the table)."""
+    import numpy as np
+
+    x = np.linspace(0.05, 3.0, 40)
+    scale = 1.0 + 0.2 * np.sin(3.0 * x) * np.exp(-x)
+    r = np.linspace(0.0, 2.0, 61)
+    tail = 0.5 * np.exp(-r) * np.cos(3.0 * r) * (1.0 - (r / 2.0) ** 2) ** 2
+    return {"scale": (scale.tolist(), 0.05, 3.0), "tail": (tail.tolist(), 0.0, 2.0)}
+
+
+# Tabulated functions (addTabulatedFunction with Continuous1DFunction) in a
+# computed value, a single-particle term and a pair term.
+TABULATED = {
+    "params": ["q", "radius"],
+    "globals": {"alpha0": -0.180, "alpha1": 1.817},
+    "integrals": [("I4", 4), ("I7", 7)],
+    "values": [("B", "1/(alpha0*(1/0.05-I4)+alpha1*(1/(4*0.05^4)-I7)^(1/4))"),
+               ("Bt", "B*scale(B)")],
+    "terms": [(f"-0.5*{K}*(1-1/80)*q^2/Bt", 0),
+              ("0.01*scale(10*radius)", 0),
+              (f"-{K}*(1-1/80)*q1*q2/sqrt(r^2+Bt1*Bt2*exp(-r^2/(4*Bt1*Bt2)))", 2),
+              ("q1*q2*tail(r)", 2)],
+    "functions": tabulated_functions(),
+}

@@ -5,6 +5,7 @@
 #include <cctype>
 
 #include "openmm/OpenMMException.h"
+#include "openmm/TabulatedFunction.h"
 
 using OpenMM::CharmmGBMVForce;
 using OpenMM::CharmmGBSWForce;
@@ -253,11 +254,22 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     state.create(cfg, system.getNumParticles());
   } else {
     // the force's own expressions, compiled for the device
-    if (force.getNumTabulatedFunctions() > 0)
-      throw OpenMMException("GB300: tabulated functions are not supported");
-    std::vector<std::string> params, integrals, values, valueExprs, terms;
-    std::vector<double> globalValues;
-    std::vector<int> orders, types, exclusions;
+    std::vector<std::string> params, integrals, values, valueExprs, terms, functionNames;
+    std::vector<double> globalValues, functionValues, functionRanges;
+    std::vector<int> orders, types, exclusions, functionSizes;
+    // tabulated functions: Continuous1DFunction (a natural cubic spline, zero outside its range)
+    for (int k = 0; k < force.getNumTabulatedFunctions(); ++k) {
+      const auto* fn = dynamic_cast<const OpenMM::Continuous1DFunction*>(&force.getTabulatedFunction(k));
+      if (!fn) throw OpenMMException("GB300: only Continuous1DFunction tabulated functions are supported");
+      std::vector<double> v;
+      double lo = 0.0, hi = 0.0;
+      fn->getFunctionParameters(v, lo, hi);
+      functionNames.push_back(force.getTabulatedFunctionName(k));
+      functionSizes.push_back((int)v.size());
+      functionValues.insert(functionValues.end(), v.begin(), v.end());
+      functionRanges.push_back(lo);
+      functionRanges.push_back(hi);
+    }
     for (int k = 0; k < force.getNumPerParticleParameters(); ++k)
       params.push_back(force.getPerParticleParameterName(k));
     for (int k = 0; k < force.getNumGlobalParameters(); ++k) {
@@ -308,7 +320,7 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
       return p;
     };
     const auto pn = ptrs(params), gn = ptrs(globalNames), in = ptrs(integrals), vn = ptrs(values),
-               ve = ptrs(valueExprs), te = ptrs(terms), pd = ptrs(paramDerivNames);
+               ve = ptrs(valueExprs), te = ptrs(terms), pd = ptrs(paramDerivNames), fnn = ptrs(functionNames);
     gbx_custom cs{};
     cs.num_params = (int)params.size();
     cs.param_names = pn.data();
@@ -328,6 +340,11 @@ void GB300CalcCharmmGBMVForceKernel::initialize(const OpenMM::System& system, co
     cs.exclusions = exclusions.data();
     cs.num_param_derivs = (int)paramDerivNames.size();
     cs.param_deriv_names = pd.data();
+    cs.num_functions = (int)functionNames.size();
+    cs.function_names = fnn.data();
+    cs.function_sizes = functionSizes.data();
+    cs.function_values = functionValues.data();
+    cs.function_ranges = functionRanges.data();
     state.createCustom(cfg, system.getNumParticles(), cs);
   }
   copyParameters(force);

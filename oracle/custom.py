@@ -30,10 +30,38 @@ _FUNCS = {
 }
 
 
-def parse(text: str, names) -> sp.Expr:
-    """Lepton syntax ("expr; a = ...; b = ...") -> sympy, over the given variable names."""
+def tabulated(functions: dict) -> dict:
+    """sympy functions for a force's Continuous1DFunction tables ({name:
+    (values, min, max)}): the natural cubic spline through the evenly spaced
+    values (scipy's CubicSpline with bc_type="natural", an implementation
+    independent of the library's), zero outside [min, max]; differentiating
+    gives the spline's first and second derivatives."""
+    from scipy.interpolate import CubicSpline
+
+    out = {}
+    for name, (vals, lo, hi) in functions.items():
+        cs = CubicSpline(np.linspace(lo, hi, len(vals)), np.asarray(vals, float), bc_type="natural")
+        classes = []
+        for d in range(3):
+            f = cs if d == 0 else cs.derivative(d)
+
+            def impl(t, f=f, lo=lo, hi=hi):
+                t = np.asarray(t, float)
+                return np.where((t >= lo) & (t <= hi), f(np.clip(t, lo, hi)), 0.0)
+
+            classes.append(type(f"{name}_d{d}", (sp.Function,), {"nargs": 1, "_imp_": staticmethod(impl)}))
+        for d in range(2):
+            classes[d].fdiff = (lambda nxt: lambda self, argindex=1: nxt(self.args[0]))(classes[d + 1])
+        out[name] = classes[0]
+    return out
+
+
+def parse(text: str, names, functions=None) -> sp.Expr:
+    """Lepton syntax ("expr; a = ...; b = ...") -> sympy, over the given
+    variable names and tabulated functions (``tabulated``)."""
     parts = [p.strip() for p in text.split(";")]
     local = dict(_FUNCS)
+    local.update(functions or {})
     for n in names:
         local[n] = sp.Symbol(n)
 
@@ -70,7 +98,10 @@ class CustomOracle:
     exclusions.  Computed values and single-particle terms may read the
     atom's coordinates x, y, z (their gradients are forces,
     CharmmReferenceGBMV.cpp:232-262,409-435); ``param_derivs`` names globals
-    whose energy derivative is returned (:225-229,263-264,438-443)."""
+    whose energy derivative is returned (:225-229,263-264,438-443);
+    ``functions`` holds Continuous1DFunction tables ({name: (values, min,
+    max)}, CharmmReferenceKernels.cpp:187-191 hands them to Lepton as custom
+    functions)."""
 
     def __init__(self, model, custom):
         self.custom = custom
@@ -87,8 +118,9 @@ class CustomOracle:
         single_names = self.params + list(self.globals) + self.integrals + vnames + ["x", "y", "z"]
         pair_names = ["r"] + list(self.globals) + [f"{x}{s}" for x in self.params + self.integrals + vnames
                                                    for s in "12"]
-        self.vexpr = [parse(e, single_names) for _, e in self.values]
-        self.texpr = [(parse(e, single_names if t == 0 else pair_names), t) for e, t in self.terms]
+        fns = tabulated(custom.get("functions", {}))
+        self.vexpr = [parse(e, single_names, fns) for _, e in self.values]
+        self.texpr = [(parse(e, single_names if t == 0 else pair_names, fns), t) for e, t in self.terms]
 
     def energy_forces(self, pos, params):
         pos = np.ascontiguousarray(pos, dtype=np.float64)

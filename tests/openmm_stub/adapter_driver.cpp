@@ -226,6 +226,33 @@ int main() {
     EXPECT(cu.paramDerivWorkspace["kr"] == 1.0 && cu.paramDerivWorkspace["alpha1"] == 2.0);  // two steps summed
     dump("gbmv exclusions and energy parameter derivatives");
   }
+  g_log.clear();
+  {
+    // tabulated functions: Continuous1DFunction passes through, another type is refused
+    CharmmGBMVForce force;
+    canonical(force, CharmmGBMVForce::GBMVIntegralTypeII);
+    force.addTabulatedFunction("tail", new OpenMM::Continuous1DFunction({0.5, 0.25, 0.0}, 0.0, 3.0));
+    force.addTabulatedFunction("scale", new OpenMM::Continuous1DFunction({1.0, 2.0}, 0.05, 3.0));
+    force.addEnergyTerm("q1*q2*tail(r)", CharmmGBMVForce::ParticlePairNoExclusions);
+    KernelFactory* gf = cuda.factories["CalcCharmmGBMVForce"];
+    std::unique_ptr<KernelImpl> k(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
+    dynamic_cast<CalcCharmmGBMVForceKernel&>(*k).initialize(system, force);
+    EXPECT(logged("create_custom n=4 model=2 params q radius integrals I4:4 I7:7 values B terms 0 2 2 "
+                  "function tail n=3 [0,3] first=0.5 last=0 function scale n=2 [0.05,3] first=1 last=2"));
+    CharmmGBMVForce other;
+    canonical(other, CharmmGBMVForce::GBMVIntegralTypeII);
+    other.addTabulatedFunction("d", new OpenMM::Discrete1DFunction({1.0, 2.0}));
+    other.addEnergyTerm("d(q)", CharmmGBMVForce::SingleParticle);
+    std::unique_ptr<KernelImpl> k2(gf->createKernelImpl("CalcCharmmGBMVForce", cuda, context));
+    bool threw = false;
+    try {
+      dynamic_cast<CalcCharmmGBMVForceKernel&>(*k2).initialize(system, other);
+    } catch (const OpenMMException& e) {
+      threw = std::string(e.what()).find("Continuous1DFunction") != std::string::npos;
+    }
+    EXPECT(threw);
+    dump("gbmv tabulated functions");
+  }
   {
     CharmmGBMVForce force;
     canonical(force, CharmmGBMVForce::CustomIntegral);

@@ -84,6 +84,15 @@ gbx_status gbx_create_custom(const gbx_config* cfg, int n, const gbx_custom* cs,
     s += " param_derivs";
     for (int k = 0; k < cs->num_param_derivs; ++k) s += std::string(" ") + cs->param_deriv_names[k];
   }
+  size_t off = 0;
+  for (int k = 0; k < cs->num_functions; ++k) {
+    char b[160];
+    std::snprintf(b, sizeof(b), " function %s n=%d [%g,%g] first=%g last=%g", cs->function_names[k],
+                  cs->function_sizes[k], cs->function_ranges[2 * k], cs->function_ranges[2 * k + 1],
+                  cs->function_values[off], cs->function_values[off + cs->function_sizes[k] - 1]);
+    s += b;
+    off += (size_t)cs->function_sizes[k];
+  }
   log(s);
   return GBX_OK;
 }

@@ -2,6 +2,8 @@
 // the CustomGBForce-style accessors of CharmmGBMVForce (CharmmGBMVForce.h:
 // 63-526 in the reference plugin) that a kernel reads.
 #pragma once
+#include "openmm/TabulatedFunction.h"
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
@@ -21,7 +23,7 @@ class CharmmGBMVForce {
   int getNumEnergyTerms() const { return (int)terms_.size(); }
   int getNumExclusions() const { return (int)exclusions_.size(); }
   int getNumEnergyParameterDerivatives() const { return (int)derivs_.size(); }
-  int getNumTabulatedFunctions() const { return 0; }
+  int getNumTabulatedFunctions() const { return (int)functions_.size(); }
   NonbondedMethod getNonbondedMethod() const { return method_; }
   void setNonbondedMethod(NonbondedMethod m) { method_ = m; }
   double getCutoffDistance() const { return cutoff_; }
@@ -87,6 +89,13 @@ class CharmmGBMVForce {
       if (gnames_[k] == name) derivs_.push_back((int)k);
   }
   const std::string& getEnergyParameterDerivativeName(int index) const { return gnames_[derivs_[index]]; }
+  // the force takes ownership of the function (CharmmGBMVForce.h:434-442)
+  int addTabulatedFunction(const std::string& name, TabulatedFunction* function) {
+    functions_.push_back({name, std::shared_ptr<TabulatedFunction>(function)});
+    return (int)functions_.size() - 1;
+  }
+  const TabulatedFunction& getTabulatedFunction(int index) const { return *functions_[index].second; }
+  const std::string& getTabulatedFunctionName(int index) const { return functions_[index].first; }
 
  private:
   struct Expr {
@@ -105,6 +114,7 @@ class CharmmGBMVForce {
   std::vector<Integral> integrals_;
   std::vector<std::pair<int, int>> exclusions_;
   std::vector<int> derivs_;
+  std::vector<std::pair<std::string, std::shared_ptr<TabulatedFunction>>> functions_;
   GBIntegralType itype_ = GBSWIntegral;
   NonbondedMethod method_ = NoCutoff;
   double cutoff_ = 1.0;

@@ -2,9 +2,10 @@
 the canonical CHARMM set written as user expressions reproduces the
 canonical evaluation (CharmmReferenceGBSW's formulas) for the GBMV-II and
 GBSW-integral classes, and its forces are minus the gradient of its energy
-for an expression set outside the canonical one.  Also the library's own
-expression compiler on the CPU: every set compiles, and a wrong one is
-refused with a message (gbx_custom_check: no device needed)."""
+for expression sets outside the canonical one (tabulated functions
+included).  Also the library's own expression compiler on the CPU: every
+set compiles, and a wrong one is refused with a message (gbx_custom_check:
+no device needed)."""
 import copy
 
 import numpy as np
@@ -14,8 +15,8 @@ from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle import oracle as O
 from oracle.custom import CustomOracle
-from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, extended_exclusions,
-                                                               modified_params)
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, TABULATED,
+                                                               extended_exclusions, modified_params)
 
 
 @pytest.fixture(scope="module")
@@ -86,10 +87,41 @@ def test_extended_expressions_gradients(glob):
     assert abs(plain["energy"] / out["energy"] - 1) > 1e-4
 
 
+def test_tabulated_expressions_gradients(glob):
+    """Tabulated functions (natural cubic splines) in a computed value, a
+    single-particle term and a pair term: forces against FP64 central
+    differences of the oracle's energy; a pair beyond the table's range
+    gets nothing from it."""
+    from oracle.custom import tabulated
+
+    g = glob
+    m = GBModel.gbmv2(box=box_for(g.positions, margin=1.0))
+    P = np.stack([g.charge, g.radius], axis=1)
+    orc = CustomOracle(m, TABULATED)
+    out = orc.energy_forces(g.positions, P)
+    rng = np.random.default_rng(6)
+    h = 1e-6
+    F = out["forces"]
+    for flat in rng.choice(3 * g.n, size=6, replace=False):
+        i, d = int(flat) // 3, int(flat) % 3
+        xp, xm = g.positions.copy(), g.positions.copy()
+        xp[i, d] += h
+        xm[i, d] -= h
+        fd = -(orc.energy_forces(xp, P)["energy"] - orc.energy_forces(xm, P)["energy"]) / (2 * h)
+        assert abs(fd - F[i, d]) <= 1e-6 * np.abs(F).max() + 1e-5 * abs(F[i, d]), (i, d, fd, F[i, d])
+    tail = tabulated(TABULATED["functions"])["tail"]
+    import sympy as sp
+
+    f = sp.lambdify([sp.Symbol("t")], tail(sp.Symbol("t")), "numpy")
+    vals, lo, hi = TABULATED["functions"]["tail"]
+    assert np.allclose(f(np.linspace(lo, hi, len(vals))), vals, atol=1e-12)  # through its points
+    assert f(np.array([hi + 0.1, lo - 0.1])).tolist() == [0.0, 0.0]  # zero outside
+
+
 def test_library_compiles_and_refuses_expression_sets():
     from openmmcustomgbintegralforce_gb300._lib import check_custom
 
-    for s in (CANONICAL, MODIFIED):
+    for s in (CANONICAL, MODIFIED, dict(EXTENDED, exclusions=extended_exclusions(50)), TABULATED):
         st, msg = check_custom(s)
         if st == 4 and "NVRTC" in msg:
             pytest.skip("NVRTC not available")
@@ -105,3 +137,19 @@ def test_library_compiles_and_refuses_expression_sets():
     bad["params"] = ["q", "s"]
     st, msg = check_custom(bad)
     assert st != 0 and "radius" in msg
+    # tabulated functions: too few values, an empty range, a missing table, a wrong argument count
+    bad = copy.deepcopy(TABULATED)
+    bad["functions"]["scale"] = ([1.0], 0.0, 1.0)
+    st, msg = check_custom(bad)
+    assert st != 0 and "at least 2 values" in msg
+    bad["functions"]["scale"] = ([1.0, 2.0], 1.0, 1.0)
+    st, msg = check_custom(bad)
+    assert st != 0 and "max > min" in msg
+    bad = copy.deepcopy(TABULATED)
+    del bad["functions"]["tail"]
+    st, msg = check_custom(bad)
+    assert st != 0 and "tail" in msg
+    bad = copy.deepcopy(TABULATED)
+    bad["terms"][3] = ("q1*q2*tail(r, r)", 2)
+    st, msg = check_custom(bad)
+    assert st != 0 and "one argument" in msg

@@ -10,6 +10,8 @@ through the C ABI, against the FP64 custom-expression oracle
 * coordinates in a computed value and a single-particle term, exclusions
   skipped by a ParticlePair term only, and energy derivatives by globals
   (addEnergyParameterDerivative);
+* tabulated functions (Continuous1DFunction) in a computed value, a
+  single-particle term and a pair term;
 * a global parameter update, bit-reproducible calls, and a refused
   expression.
 
@@ -25,8 +27,8 @@ from openmmcustomgbintegralforce_gb300._lib import Context, CustomContext, GBXEr
 from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle.custom import CustomOracle
-from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, extended_exclusions,
-                                                               modified_params)
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, TABULATED,
+                                                               extended_exclusions, modified_params)
 
 pytestmark = pytest.mark.gpu
 
@@ -232,3 +234,55 @@ def test_kernel_mirror_exclusions_and_param_derivs(glob):
     assert sorted(pd) == sorted(EXTENDED["param_derivs"])
     for n, v in zip(EXTENDED["param_derivs"], ref["param_derivs"]):
         assert abs(pd[n] / v - 1) < E_TOL * 5
+
+
+@pytest.mark.parametrize("cls", ["gbmv2", "gbsw_integral"])
+def test_tabulated_set_vs_oracle(glob, cls):
+    """Natural cubic splines evaluated on the device (FP64 in the values,
+    FP32 in the pair terms) against scipy's in the oracle."""
+    g = glob
+    m = model_of(cls, g)
+    P = np.stack([g.charge, g.radius], axis=1)
+    ctx = CustomContext(m, g.n, TABULATED)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(g.positions)
+    E2, F2 = ctx.execute_host(g.positions)
+    assert E2 == E and np.array_equal(F2, F)
+    ref = CustomOracle(m, TABULATED).energy_forces(g.positions, P)
+    print(f"{cls} tabulated: energy {abs(E / ref['energy'] - 1):.2e} forces {rel_rms(F, ref['forces']):.2e}")
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    assert np.abs(ctx.born_radii() / ref["values"][0] - 1).max() < B_TOL
+    ctx.close()
+
+
+def test_kernel_mirror_tabulated_functions(glob):
+    """The GBMV kernel mirror passes Continuous1DFunction tables to the
+    compiled path."""
+    from openmmcustomgbintegralforce_gb300 import api
+
+    g = glob
+    f = api.CharmmGBMVForce()
+    for p in TABULATED["params"]:
+        f.addPerParticleParameter(p)
+    for k, v in TABULATED["globals"].items():
+        f.addGlobalParameter(k, v)
+    for name, (vals, lo, hi) in TABULATED["functions"].items():
+        f.addTabulatedFunction(name, api.Continuous1DFunction(vals, lo, hi))
+    for name, order in TABULATED["integrals"]:
+        f.addGBIntegral(name, [order], [])
+    for name, e in TABULATED["values"]:
+        f.addComputedValue(name, e, api.SingleParticle)
+    for e, t in TABULATED["terms"]:
+        f.addEnergyTerm(e, api.SingleParticle if t == 0 else api.ParticlePairNoExclusions)
+    f.setGBIntegralType(api.GBMVIntegralTypeII)
+    P = np.stack([g.charge, g.radius], axis=1)
+    for row in P:
+        f.addParticle(list(row))
+    box = box_for(g.positions, margin=1.0)
+    k = api.CalcCharmmGBMVForceKernel(box=box)
+    k.initialize(g.n, f)
+    E, F = k.execute(g.positions)
+    ref = CustomOracle(GBModel.gbmv2(box=box), TABULATED).energy_forces(g.positions, P)
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL

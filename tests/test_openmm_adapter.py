@@ -13,7 +13,8 @@ overflowed table surfacing as an OpenMMException, a force outside the
 canonical expression set handed to gbx_create_custom with its global
 parameters followed, a force's exclusions, term types and energy parameter
 derivatives passed on (the derivatives summed into the context's workspace
-each step), and the refusal of CustomIntegral.
+each step), Continuous1DFunction tables passed on and other tabulated
+function types refused, and the refusal of CustomIntegral.
 """
 import os
 import shutil
