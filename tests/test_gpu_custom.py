@@ -12,6 +12,8 @@ through the C ABI, against the FP64 custom-expression oracle
   (addEnergyParameterDerivative);
 * tabulated functions (Continuous1DFunction) in a computed value, a
   single-particle term and a pair term;
+* the pair kernel's tile edges: 1, 2, 31, 33, 64 and 97 particles with
+  exclusions inside and across tiles, with and without a cutoff;
 * a global parameter update, bit-reproducible calls, and a refused
   expression.
 
@@ -286,3 +288,29 @@ def test_kernel_mirror_tabulated_functions(glob):
     ref = CustomOracle(GBModel.gbmv2(box=box), TABULATED).energy_forces(g.positions, P)
     assert abs(E / ref["energy"] - 1) < E_TOL
     assert rel_rms(F, ref["forces"]) < F_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 64, 97])
+@pytest.mark.parametrize("cutoff", [0.0, 0.9])
+def test_tile_edges_vs_oracle(n, cutoff):
+    """The pair kernel's 32-particle tiles at ragged and exact sizes (a lone
+    particle, part tiles, whole tiles, a diagonal tile only), with
+    exclusions inside and across tiles and with a cutoff, against the
+    oracle."""
+    g = make_globule(max(n, 2), seed=300 + n)
+    pos = g.positions[:n]
+    P = np.stack([g.charge[:n], g.radius[:n]], axis=1)
+    # exclusions between tiles too: every 7th particle with the one 40 places on
+    excl = extended_exclusions(n) + [(i, i + 40) for i in range(0, n - 40, 7)]
+    ext = dict(EXTENDED, exclusions=excl)
+    m = GBModel.gbmv2(box=box_for(pos, margin=1.0), cutoff=cutoff)
+    ctx = CustomContext(m, n, ext)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(pos)
+    pd = ctx.param_derivs()
+    ref = CustomOracle(m, ext).energy_forces(pos, P)
+    tolE = E_TOL if cutoff == 0.0 else 1e-4  # pairs within FP32 rounding of the cutoff
+    assert abs(E / ref["energy"] - 1) < tolE, (E, ref["energy"])
+    assert rel_rms(F, ref["forces"]) < (F_TOL if cutoff == 0.0 else 1e-3)
+    assert np.abs(pd / ref["param_derivs"] - 1).max() < 1e-4
+    ctx.close()
