@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
   const float Cp = 10.0f * m.p1;
   for (int base = 0; base < P; base += kWarp) {
     // lane t prepares point base + t
+    int np;
     {
       const int k = base + lane;
       PointChain pc;
@@ -570,10 +571,14 @@ __global__ void __launch_bounds__(kCellThreads) gbmv_cell_chain_kernel(const flo
           pc.vz = bc2(vz);
         }
       }
-      pts[lane] = pc;
+      // only points with a nonzero factor pull on anything (a saturated
+      // solvent fraction gives exact zeros): they are packed in order, so
+      // the sums see the same nonzero terms in the same order
+      const unsigned lm = __ballot_sync(0xffffffffu, pc.cS != 0.0f);
+      if (pc.cS != 0.0f) pts[__popc(lm & ((1u << lane) - 1u))] = pc;
+      np = __popc(lm);
     }
     __syncwarp();
-    const int np = min(kWarp, P - base);
     for (int sub = 0; sub < np; sub += kChainPts) {
       const int t = sub + ps;
       const PointChain& pc = pts[t < np ? t : 0];
