@@ -473,9 +473,14 @@ __global__ void __launch_bounds__(kSymThreads, (CUTOFF || ADJ) ? 1 : 5) pair_sym
 
 // Pairs inside each i-block (i side only, each ordered pair once: lane t of
 // slot h broadcasts its atom to the warp) and the self terms 1/2 pref q^2 / B.
+// A warp per (i-block, slot h, half of the slot's lanes): the partial sums
+// are separate fixed-point reductions, so small systems get eight times the
+// warps.
+constexpr int kBlockSplit = 2;  // warps per broadcast slot
 template <bool CUTOFF, bool ADJ, bool PER = false>
 __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
-  const int b = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int b = wid / (kNI * kBlockSplit), h = (wid / kBlockSplit) % kNI, part = wid % kBlockSplit;
   const int lane = threadIdx.x % kWarp;
   if (b >= a.nblocks) return;
   PAtom I[kNI];
@@ -490,27 +495,32 @@ __global__ void __launch_bounds__(kSymThreads) pair_block_kernel(SymArgs a) {
     ai[u] = PAcc{0.f, 0.f, 0.f, 0.f, 0.f};
     e[u] = 0.0f;
   }
+  // slot h's atoms, selected without indexing the register array
+  PAtom src = I[0];
 #pragma unroll
-  for (int h = 0; h < kNI; ++h)
-    for (int t = 0; t < kWarp; ++t) {
-      const PAtom J{__shfl_sync(0xffffffffu, I[h].x, t), __shfl_sync(0xffffffffu, I[h].y, t),
-                    __shfl_sync(0xffffffffu, I[h].z, t), __shfl_sync(0xffffffffu, I[h].q, t),
-                    __shfl_sync(0xffffffffu, I[h].B, t), __shfl_sync(0xffffffffu, I[h].invB, t)};
+  for (int u = 1; u < kNI; ++u)
+    if (h == u) src = I[u];
+  for (int t = part * (kWarp / kBlockSplit); t < (part + 1) * (kWarp / kBlockSplit); ++t) {
+    const PAtom J{__shfl_sync(0xffffffffu, src.x, t), __shfl_sync(0xffffffffu, src.y, t),
+                  __shfl_sync(0xffffffffu, src.z, t), __shfl_sync(0xffffffffu, src.q, t),
+                  __shfl_sync(0xffffffffu, src.B, t), __shfl_sync(0xffffffffu, src.invB, t)};
 #pragma unroll
-      for (int u = 0; u < kNI; ++u)
-        if (h != u || t != lane)
-          gb_pair<false, CUTOFF, ADJ, PER>(I[u], pq[u], kD[u], kB[u], J, 0.f, a.pref, a.cutoff2, ai[u], dummy, e[u],
-                                           a.L, a.iL);
-    }
+    for (int u = 0; u < kNI; ++u)
+      if (h != u || t != lane)
+        gb_pair<false, CUTOFF, ADJ, PER>(I[u], pq[u], kD[u], kB[u], J, 0.f, a.pref, a.cutoff2, ai[u], dummy, e[u],
+                                         a.L, a.iL);
+  }
   double E = 0.0;
 #pragma unroll
   for (int u = 0; u < kNI; ++u) {
     PFixed su;
     su.add(ai[u]);
-    su.db += float_to_fixed(-0.5f * pq[u] * I[u].q * I[u].invB * I[u].invB);
-    if (ADJ) su.dq += float_to_fixed(pq[u] * I[u].invB);
+    if (h == 0 && part == 0) {  // the self terms, once
+      su.db += float_to_fixed(-0.5f * pq[u] * I[u].q * I[u].invB * I[u].invB);
+      if (ADJ) su.dq += float_to_fixed(pq[u] * I[u].invB);
+    }
     push_atom<ADJ>(a, kSymI * b + kWarp * u + lane, su);
-    E += 0.5 * (double)e[u] + 0.5 * (double)pq[u] * I[u].q * I[u].invB;
+    E += 0.5 * (double)e[u] + (h == 0 && part == 0 ? 0.5 * (double)pq[u] * I[u].q * I[u].invB : 0.0);
   }
   E = warp_sum(E);
   if (lane == 0 && E != 0.0) atomicAdd(a.energy, (unsigned long long)__double2ll_rn(E * kFixedScale));
@@ -744,7 +754,7 @@ gbx_status launch_pair(Context* ctx, const float4* pos, unsigned long long* forc
   a.tile_box = ctx->d_tile_box;
   a.perm = nullptr;
   const int wpb = kSymThreads / kWarp;
-  const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks + wpb - 1) / wpb;
+  const int gu = (a.nblocks * a.chunks + wpb - 1) / wpb, gb = (a.nblocks * kNI * kBlockSplit + wpb - 1) / wpb;
   cudaStream_t st = ctx->stream;
   cudaMemsetAsync(ctx->d_energy_fx, 0, sizeof(unsigned long long), st);
   if (ctx->cfg.periodic) {

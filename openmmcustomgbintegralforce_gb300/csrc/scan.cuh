@@ -49,6 +49,11 @@ __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int* __r
                                                                   int* __restrict__ block_sums, long long cell_cap) {
   __shared__ int s_warp[kWarp];
   const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
+  // the grid covers the capacity; tiles past this geometry's cells hold nothing
+  if ((long long)blockIdx.x * kScanThreads * kScanItems >= ncell && blockIdx.x > 0) {
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = 0;
+    return;
+  }
   const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
   int v = 0;
   for (int k = 0; k < kScanItems; ++k)
@@ -84,6 +89,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* __r
                                                                   unsigned* __restrict__ status) {
   __shared__ int s_warp[kWarp];
   const long long ncell = gp->ncell <= cell_cap ? gp->ncell : 0;
+  if ((long long)blockIdx.x * kScanThreads * kScanItems >= ncell && blockIdx.x > 0) return;  // past the cells
   const long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
   int v[kScanItems];
   int sum = 0;
