@@ -6,7 +6,7 @@ is outside it: a per-atom scale of the Born radius through a second computed
 value, the solvent dielectric as a global parameter, an ACE-style nonpolar
 single-particle term and a Lepton definition in the pair term.  EXTENDED
 adds coordinates, exclusions and energy parameter derivatives; TABULATED
-calls tabulated functions.
+calls tabulated functions; FUNCTIONS uses the Lepton function set.
 """
 from openmmcustomgbintegralforce_gb300.spec import ONE_4PI_EPS0
 
@@ -100,4 +100,23 @@ TABULATED = {
               (f"-{K}*(1-1/80)*q1*q2/sqrt(r^2+Bt1*Bt2*exp(-r^2/(4*Bt1*Bt2)))", 2),
               ("q1*q2*tail(r)", 2)],
     "functions": tabulated_functions(),
+}
+
+
+# The Lepton function set in a computed value, a single-particle term and a
+# pair term (smooth where the globule's values fall, so central differences
+# and FP32 both apply).
+FUNCTIONS = {
+    "params": ["q", "radius"],
+    "globals": {"alpha0": -0.180, "alpha1": 1.817},
+    "integrals": [("I4", 4), ("I7", 7)],
+    "values": [("B", "1/(alpha0*(1/0.05-I4)+alpha1*(1/(4*0.05^4)-I7)^(1/4))"),
+               ("Bf", "B*(1+0.05*erf(q))*(1+0.02*tanh(B-0.3))")],
+    "terms": [(f"-0.5*{K}*(1-1/80)*q^2/Bf", 0),
+              ("0.01*(abs(q) + step(q)*square(q) + select(step(radius-0.15), 1, 2)*sqrt(radius)"
+               " + min(radius, 0.16) + max(radius, 0.14) + log(radius) + exp(-radius) + sin(radius)"
+               " + cos(radius) + atan(radius) + cosh(radius)/sinh(radius+1) + recip(radius+1)"
+               " + cube(radius) + erfc(radius) + tan(radius) + asin(radius) + acos(radius))", 0),
+              (f"-{K}*(1-1/80)*q1*q2/sqrt(r^2+Bf1*Bf2*exp(-r^2/(4*Bf1*Bf2)))", 2),
+              ("0.01*q1*q2*exp(-r)*(1+0.1*cos(3*r))*atan(Bf1+Bf2) + 0.001*erfc(r)*min(Bf1, Bf2)", 2)],
 }

@@ -82,7 +82,8 @@ def parse(text: str, names, functions=None) -> sp.Expr:
 
 
 def _lam(e, syms):
-    return sp.lambdify(syms, e, modules=[{"Heaviside": lambda x, h=1: np.heaviside(x, h)}, "numpy"])
+    # scipy supplies the array forms of erf and erfc
+    return sp.lambdify(syms, e, modules=[{"Heaviside": lambda x, h=1: np.heaviside(x, h)}, "numpy", "scipy"])
 
 
 def _ev(e, env, count):

@@ -15,7 +15,7 @@ from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle import oracle as O
 from oracle.custom import CustomOracle
-from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, TABULATED,
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, FUNCTIONS, MODIFIED, TABULATED,
                                                                extended_exclusions, modified_params)
 
 
@@ -118,10 +118,29 @@ def test_tabulated_expressions_gradients(glob):
     assert f(np.array([hi + 0.1, lo - 0.1])).tolist() == [0.0, 0.0]  # zero outside
 
 
+def test_function_set_gradients(glob):
+    """The Lepton function set (FUNCTIONS): forces against FP64 central
+    differences of the oracle's energy."""
+    g = glob
+    m = GBModel.gbmv2(box=box_for(g.positions, margin=1.0))
+    P = np.stack([g.charge, g.radius], axis=1)
+    orc = CustomOracle(m, FUNCTIONS)
+    F = orc.energy_forces(g.positions, P)["forces"]
+    rng = np.random.default_rng(7)
+    h = 1e-6
+    for flat in rng.choice(3 * g.n, size=6, replace=False):
+        i, d = int(flat) // 3, int(flat) % 3
+        xp, xm = g.positions.copy(), g.positions.copy()
+        xp[i, d] += h
+        xm[i, d] -= h
+        fd = -(orc.energy_forces(xp, P)["energy"] - orc.energy_forces(xm, P)["energy"]) / (2 * h)
+        assert abs(fd - F[i, d]) <= 1e-6 * np.abs(F).max() + 1e-5 * abs(F[i, d]), (i, d, fd, F[i, d])
+
+
 def test_library_compiles_and_refuses_expression_sets():
     from openmmcustomgbintegralforce_gb300._lib import check_custom
 
-    for s in (CANONICAL, MODIFIED, dict(EXTENDED, exclusions=extended_exclusions(50)), TABULATED):
+    for s in (CANONICAL, MODIFIED, dict(EXTENDED, exclusions=extended_exclusions(50)), TABULATED, FUNCTIONS):
         st, msg = check_custom(s)
         if st == 4 and "NVRTC" in msg:
             pytest.skip("NVRTC not available")

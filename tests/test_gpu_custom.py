@@ -12,6 +12,8 @@ through the C ABI, against the FP64 custom-expression oracle
   (addEnergyParameterDerivative);
 * tabulated functions (Continuous1DFunction) in a computed value, a
   single-particle term and a pair term;
+* the Lepton function set (FP64 in the values and single-particle terms,
+  FP32 fast math in the pair terms);
 * the pair kernel's tile edges: 1, 2, 31, 33, 64 and 97 particles with
   exclusions inside and across tiles, with and without a cutoff;
 * a global parameter update, bit-reproducible calls, and a refused
@@ -29,7 +31,7 @@ from openmmcustomgbintegralforce_gb300._lib import Context, CustomContext, GBXEr
 from openmmcustomgbintegralforce_gb300.globule import make_globule
 from openmmcustomgbintegralforce_gb300.spec import GBModel, box_for
 from oracle.custom import CustomOracle
-from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, MODIFIED, TABULATED,
+from openmmcustomgbintegralforce_gb300.expression_sets import (CANONICAL, EXTENDED, FUNCTIONS, MODIFIED, TABULATED,
                                                                extended_exclusions, modified_params)
 
 pytestmark = pytest.mark.gpu
@@ -313,4 +315,21 @@ def test_tile_edges_vs_oracle(n, cutoff):
     assert abs(E / ref["energy"] - 1) < tolE, (E, ref["energy"])
     assert rel_rms(F, ref["forces"]) < (F_TOL if cutoff == 0.0 else 1e-3)
     assert np.abs(pd / ref["param_derivs"] - 1).max() < 1e-4
+    ctx.close()
+
+
+@pytest.mark.parametrize("cls", ["gbmv2", "gbsw_integral"])
+def test_function_set_vs_oracle(glob, cls):
+    """Every Lepton function in generated code against the oracle."""
+    g = glob
+    m = model_of(cls, g)
+    P = np.stack([g.charge, g.radius], axis=1)
+    ctx = CustomContext(m, g.n, FUNCTIONS)
+    ctx.set_custom_parameters(P)
+    E, F = ctx.execute_host(g.positions)
+    ref = CustomOracle(m, FUNCTIONS).energy_forces(g.positions, P)
+    print(f"{cls} functions: energy {abs(E / ref['energy'] - 1):.2e} forces {rel_rms(F, ref['forces']):.2e}")
+    assert abs(E / ref["energy"] - 1) < E_TOL
+    assert rel_rms(F, ref["forces"]) < F_TOL
+    assert np.abs(ctx.born_radii() / ref["values"][0] - 1).max() < B_TOL
     ctx.close()
