@@ -175,10 +175,14 @@ gbx_status upload_quadrature(Context* ctx) {
 }
 
 // The volume kernels run one warp per (atom, chunk of quadrature points)
-// with lanes over points: enough warps for ~48 per SM on the device's SMs,
-// and >= 64 points (2 per lane) per chunk.
+// with lanes over points: enough warps for ~48 per SM on the device's SMs;
+// chunks of at most 896 points while that keeps under ~400 warps per SM (a
+// whole 32 x 110 atom per warp left the last waves ragged: buried and
+// surface atoms differ several-fold in work; measured best at 4 chunks for
+// 10,000 atoms and 2 for 50,000); >= 64 points (2 per lane) per chunk.
 int choose_chunks(int n, int Q, int sms) {
   int c = (sms * 48 + n - 1) / n;
+  c = std::max(c, std::min((Q + 895) / 896, (sms * 400 + n - 1) / n));
   c = std::max(1, std::min(c, std::max(1, Q / 64)));
   return c;
 }
