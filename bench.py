@@ -78,11 +78,11 @@ FLOPS_PAIR = 39.0
 
 # DRAM bytes (read + write) per step of each stage's kernels, from one ncu
 # capture of the same workload and build (the files named in TRAFFIC_SOURCE).
-TRAFFIC = {"gbsw50k": {"integrals": 2353.1e6, "pair": 3.09e6 + 3.03e6, "chain_rule": 1089.3e6,
+TRAFFIC = {"gbsw50k": {"integrals": 1628.5e6 + 715.5e6, "pair": 3.0e6 + 3.0e6, "chain_rule": 1106.8e6,
                        "lookup_table": 180.0e6 + 146.6e6 + 5.5e6 + 9.6e6},
-           "gbmv10k": {"integrals": 405.2e6 + 48.0e6, "chain_rule": 291.7e6, "point_binning": 89.0e6 + 145.2e6,
+           "gbmv10k": {"integrals": 404.7e6 + 48.0e6, "chain_rule": 291.8e6, "point_binning": 93.0e6 + 153.1e6,
                        "pair": 0.63e6 + 0.63e6},
-           "gbmv1_10k": {"integrals": 211.4e6 + 48.0e6, "chain_rule": 127.4e6, "point_binning": 85.8e6 + 144.0e6,
+           "gbmv1_10k": {"integrals": 211.0e6 + 48.0e6, "chain_rule": 127.1e6, "point_binning": 89.7e6 + 151.1e6,
                          "pair": 0.63e6 + 0.62e6}}
 TRAFFIC_SOURCE = {"gbsw50k": "profiles/launches_gbsw50k.md", "gbmv10k": "profiles/launches_gbmv10k.md",
                   "gbmv1_10k": "profiles/launches_gbmv1_10k.md"}
