@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_kernel(PairArgs a) {
 // ---------------------------------------------------------------------------
 constexpr int kNI = 4;          // i-atoms per lane
 constexpr int kSymI = kWarp * kNI;  // atoms per i-block (one warp)
-constexpr int kSymChunkMax = 16;  // j-tiles per warp unit, at most
+constexpr int kSymChunkMax = 8;  // j-tiles per warp unit, at most (16 and 32 measured slower at 50k: ragged tails)
 constexpr int kSymThreads = 128;
 
 struct SymArgs {
