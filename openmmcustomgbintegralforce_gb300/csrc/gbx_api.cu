@@ -233,6 +233,7 @@ gbx_status alloc_atom_buffers(Context* ctx) {
   GBX_TRY(dalloc(ctx, &ctx->d_status, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_work, 4));
   GBX_TRY(dalloc(ctx, &ctx->d_rmax, 1));
+  GBX_TRY(dalloc(ctx, &ctx->d_next_item, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_geom, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_tgeom, 1));
   GBX_TRY(dalloc(ctx, &ctx->d_wgeom, 1));
@@ -777,7 +778,7 @@ gbx_status gbx_destroy(gbx_context* handle) {
                   ctx->d_energy, ctx->d_dEdR_fx, ctx->d_dEdq_fx, ctx->d_alpha_grad, ctx->d_status, ctx->d_work,
                   ctx->d_tgeom, ctx->d_wgeom, ctx->d_tcount, ctx->d_tstart, ctx->d_tcursor, ctx->d_tburied,
                   ctx->d_tblock_sums, ctx->d_tentry, ctx->d_tindex, ctx->d_entry4, ctx->d_entry_par,
-                  ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
+                  ctx->d_cell2, ctx->d_tcell, ctx->d_tfirst, ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->d_next_item, ctx->d_energy_fx, ctx->d_tile_box, ctx->d_perm,
                   ctx->d_perm_tmp, ctx->d_cell_of, ctx->d_scount, ctx->d_sstart, ctx->d_scursor, ctx->d_sgeom, ctx->d_pstate,
                   ctx->d_pcell, ctx->d_prank, ctx->d_porder, ctx->d_sval, ctx->d_pcount, ctx->d_pstart,
                   ctx->d_pblock_sums, ctx->d_pgeom, ctx->d_slot_of, ctx->d_pub};

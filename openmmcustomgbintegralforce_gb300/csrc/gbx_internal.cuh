@@ -200,6 +200,8 @@ struct Context {
   long long srec_warps = 0;      // warps the buffer was sized for
   int* d_rcount = nullptr;       // [warps] records written, or -1 - needed
   unsigned* d_rmax = nullptr;    // largest per-warp need of the call
+  unsigned* d_next_item = nullptr;  // the GBSW integral pass's (atom, chunk) work counter
+  int integral_grid = 0;            // its persistent grid: resident blocks on all SMs
   unsigned* h_rmax = nullptr;    // pinned copy of the last d_rmax
   unsigned* h_status = nullptr;  // pinned: status word of the last host-path call
   double* h_energy = nullptr;    // pinned: energy of the last host-path call

@@ -410,22 +410,30 @@ static_assert(kRefillBelow - 1 + kRefill <= kStage, "ring overwrite");
 constexpr int kEnt = 2;            // list entries per lane step, loaded one step ahead (3 and 4 measured slower)
 static_assert(kEnt == 2, "the exact table's lists are read in aligned pairs");
 
+// Persistent: a grid of resident blocks whose warps take (atom, chunk) items
+// from `next_item` one at a time, so a warp that finishes a cheap item (a
+// buried or exposed atom) takes the next instead of idling until the slowest
+// warp of its block is done.  Each item's results depend on the item alone.
 template <class Q, bool EMIT>
 __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* __restrict__ pos, int n, Entries tab,
                                                                  Quad quad, ModelConst m, int chunk, int n_chunks,
-                                                                 float* __restrict__ Jpart, ShellSink sink) {
+                                                                 float* __restrict__ Jpart, ShellSink sink,
+                                                                 unsigned* __restrict__ next_item) {
   __shared__ int3 s_queue[kThreads / kWarp][kStage];  // (q, list start, list length)
   __shared__ int s_long[kThreads / kWarp];  // a shaping entry beyond list position 63
   // the exact table: lists start at even entries and each cell's record sits
   // beside its first entry, so both are read 32 bytes at a time
   constexpr bool kTight = IsTight<Q>::value;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x % kWarp;
   const int wib = threadIdx.x / kWarp;
   const unsigned lt = (1u << lane) - 1u;
+  for (;;) {
+  unsigned item = 0;
+  if (lane == 0) item = atomicAdd(next_item, 1u);
+  const int warp = (int)__shfl_sync(0xffffffffu, item, 0);
+  if (warp >= n * n_chunks) return;
   if (lane == 0) s_long[wib] = 0;
   __syncwarp();
-  if (warp >= n * n_chunks) return;
   int3* queue = s_queue[wib];
   int fill = 0;  // warp-uniform: points recorded so far (may exceed R)
   const int i = warp % n, c = warp / n;
@@ -614,6 +622,8 @@ __global__ void __launch_bounds__(kThreads) gbsw_integral_kernel(const float4* _
       sink.count[warp] = fill <= sink.R && !s_long[wib] ? fill : -1 - fill;
       if (fill > 0) atomicMax(sink.max_seen, (unsigned)fill);
     }
+  }
+  __syncwarp();  // the ring and the long-list flag are reused by the next item
   }
 }
 
@@ -1070,12 +1080,25 @@ void launch_integrals_t(Context* ctx, const float4* pos, const ModelConst& m, bo
   const Quad qd{ctx->d_qv, ctx->d_qw, ctx->d_qoff};
   const int chunk = (m.nq + ctx->n_chunks - 1) / ctx->n_chunks;
   const ShellSink sink{ctx->d_srec, ctx->d_srec_st, ctx->d_rcount, ctx->d_rmax, ctx->srec_R};
-  if (MODEL == GBX_MODEL_GBSW && ctx->records && !count_work)
-    gbsw_integral_kernel<Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
-        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
-  else if (MODEL == GBX_MODEL_GBSW && !count_work)
-    gbsw_integral_kernel<Q, false><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
-        pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, sink);
+  if (MODEL == GBX_MODEL_GBSW && !count_work) {
+    // persistent grid: the resident blocks of every SM (or fewer, for few items)
+    if (ctx->integral_grid == 0) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gbsw_integral_kernel<Q, true>, kThreads, 0) !=
+              cudaSuccess ||
+          per_sm < 1)
+        per_sm = 1;
+      ctx->integral_grid = per_sm * ctx->sms;
+    }
+    const int grid = std::min(volume_blocks(ctx), ctx->integral_grid);
+    cudaMemsetAsync(ctx->d_next_item, 0, sizeof(unsigned), ctx->stream);
+    if (ctx->records)
+      gbsw_integral_kernel<Q, true><<<grid, kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk, ctx->n_chunks,
+                                                                         ctx->d_J, sink, ctx->d_next_item);
+    else
+      gbsw_integral_kernel<Q, false><<<grid, kThreads, 0, ctx->stream>>>(pos, ctx->n, t, qd, m, chunk, ctx->n_chunks,
+                                                                          ctx->d_J, sink, ctx->d_next_item);
+  }
   else if (count_work)
     integral_kernel<MODEL, Q, true><<<volume_blocks(ctx), kThreads, 0, ctx->stream>>>(
         pos, ctx->n, t, qd, m, chunk, ctx->n_chunks, ctx->d_J, ctx->d_work, ctx->d_pstate);
