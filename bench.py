@@ -78,7 +78,7 @@ FLOPS_PAIR = 39.0
 
 # DRAM bytes (read + write) per step of each stage's kernels, from one ncu
 # capture of the same workload and build (the files named in TRAFFIC_SOURCE).
-TRAFFIC = {"gbsw50k": {"integrals": 1628.5e6 + 715.5e6, "pair": 3.0e6 + 3.0e6, "chain_rule": 1106.8e6,
+TRAFFIC = {"gbsw50k": {"integrals": 1689.1e6 + 715.5e6, "pair": 3.0e6 + 3.0e6, "chain_rule": 1107.7e6,
                        "lookup_table": 180.0e6 + 146.6e6 + 5.5e6 + 9.6e6},
            "gbmv10k": {"integrals": 404.7e6 + 48.0e6, "chain_rule": 291.8e6, "point_binning": 93.0e6 + 153.1e6,
                        "pair": 0.63e6 + 0.63e6},
