@@ -576,11 +576,13 @@ def measure_config(name, steps, jitter_A, dev, flush):
         # host arrays in, every gradient out
         ctx.adjoint(x)
         t = []
-        for _ in range(5):
+        for _ in range(20):
             t0 = time.perf_counter()
             got = ctx.adjoint(x)
             t.append(time.perf_counter() - t0)
-        res["e2e"] = {"evals_per_s": 1.0 / float(np.mean(t)), "call": "gbx_adjoint_host"}
+        # the median: a single host-side hiccup among a few sub-millisecond calls moved the mean by a quarter
+        res["e2e"] = {"evals_per_s": 1.0 / float(np.median(t)), "call": "gbx_adjoint_host",
+                      "calls": len(t), "statistic": "median"}
         t0 = time.perf_counter()
         ref = O.Oracle(model, nthreads=os.cpu_count() or 1).energy_forces(x, g.charge, g.radius, adjoint=True)
         dt = time.perf_counter() - t0
